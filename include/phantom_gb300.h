@@ -1,0 +1,157 @@
+/*
+ * phantom_gb300.h — C ABI of the GB300-native RNS ciphertext-arithmetic library.
+ *
+ * This is the drop-in boundary for PhantomFHE's hot path.  The reference ships a C++
+ * source API (include/phantom.h, include/evaluate.cuh) with no C ABI of its own; every
+ * entry point below names the reference interface it replaces (file:line in the
+ * PhantomFHE tree).  The C++ compatibility layer (phantom-fhe_gb300/cpp/phantom.h) and the
+ * Python bindings sit on top of these calls.
+ *
+ * Conventions
+ *  - All ciphertext / key pointers are DEVICE pointers; layout is the reference's:
+ *    ciphertext = [size][coeff_modulus_size][N] uint64 limb-major (include/ciphertext.h:44-72),
+ *    key-switching key = dnum device pointers (a device array, as returned by
+ *    PhantomRelinKey::public_keys_ptr(), include/secretkey.h:124-127), each to [2][QP][N]
+ *    in NTT form.
+ *  - `chain_index` follows the reference: 0 is the key level (QP), 1 the full data level Q,
+ *    each further index drops one prime (src/context.cu:141-158).
+ *  - Calls enqueue work on `stream` (a cudaStream_t; NULL = the legacy default stream) and
+ *    return without synchronising.  Calls never allocate device memory: scratch comes from an
+ *    fhe_workspace, which must not be shared by two calls that can run concurrently.
+ *  - Return value: FHE_OK or a negative status.  FHE_ERR_INVALID_ARGUMENT and FHE_ERR_LOGIC
+ *    correspond to the std::invalid_argument / std::logic_error the reference throws;
+ *    fhe_last_error() returns the message of the calling thread's last failure.
+ */
+#ifndef PHANTOM_GB300_H
+#define PHANTOM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FHE_OK 0
+#define FHE_ERR_INVALID_ARGUMENT (-1)
+#define FHE_ERR_LOGIC (-2)
+#define FHE_ERR_CUDA (-3)
+#define FHE_ERR_OUT_OF_MEMORY (-4)
+#define FHE_ERR_UNSUPPORTED (-5)
+
+/* scheme_type and mul_tech_type values of include/host/encryptionparams.h */
+#define FHE_SCHEME_BFV 1
+#define FHE_SCHEME_CKKS 2
+#define FHE_MUL_TECH_HPS 2
+
+typedef struct fhe_context fhe_context;
+typedef struct fhe_workspace fhe_workspace;
+
+/* Mirrors phantom::EncryptionParameters (include/host/encryptionparams.h:12-246). */
+typedef struct fhe_params {
+    int scheme;                     /* FHE_SCHEME_* */
+    int mul_tech;                   /* FHE_MUL_TECH_HPS for BFV; ignored for CKKS */
+    uint64_t poly_modulus_degree;   /* N, a power of two in [2^12, 2^17] */
+    const uint64_t *coeff_modulus;  /* QP: data primes Q first, then special primes P */
+    size_t coeff_modulus_size;
+    size_t special_modulus_size;    /* |P| = alpha */
+    uint64_t plain_modulus;         /* BFV t; 0 for CKKS */
+    const uint32_t *galois_elts;    /* NULL/0: all power-of-two rotations (src/galois.cu:41-65) */
+    size_t galois_elts_size;
+} fhe_params;
+
+const char *fhe_last_error(void);
+
+/* CoeffModulus::Create (include/host/modulus.h:295, src/host/modulus.cu:80-111). */
+int fhe_create_coeff_modulus(uint64_t poly_modulus_degree, const int *bit_sizes, size_t count, uint64_t *out);
+
+/* phantom::util::get_elt_from_step (include/galois.cuh:16-49).  Returns 0 on error. */
+uint32_t fhe_galois_elt_from_step(int step, uint64_t poly_modulus_degree);
+
+/* PhantomContext::PhantomContext(const EncryptionParameters&) (include/context.cuh:161,
+ * src/context.cu:121-232): builds and uploads every table. */
+int fhe_context_create(const fhe_params *params, fhe_context **out);
+void fhe_context_destroy(fhe_context *ctx);
+
+/* Sizes of a context: N, |Q|, |P|, |R| (BFV HPS base, else 0), dnum = ceil(|Q|/|P|). */
+int fhe_context_sizes(const fhe_context *ctx, uint64_t *n, size_t *size_q, size_t *size_p, size_t *size_r,
+                      size_t *dnum);
+/* The context's prime list (QP then R); `out` holds at least |Q|+|P|+|R| words. */
+int fhe_context_moduli(const fhe_context *ctx, uint64_t *out);
+/* The Galois elements the context was built with (PhantomGaloisTool::galois_elts_). */
+int fhe_context_galois_elts(const fhe_context *ctx, uint32_t *out, size_t *count);
+
+/* Scratch for the evaluator calls (replaces the reference's per-call cudaMallocAsync,
+ * src/eval_key_switch.cu:143-181).  Sized for the key level. */
+size_t fhe_workspace_bytes(const fhe_context *ctx);
+int fhe_workspace_create(const fhe_context *ctx, fhe_workspace **out);
+void fhe_workspace_destroy(fhe_workspace *ws);
+
+/* nwt_2d_radix8_forward_inplace / nwt_2d_radix8_backward_inplace (include/ntt.cuh:157-226):
+ * in-place transform of `num_polys` polynomials of `coeff_modulus_size` limbs each
+ * (contiguous), limb k using prime start_modulus_idx + k of the context's QP list.
+ * For BFV contexts, indices >= |Q|+|P| address the HPS base R. */
+int fhe_ntt_forward(const fhe_context *ctx, uint64_t *data, size_t num_polys, size_t coeff_modulus_size,
+                    size_t start_modulus_idx, void *stream);
+int fhe_ntt_inverse(const fhe_context *ctx, uint64_t *data, size_t num_polys, size_t coeff_modulus_size,
+                    size_t start_modulus_idx, void *stream);
+
+/* bgv_ckks_multiply (src/evaluate.cu:345-397): CKKS tensor product.  ct1 holds 3
+ * polynomials of capacity (the first two are the input), ct2 two; ct1 == ct2 squares. */
+int fhe_ckks_multiply(const fhe_context *ctx, uint64_t *ct1, const uint64_t *ct2, size_t chain_index,
+                      void *stream);
+
+/* keyswitch_inplace (include/evaluate.cuh:29, src/eval_key_switch.cu:95-182):
+ * ct (2 polynomials at chain_index) += KeySwitch(c2) under evk. */
+int fhe_keyswitch(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, const uint64_t *c2,
+                  size_t chain_index, const uint64_t *const *evk, void *stream);
+
+/* relinearize_inplace (include/evaluate.cuh:125, src/evaluate.cu:1342-1374): ct holds 3
+ * polynomials; on return its first two are the relinearised ciphertext. */
+int fhe_relinearize(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t chain_index,
+                    const uint64_t *const *rlk, void *stream);
+
+/* multiply_and_relin_inplace (include/evaluate.cuh:115, src/evaluate.cu:1061-1104).
+ * CKKS: ct1 (2 polys, NTT form) *= ct2, relinearised, written to ct1.  The tensor product is
+ * fused into the key switch and never materialised, so ct1 needs room for 2 polynomials only.
+ * BFV (mul_tech hps, src/evaluate.cu:820-1026): ct1, ct2 in coefficient form at chain 1. */
+int fhe_multiply_and_relin(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct1, const uint64_t *ct2,
+                           size_t chain_index, const uint64_t *const *rlk, void *stream);
+
+/* rescale_to_next (include/evaluate.cuh:137-140, src/evaluate.cu:1545-1565 via
+ * DRNSTool::divide_and_round_q_last_ntt, src/rns.cu:1160-1184): in (size polys at
+ * chain_index) -> out (size polys at chain_index + 1).  in and out may not overlap. */
+int fhe_rescale_to_next(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *in, uint64_t *out, size_t size,
+                        size_t chain_index, void *stream);
+
+/* mod_switch_to_next for BFV (src/rns.cu:1082-1126): coefficient-domain divide by q_last. */
+int fhe_bfv_mod_switch_to_next(const fhe_context *ctx, const uint64_t *in, uint64_t *out, size_t size,
+                               size_t chain_index, void *stream);
+
+/* HMult + relinearise + rescale as one call (multiply_and_relin_inplace followed by
+ * rescale_to_next_inplace, src/evaluate.cu:1061-1104 and 1545-1565): out (2 polys at
+ * chain_index + 1) = Rescale(Relin(ct1 * ct2)).  Bit-identical to the two-call sequence. */
+int fhe_ckks_multiply_relin_rescale(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *ct1,
+                                    const uint64_t *ct2, uint64_t *out, size_t chain_index,
+                                    const uint64_t *const *rlk, void *stream);
+
+/* apply_galois_inplace (include/evaluate.cuh:215, src/evaluate.cu:1567-1630), CKKS:
+ * ct (2 polys) <- KeySwitch of the automorphism X -> X^galois_elt under gk. */
+int fhe_apply_galois(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t chain_index,
+                     uint32_t galois_elt, const uint64_t *const *gk, void *stream);
+
+/* rotate_inplace (include/evaluate.cuh:225, src/evaluate.cu:1633-1668), CKKS: rotation by
+ * `step` slots; when no key exists for the step's element, the NAF decomposition of the
+ * step is applied key by key.  galois_keys[i] is the key of the context's i-th element. */
+int fhe_rotate(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t chain_index, int step,
+               const uint64_t *const *const *galois_keys, void *stream);
+
+/* hoisting_inplace (include/evaluate.cuh:237, src/evaluate.cu:1670-1865), CKKS:
+ * ct <- sum over steps of rotate(ct, step), sharing one mod-up of c1. */
+int fhe_hoisting(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t chain_index, const int *steps,
+                 size_t num_steps, const uint64_t *const *const *galois_keys, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -176,6 +176,16 @@ class Context:
         lib().orc_ntt_inv(self._h, p64(data), limbs, t)
         return data
 
+    def ntt_fwd_qr(self, data):
+        data = np.ascontiguousarray(data, dtype=np.uint64).copy()
+        lib().orc_ntt_fwd_qr(self._h, p64(data), data.size // self.n)
+        return data
+
+    def ntt_inv_qr(self, data):
+        data = np.ascontiguousarray(data, dtype=np.uint64).copy()
+        lib().orc_ntt_inv_qr(self._h, p64(data), data.size // self.n)
+        return data
+
     def tensor(self, l, a, b):
         out = np.zeros((3, l, self.n), dtype=np.uint64)
         if a is b:

@@ -1,0 +1,389 @@
+// capi.cu — the extern "C" boundary (include/phantom_gb300.h): argument checks with the
+// reference's error classes, chain-index bookkeeping, and dispatch to the kernels.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+
+#include "context.cuh"
+#include "host_tables.hpp"
+#include "ops.hpp"
+#include "phantom_gb300.h"
+
+struct fhe_context {
+    std::unique_ptr<pfg::Context> c;
+};
+
+struct fhe_workspace {
+    const fhe_context *ctx = nullptr;
+    uint64_t *base = nullptr;
+    size_t words = 0;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct Status {
+    int code;
+    std::string msg;
+};
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+// Runs `body`, translating the reference's exception classes into status codes; with
+// `launches` it also checks that every kernel launch the body made was accepted.
+template <class F>
+int guarded(F &&body, bool launches = true) {
+    try {
+        body();
+        if (launches) {
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return fail(FHE_ERR_CUDA, std::string("CUDA error: ") + cudaGetErrorString(e));
+        }
+        return FHE_OK;
+    } catch (const std::invalid_argument &e) {
+        return fail(FHE_ERR_INVALID_ARGUMENT, e.what());
+    } catch (const std::logic_error &e) {
+        return fail(FHE_ERR_LOGIC, e.what());
+    } catch (const std::bad_alloc &) {
+        return fail(FHE_ERR_OUT_OF_MEMORY, "out of host memory");
+    } catch (const std::runtime_error &e) {
+        return fail(FHE_ERR_CUDA, e.what());
+    } catch (...) {
+        return fail(FHE_ERR_LOGIC, "unknown error");
+    }
+}
+
+struct unsupported : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+const pfg::Context &ctx_of(const fhe_context *ctx) {
+    if (!ctx || !ctx->c) throw std::invalid_argument("context is null");
+    return *ctx->c;
+}
+
+// chain index -> number of data limbs (src/context.cu:141-158)
+int level_of(const pfg::Context &c, size_t chain_index) {
+    if (chain_index < 1 || chain_index > (size_t)c.nQ) throw std::invalid_argument("chain_index out of range");
+    return c.nQ - (int)(chain_index - 1);
+}
+
+pfg::Workspace ws_of(const fhe_context *ctx, fhe_workspace *ws) {
+    if (!ws || !ws->base) throw std::invalid_argument("workspace is null");
+    if (ws->ctx != ctx) throw std::invalid_argument("workspace belongs to another context");
+    return pfg::Workspace{ws->base, ws->words};
+}
+
+void need_ptr(const void *p, const char *what) {
+    if (!p) throw std::invalid_argument(std::string(what) + " is null");
+}
+
+void need_keyswitching(const pfg::Context &c) {
+    if (c.nP == 0) throw std::logic_error("key switching needs special primes (special_modulus_size > 0)");
+}
+
+cudaStream_t st(void *s) { return static_cast<cudaStream_t>(s); }
+
+}  // namespace
+
+extern "C" {
+
+const char *fhe_last_error(void) { return g_last_error.c_str(); }
+
+int fhe_create_coeff_modulus(uint64_t poly_modulus_degree, const int *bit_sizes, size_t count, uint64_t *out) {
+    return guarded([&] {
+        need_ptr(bit_sizes, "bit_sizes");
+        need_ptr(out, "out");
+        if (poly_modulus_degree < 2 || (poly_modulus_degree & (poly_modulus_degree - 1)))
+            throw std::invalid_argument("poly_modulus_degree is invalid");
+        auto v = pfg::host::create_coeff_modulus(poly_modulus_degree, std::vector<int>(bit_sizes, bit_sizes + count));
+        std::copy(v.begin(), v.end(), out);
+    }, false);
+}
+
+uint32_t fhe_galois_elt_from_step(int step, uint64_t poly_modulus_degree) {
+    try {
+        return pfg::host::elt_from_step(step, poly_modulus_degree);
+    } catch (const std::exception &e) {
+        g_last_error = e.what();
+        return 0;
+    }
+}
+
+int fhe_context_create(const fhe_params *p, fhe_context **out) {
+    return guarded([&] {
+        need_ptr(p, "params");
+        need_ptr(out, "out");
+        need_ptr(p->coeff_modulus, "coeff_modulus");
+        std::vector<uint64_t> mods(p->coeff_modulus, p->coeff_modulus + p->coeff_modulus_size);
+        std::vector<uint32_t> elts;
+        if (p->galois_elts && p->galois_elts_size) elts.assign(p->galois_elts, p->galois_elts + p->galois_elts_size);
+        auto c = pfg::make_context(p->scheme, p->mul_tech, p->poly_modulus_degree, mods,
+                                   (int)p->special_modulus_size, p->plain_modulus, elts);
+        *out = new fhe_context{std::move(c)};
+    });
+}
+
+void fhe_context_destroy(fhe_context *ctx) { delete ctx; }
+
+int fhe_context_sizes(const fhe_context *ctx, uint64_t *n, size_t *size_q, size_t *size_p, size_t *size_r,
+                      size_t *dnum) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        if (n) *n = c.n;
+        if (size_q) *size_q = c.nQ;
+        if (size_p) *size_p = c.nP;
+        if (size_r) *size_r = c.nR;
+        if (dnum) *dnum = c.nP ? c.beta(c.nQ) : 0;
+    }, false);
+}
+
+int fhe_context_moduli(const fhe_context *ctx, uint64_t *out) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        need_ptr(out, "out");
+        std::copy(c.mods.begin(), c.mods.end(), out);
+    }, false);
+}
+
+int fhe_context_galois_elts(const fhe_context *ctx, uint32_t *out, size_t *count) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        need_ptr(count, "count");
+        if (out) std::copy(c.galois_elts.begin(), c.galois_elts.end(), out);
+        *count = c.galois_elts.size();
+    }, false);
+}
+
+size_t fhe_workspace_bytes(const fhe_context *ctx) {
+    if (!ctx || !ctx->c) return 0;
+    return pfg::workspace_words(*ctx->c) * sizeof(uint64_t);
+}
+
+int fhe_workspace_create(const fhe_context *ctx, fhe_workspace **out) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        need_ptr(out, "out");
+        auto *w = new fhe_workspace;
+        w->ctx = ctx;
+        w->words = pfg::workspace_words(c);
+        cudaError_t e = cudaMalloc(&w->base, w->words * sizeof(uint64_t));
+        if (e != cudaSuccess) {
+            delete w;
+            cudaGetLastError();
+            throw std::bad_alloc();
+        }
+        *out = w;
+    });
+}
+
+void fhe_workspace_destroy(fhe_workspace *ws) {
+    if (!ws) return;
+    if (ws->base) cudaFree(ws->base);
+    delete ws;
+}
+
+static int ntt_common(const fhe_context *ctx, uint64_t *data, size_t num_polys, size_t size, size_t start,
+                      void *stream, bool fwd) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        need_ptr(data, "data");
+        if (size == 0 || num_polys == 0) return;
+        if (start + size > c.mods.size()) throw std::invalid_argument("modulus index out of range");
+        if (num_polys * size > 65535) throw std::invalid_argument("too many limbs in one call");
+        if (fwd)
+            pfg::ntt_forward(c, data, (int)num_polys, (int)size, (int)start, st(stream));
+        else
+            pfg::ntt_inverse(c, data, (int)num_polys, (int)size, (int)start, st(stream));
+    });
+}
+
+int fhe_ntt_forward(const fhe_context *ctx, uint64_t *data, size_t num_polys, size_t coeff_modulus_size,
+                    size_t start_modulus_idx, void *stream) {
+    return ntt_common(ctx, data, num_polys, coeff_modulus_size, start_modulus_idx, stream, true);
+}
+
+int fhe_ntt_inverse(const fhe_context *ctx, uint64_t *data, size_t num_polys, size_t coeff_modulus_size,
+                    size_t start_modulus_idx, void *stream) {
+    return ntt_common(ctx, data, num_polys, coeff_modulus_size, start_modulus_idx, stream, false);
+}
+
+int fhe_ckks_multiply(const fhe_context *ctx, uint64_t *ct1, const uint64_t *ct2, size_t chain_index, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("fhe_ckks_multiply needs a CKKS context");
+        need_ptr(ct1, "ct1");
+        need_ptr(ct2, "ct2");
+        pfg::ckks_tensor(c, ct1, ct2, level_of(c, chain_index), st(stream));
+    });
+}
+
+int fhe_keyswitch(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, const uint64_t *c2, size_t chain_index,
+                  const uint64_t *const *evk, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        pfg::Workspace w = ws_of(ctx, ws);
+        need_keyswitching(c);
+        need_ptr(ct, "ct");
+        need_ptr(c2, "c2");
+        need_ptr(evk, "evk");
+        const int l = level_of(c, chain_index);
+        if (c.scheme == pfg::kSchemeBFV) {
+            if (chain_index != 1) throw std::invalid_argument("BFV key switching works at chain index 1");
+            pfg::bfv_keyswitch(c, w, ct, c2, l, evk, st(stream));
+        } else {
+            pfg::ckks_keyswitch(c, w, ct, c2, l, evk, st(stream));
+        }
+    });
+}
+
+int fhe_relinearize(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t chain_index,
+                    const uint64_t *const *rlk, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        const int l = level_of(c, chain_index);
+        need_ptr(ct, "ct");
+        const uint64_t *c2 = ct + ((size_t)2 * l << c.log_n);
+        int rc = fhe_keyswitch(ctx, ws, ct, c2, chain_index, rlk, stream);
+        if (rc != FHE_OK) throw std::invalid_argument(g_last_error);
+    });
+}
+
+int fhe_multiply_and_relin(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct1, const uint64_t *ct2,
+                           size_t chain_index, const uint64_t *const *rlk, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        pfg::Workspace w = ws_of(ctx, ws);
+        need_keyswitching(c);
+        need_ptr(ct1, "ct1");
+        need_ptr(ct2, "ct2");
+        need_ptr(rlk, "rlk");
+        const int l = level_of(c, chain_index);
+        if (c.scheme == pfg::kSchemeBFV) {
+            if (chain_index != 1) throw std::invalid_argument("BFV HPS multiplication works at chain index 1");
+            pfg::bfv_mul_relin_hps(c, w, ct1, ct2, rlk, st(stream));
+        } else {
+            pfg::ckks_mul_relin(c, w, ct1, ct2, l, rlk, st(stream));
+        }
+    });
+}
+
+int fhe_rescale_to_next(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *in, uint64_t *out, size_t size,
+                        size_t chain_index, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        pfg::Workspace w = ws_of(ctx, ws);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("unsupported scheme");
+        need_ptr(in, "in");
+        need_ptr(out, "out");
+        const int l = level_of(c, chain_index);
+        if (l < 2) throw std::invalid_argument("end of modulus switching chain reached");
+        if (size == 0 || size > (size_t)c.nQ) throw std::invalid_argument("bad ciphertext size");
+        pfg::ckks_rescale(c, w, in, out, (int)size, l, st(stream));
+    });
+}
+
+int fhe_bfv_mod_switch_to_next(const fhe_context *ctx, const uint64_t *in, uint64_t *out, size_t size,
+                               size_t chain_index, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        if (c.scheme != pfg::kSchemeBFV) throw std::invalid_argument("fhe_bfv_mod_switch_to_next needs BFV");
+        need_ptr(in, "in");
+        need_ptr(out, "out");
+        const int l = level_of(c, chain_index);
+        if (l < 2) throw std::invalid_argument("end of modulus switching chain reached");
+        pfg::bfv_divide_round_q_last(c, in, out, (int)size, l, st(stream));
+    });
+}
+
+int fhe_ckks_multiply_relin_rescale(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *ct1,
+                                    const uint64_t *ct2, uint64_t *out, size_t chain_index,
+                                    const uint64_t *const *rlk, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        pfg::Workspace w = ws_of(ctx, ws);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("fhe_ckks_multiply_relin_rescale needs CKKS");
+        need_keyswitching(c);
+        need_ptr(ct1, "ct1");
+        need_ptr(ct2, "ct2");
+        need_ptr(out, "out");
+        need_ptr(rlk, "rlk");
+        const int l = level_of(c, chain_index);
+        if (l < 2) throw std::invalid_argument("end of modulus switching chain reached");
+        pfg::ckks_mul_relin_rescale(c, w, ct1, ct2, out, l, rlk, st(stream));
+    });
+}
+
+static int galois_index(const pfg::Context &c, uint32_t elt) {
+    auto it = std::find(c.galois_elts.begin(), c.galois_elts.end(), elt);
+    return it == c.galois_elts.end() ? -1 : (int)(it - c.galois_elts.begin());
+}
+
+int fhe_apply_galois(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t chain_index, uint32_t galois_elt,
+                     const uint64_t *const *gk, void *stream) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        pfg::Workspace w = ws_of(ctx, ws);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("Galois automorphisms are implemented for CKKS");
+        need_keyswitching(c);
+        need_ptr(ct, "ct");
+        need_ptr(gk, "gk");
+        if (galois_index(c, galois_elt) < 0) throw std::invalid_argument("Galois elt not present");
+        pfg::ckks_apply_galois(c, w, ct, level_of(c, chain_index), c.perm_table(galois_elt), gk, st(stream));
+    });
+}
+
+static void rotate_rec(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t chain_index, int step,
+                       const uint64_t *const *const *gks, void *stream) {
+    const pfg::Context &c = ctx_of(ctx);
+    const uint32_t elt = pfg::host::elt_from_step(step, c.n);
+    const int idx = galois_index(c, elt);
+    if (idx >= 0) {
+        int rc = fhe_apply_galois(ctx, ws, ct, chain_index, elt, gks[idx], stream);
+        if (rc != FHE_OK) throw std::invalid_argument(g_last_error);
+        return;
+    }
+    // NAF decomposition (src/evaluate.cu:1647-1661)
+    auto naf = pfg::host::naf(step);
+    if (naf.size() == 1) throw std::invalid_argument("Galois key not present");
+    for (int s : naf)
+        if ((uint64_t)std::abs(s) != (c.n >> 1)) rotate_rec(ctx, ws, ct, chain_index, s, gks, stream);
+}
+
+int fhe_rotate(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t chain_index, int step,
+               const uint64_t *const *const *galois_keys, void *stream) {
+    return guarded([&] {
+        need_ptr(galois_keys, "galois_keys");
+        rotate_rec(ctx, ws, ct, chain_index, step, galois_keys, stream);
+    });
+}
+
+int fhe_hoisting(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t chain_index, const int *steps,
+                 size_t num_steps, const uint64_t *const *const *galois_keys, void *stream) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        pfg::Workspace w = ws_of(ctx, ws);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("hoisting is implemented for CKKS");
+        need_keyswitching(c);
+        need_ptr(ct, "ct");
+        need_ptr(steps, "steps");
+        need_ptr(galois_keys, "galois_keys");
+        if (num_steps == 0) throw std::invalid_argument("no rotation steps");
+        std::vector<pfg::StepKey> sk;
+        for (size_t i = 0; i < num_steps; i++) {
+            const uint32_t elt = pfg::host::elt_from_step(steps[i], c.n);
+            const int idx = galois_index(c, elt);
+            if (idx < 0) throw std::logic_error("Galois key not present in hoisting");
+            sk.push_back(pfg::StepKey{c.perm_table(elt), galois_keys[idx]});
+        }
+        pfg::ckks_hoisting(c, w, ct, level_of(c, chain_index), sk, st(stream));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,231 @@
+// context.cu — builds and uploads the device tables (see context.cuh).
+#include <stdexcept>
+#include <string>
+
+#include "context.cuh"
+#include "host_tables.hpp"
+
+namespace pfg {
+
+static void check(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+DevBuf::~DevBuf() {
+    if (p) cudaFree(p);
+}
+
+void DevBuf::upload(const void *src, size_t n) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = n;
+    if (!n) return;
+    check(cudaMalloc(&p, n), "cudaMalloc(context table)");
+    check(cudaMemcpy(p, src, n, cudaMemcpyHostToDevice), "cudaMemcpy(context table)");
+}
+
+template <class T>
+static void up(DevBuf &b, const std::vector<T> &v) {
+    b.upload(v.data(), v.size() * sizeof(T));
+}
+
+const uint32_t *Context::perm_table(uint32_t elt) {
+    std::lock_guard<std::mutex> g(perm_mu);
+    auto it = perms.find(elt);
+    if (it != perms.end()) return it->second->as<uint32_t>();
+    auto perm = host::galois_perm(log_n, elt);
+    auto buf = std::make_unique<DevBuf>();
+    up(*buf, perm);
+    const uint32_t *p = buf->as<uint32_t>();
+    perms.emplace(elt, std::move(buf));
+    return p;
+}
+
+std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, const std::vector<uint64_t> &coeff_modulus,
+                                      int special_size, uint64_t plain_modulus,
+                                      const std::vector<uint32_t> &galois_elts) {
+    using namespace host;
+    auto c = std::make_unique<Context>();
+    int log_n = 0;
+    while ((uint64_t(1) << log_n) < n) log_n++;
+    if ((uint64_t(1) << log_n) != n || log_n < 12 || log_n > 17)
+        throw std::invalid_argument("poly_modulus_degree must be a power of two in [2^12, 2^17]");
+    if (coeff_modulus.size() < 2 || (int)coeff_modulus.size() <= special_size || special_size < 0)
+        throw std::invalid_argument("coefficient modulus needs at least one data prime and two primes in total");
+    if (coeff_modulus.size() > 64) throw std::invalid_argument("at most 64 primes are supported");
+    if (scheme != kSchemeCKKS && scheme != kSchemeBFV) throw std::invalid_argument("unsupported scheme");
+    for (uint64_t q : coeff_modulus) {
+        if (q >> 61 || !is_prime(q) || (q - 1) % (2 * n))
+            throw std::invalid_argument("every modulus must be a prime below 2^61 with q = 1 mod 2N");
+    }
+    c->scheme = scheme;
+    c->mul_tech = mul_tech;
+    c->log_n = log_n;
+    c->n = n;
+    c->nP = special_size;
+    c->nQ = (int)coeff_modulus.size() - special_size;
+    c->t = plain_modulus;
+    c->mods = coeff_modulus;
+    const int nQ = c->nQ, nP = c->nP;
+    std::vector<uint64_t> Q(coeff_modulus.begin(), coeff_modulus.begin() + nQ);
+    std::vector<uint64_t> P(coeff_modulus.begin() + nQ, coeff_modulus.end());
+
+    std::vector<uint64_t> R;
+    if (scheme == kSchemeBFV) {
+        if (!plain_modulus) throw std::invalid_argument("BFV needs a plain modulus");
+        if (mul_tech != kMulHPS) throw std::invalid_argument("only mul_tech hps is supported for BFV");
+        uint64_t minq = Q[0];
+        for (uint64_t q : Q) minq = std::min(minq, q);
+        R = get_primes_below(n, minq, nQ + 1);
+        c->nR = nQ + 1;
+        c->mods.insert(c->mods.end(), R.begin(), R.end());
+    }
+
+    // moduli and NTT tables for QP and R
+    const size_t np = c->mods.size();
+    std::vector<uint64_t> modw(3 * np), tw, itw, all_tw, all_itw, ninv(2 * np);
+    all_tw.reserve(np * 2 * n);
+    all_itw.reserve(np * 2 * n);
+    for (size_t i = 0; i < np; i++) {
+        modw[3 * i] = c->mods[i];
+        barrett(c->mods[i], modw[3 * i + 1], modw[3 * i + 2]);
+        ntt_tables(log_n, c->mods[i], tw, itw, ninv[2 * i], ninv[2 * i + 1]);
+        all_tw.insert(all_tw.end(), tw.begin(), tw.end());
+        all_itw.insert(all_itw.end(), itw.begin(), itw.end());
+    }
+    up(c->d_mods, modw);
+    up(c->d_tw, all_tw);
+    up(c->d_itw, all_itw);
+    up(c->d_ninv, ninv);
+
+    if (nP > 0) {
+        // mod-down constants (rns.cu:107-124, BaseConverter(P -> Ql), host/rns.cu:438-498)
+        std::vector<uint64_t> phi(2 * nP), pmat((size_t)nQ * nP), pinv(2 * nQ);
+        for (int k = 0; k < nP; k++) {
+            phi[2 * k] = invmod(prod_mod(P, k, P[k]), P[k]);
+            phi[2 * k + 1] = shoup(phi[2 * k], P[k]);
+        }
+        for (int j = 0; j < nQ; j++) {
+            for (int k = 0; k < nP; k++) pmat[(size_t)j * nP + k] = prod_mod(P, k, Q[j]);
+            pinv[2 * j] = invmod(prod_mod(P, -1, Q[j]), Q[j]);
+            pinv[2 * j + 1] = shoup(pinv[2 * j], Q[j]);
+        }
+        up(c->p_hat_inv, phi);
+        up(c->p_mat, pmat);
+        up(c->p_inv, pinv);
+    }
+
+    // per data level (rns.cu:66-195)
+    c->levels.resize(nQ + 1);
+    for (int l = 1; l <= nQ; l++) {
+        auto lt = std::make_unique<LevelTables>();
+        lt->l = l;
+        if (nP > 0) {
+            const int alpha = nP, beta = c->beta(l);
+            lt->beta = beta;
+            std::vector<uint64_t> phi(2 * l), mat((size_t)beta * (l + alpha) * alpha, 0);
+            for (int d = 0; d < beta; d++) {
+                const int s = d * alpha, sz = std::min(alpha, l - s);
+                std::vector<uint64_t> dig(Q.begin() + s, Q.begin() + s + sz);
+                for (int i = 0; i < sz; i++) {
+                    phi[2 * (s + i)] = invmod(prod_mod(dig, i, Q[s + i]), Q[s + i]);
+                    phi[2 * (s + i) + 1] = shoup(phi[2 * (s + i)], Q[s + i]);
+                }
+                for (int jj = 0; jj < l + alpha; jj++) {
+                    if (jj >= s && jj < s + sz) continue;
+                    const uint64_t p = c->mods[c->qlp_table(l, jj)];
+                    for (int i = 0; i < sz; i++)
+                        mat[((size_t)d * (l + alpha) + jj) * alpha + i] = prod_mod(dig, i, p);
+                }
+            }
+            up(lt->part_hat_inv, phi);
+            up(lt->modup_mat, mat);
+        }
+        if (l > 1) {
+            std::vector<uint64_t> iq(2 * (l - 1));
+            for (int j = 0; j < l - 1; j++) {
+                iq[2 * j] = invmod(Q[l - 1] % Q[j], Q[j]);
+                iq[2 * j + 1] = shoup(iq[2 * j], Q[j]);
+            }
+            up(lt->inv_qlast, iq);
+        }
+        c->levels[l] = std::move(lt);
+    }
+
+    if (scheme == kSchemeBFV) {
+        // HPS constants (rns.cu:687-777; BaseConverter host/rns.cu:438-498; RNSBase inv_)
+        const int nR = c->nR;
+        std::vector<uint64_t> qhi(2 * nQ), rhi(2 * nR), q2r((size_t)nR * nQ), r2q((size_t)nQ * nR);
+        std::vector<uint64_t> q2ra((size_t)(nQ + 1) * nR), r2qa((size_t)(nR + 1) * nQ);
+        std::vector<double> qinv(nQ), rinv(nR), frac(nQ);
+        std::vector<uint64_t> modr((size_t)nR * (nQ + 1));
+        for (int i = 0; i < nQ; i++) {
+            qhi[2 * i] = invmod(prod_mod(Q, i, Q[i]), Q[i]);
+            qhi[2 * i + 1] = shoup(qhi[2 * i], Q[i]);
+            qinv[i] = 1.0 / static_cast<double>(Q[i]);
+        }
+        for (int j = 0; j < nR; j++) {
+            rhi[2 * j] = invmod(prod_mod(R, j, R[j]), R[j]);
+            rhi[2 * j + 1] = shoup(rhi[2 * j], R[j]);
+            rinv[j] = 1.0 / static_cast<double>(R[j]);
+        }
+        for (int j = 0; j < nR; j++)
+            for (int i = 0; i < nQ; i++) q2r[(size_t)j * nQ + i] = prod_mod(Q, i, R[j]);
+        for (int j = 0; j < nQ; j++)
+            for (int i = 0; i < nR; i++) r2q[(size_t)j * nR + i] = prod_mod(R, i, Q[j]);
+        for (int a = 0; a <= nQ; a++)
+            for (int j = 0; j < nR; j++) q2ra[(size_t)a * nR + j] = mulmod(a, prod_mod(Q, -1, R[j]), R[j]);
+        for (int a = 0; a <= nR; a++)
+            for (int j = 0; j < nQ; j++) r2qa[(size_t)a * nQ + j] = mulmod(a, prod_mod(R, -1, Q[j]), Q[j]);
+        // S = QR.  For q_i: X = t*R*[(S/q_i)^-1]_{q_i}; rem = X mod q_i; frac = rem / q_i;
+        // floor(X / q_i) mod r_j = -rem * q_i^-1 (R divides X).  For r_j:
+        // floor(X / r_j) = t * (R / r_j) * [(S/r_j)^-1]_{r_j}.
+        std::vector<uint64_t> S(Q);
+        S.insert(S.end(), R.begin(), R.end());
+        for (int i = 0; i < nQ; i++) {
+            const uint64_t q = Q[i];
+            const uint64_t shat_inv = invmod(prod_mod(S, i, q), q);
+            const uint64_t rem = mulmod(mulmod(plain_modulus % q, prod_mod(R, -1, q), q), shat_inv, q);
+            frac[i] = static_cast<double>(rem) / static_cast<double>(q);
+            for (int j = 0; j < nR; j++) {
+                const uint64_t v = mulmod(rem % R[j], invmod(q % R[j], R[j]), R[j]);
+                modr[(size_t)j * (nQ + 1) + i] = v ? R[j] - v : 0;
+            }
+        }
+        for (int j = 0; j < nR; j++) {
+            const uint64_t shat_inv = invmod(prod_mod(S, nQ + j, R[j]), R[j]);
+            modr[(size_t)j * (nQ + 1) + nQ] =
+                    mulmod(mulmod(plain_modulus % R[j], prod_mod(R, j, R[j]), R[j]), shat_inv, R[j]);
+        }
+        up(c->hps_q_hat_inv, qhi);
+        up(c->hps_r_hat_inv, rhi);
+        up(c->hps_q_inv, qinv);
+        up(c->hps_r_inv, rinv);
+        up(c->hps_q2r_mat, q2r);
+        up(c->hps_r2q_mat, r2q);
+        up(c->hps_q2r_alpha, q2ra);
+        up(c->hps_r2q_alpha, r2qa);
+        up(c->hps_frac, frac);
+        up(c->hps_modr, modr);
+    }
+
+    c->galois_elts = galois_elts;
+    if (c->galois_elts.empty() && scheme == kSchemeCKKS) {
+        // all power-of-two rotations plus conjugation (src/galois.cu:41-65)
+        const uint32_t m = (uint32_t)(2 * n);
+        c->galois_elts.push_back(m - 1);
+        uint64_t pos = 5, neg = invmod(5, m);
+        for (int i = 0; i < log_n - 1; i++) {
+            c->galois_elts.push_back((uint32_t)pos);
+            pos = (pos * pos) & (m - 1);
+            c->galois_elts.push_back((uint32_t)neg);
+            neg = (neg * neg) & (m - 1);
+        }
+    }
+    // permutation tables for every Galois element, built up front so that no evaluator call
+    // allocates or copies host data (include/galois.cuh:98-113)
+    for (uint32_t elt : c->galois_elts) c->perm_table(elt);
+    return c;
+}
+
+}  // namespace pfg

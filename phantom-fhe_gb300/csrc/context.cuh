@@ -1,0 +1,93 @@
+// context.cuh — device-resident parameter tables for one parameter set.
+//
+// Plays the role of the reference's PhantomContext + per-level DRNSTool
+// (src/context.cu:121-232, src/rns.cu:11-195, 573-777): the modulus chain, the NTT tables
+// of every prime (Q, P and the BFV HPS base R), the hybrid key-switching constants of every
+// data level, the mod-down and rescale constants, the HPS scale-and-round constants and the
+// Galois permutation tables.  Everything is built once on the host and uploaded; kernels
+// read it through the small POD views below.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "ntt.cuh"
+
+namespace pfg {
+
+enum Scheme { kSchemeNone = 0, kSchemeBFV = 1, kSchemeCKKS = 2, kSchemeBGV = 3 };
+enum MulTech { kMulNone = 0, kMulBEHZ = 1, kMulHPS = 2, kMulHPSOverQ = 3, kMulHPSOverQLeveled = 4 };
+
+// Device memory owned by the context (plain cudaMalloc, freed in the destructor).
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf();
+    template <class T>
+    T *as() const {
+        return static_cast<T *>(p);
+    }
+    void upload(const void *src, size_t n);  // allocates n bytes and copies
+};
+
+// Per data level l (number of Q limbs): hybrid key-switching and rescale constants.
+struct LevelTables {
+    int l = 0, beta = 0;
+    // partQlHatInv (value, Shoup) per Ql limb: inverse of (Q_digit / q_i) mod q_i
+    DevBuf part_hat_inv;  // [l][2]
+    // modup base-change rows M_d[jj][i] = (Q_digit / q_{s+i}) mod p_jj, zero rows for the
+    // digit's own limbs: [beta][l + alpha][alpha]
+    DevBuf modup_mat;
+    // q_last^-1 mod q_j (value, Shoup), j < l - 1
+    DevBuf inv_qlast;  // [l-1][2]
+};
+
+struct Context {
+    int scheme = kSchemeCKKS, mul_tech = kMulHPS;
+    int log_n = 0;
+    uint64_t n = 0;
+    int nQ = 0, nP = 0, nR = 0;
+    uint64_t t = 0;
+    std::vector<uint64_t> mods;  // QP, then R (BFV HPS)
+    DevBuf d_mods, d_tw, d_itw, d_ninv;
+    // mod-down (level independent): PHatInv (value, Shoup) [nP][2]; (P/p_k) mod q_j [nQ][nP];
+    // P^-1 mod q_j (value, Shoup) [nQ][2]
+    DevBuf p_hat_inv, p_mat, p_inv;
+    std::vector<std::unique_ptr<LevelTables>> levels;  // index l = 1..nQ
+    // BFV HPS
+    DevBuf hps_q_hat_inv, hps_r_hat_inv;   // [nQ][2], [nR][2]
+    DevBuf hps_q_inv, hps_r_inv;           // 1/q_i, 1/r_j as doubles
+    DevBuf hps_q2r_mat, hps_r2q_mat;       // [nR][nQ], [nQ][nR]
+    DevBuf hps_q2r_alpha, hps_r2q_alpha;   // [nQ+1][nR], [nR+1][nQ]
+    DevBuf hps_frac;                        // [nQ] doubles
+    DevBuf hps_modr;                        // [nR][nQ+1]
+    // Galois
+    std::vector<uint32_t> galois_elts;
+    std::map<uint32_t, std::unique_ptr<DevBuf>> perms;
+    std::mutex perm_mu;
+
+    int l1() const { return log_n / 2; }
+    int l2() const { return log_n - log_n / 2; }
+    NttTables ntt() const {
+        return NttTables{d_mods.as<Mod>(), d_tw.as<TwPair>(), d_itw.as<TwPair>(), d_ninv.as<uint64_t>(), log_n,
+                         l1(), l2()};
+    }
+    int beta(int l) const { return (l + nP - 1) / nP; }
+    // Table index of QlP limb jj at level l.
+    int qlp_table(int l, int jj) const { return jj < l ? jj : nQ + (jj - l); }
+    const uint32_t *perm_table(uint32_t elt);  // builds and caches on first use
+};
+
+// Builds every table; throws std::invalid_argument / std::logic_error on bad parameters.
+std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, const std::vector<uint64_t> &coeff_modulus,
+                                      int special_size, uint64_t plain_modulus,
+                                      const std::vector<uint32_t> &galois_elts);
+
+}  // namespace pfg

@@ -1,0 +1,124 @@
+// launch.cuh — NTT pass dispatch, limb maps and the shared element-wise functors.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "context.cuh"
+#include "ntt.cuh"
+
+namespace pfg {
+
+// ---------------------------------------------------------------- limb maps
+// A map turns blockIdx.y into (poly, limb k, prime table index) and may idle a block.
+
+// Contiguous [poly][limbs][N] data, limb k uses prime table start + k.
+struct SeqMap {
+    int limbs, start;
+    __device__ __forceinline__ bool operator()(int b, int &poly, int &k, int &tbl) const {
+        poly = b / limbs;
+        k = b % limbs;
+        tbl = start + k;
+        return true;
+    }
+};
+
+// QlP limbs [0, l + alpha) of `polys` polynomials at level l, starting at limb k0.
+struct QlpMap {
+    int limbs, k0, l, nQ;
+    __device__ __forceinline__ bool operator()(int b, int &poly, int &k, int &tbl) const {
+        poly = b / limbs;
+        k = k0 + b % limbs;
+        tbl = k < l ? k : nQ + (k - l);
+        return true;
+    }
+};
+
+// Mod-up digits: block b -> digit d = b / qlp, QlP limb jj = b % qlp; the digit's own
+// limbs idle when skip_own (they are already in NTT form, CKKS).
+struct ModupMap {
+    int qlp, l, nQ, alpha;
+    bool skip_own;
+    __device__ __forceinline__ bool operator()(int b, int &d, int &jj, int &tbl) const {
+        d = b / qlp;
+        jj = b % qlp;
+        tbl = jj < l ? jj : nQ + (jj - l);
+        if (skip_own && jj >= d * alpha && jj < d * alpha + alpha && jj < l) return false;
+        return true;
+    }
+};
+
+// ---------------------------------------------------------------- generic functors
+
+struct PtrLoad {  // base[poly * ps + k * N + idx]
+    const uint64_t *base;
+    long long ps;
+    int log_n;
+    __device__ __forceinline__ uint64_t operator()(int poly, int k, int, uint32_t idx) const {
+        return base[poly * ps + ((long long)k << log_n) + idx];
+    }
+};
+
+struct PtrStore {
+    uint64_t *base;
+    long long ps;
+    int log_n;
+    __device__ __forceinline__ void operator()(int poly, int k, int, uint32_t idx, uint64_t v) const {
+        base[poly * ps + ((long long)k << log_n) + idx] = v;
+    }
+};
+
+// Stores v * s[k] mod q (s as (value, Shoup) pairs indexed by logical limb k - kofs).
+struct ScaleStore {
+    uint64_t *base;
+    long long ps;
+    int log_n, kofs;
+    const uint64_t *s;
+    const Mod *mods;
+    __device__ __forceinline__ void operator()(int poly, int k, int tbl, uint32_t idx, uint64_t v) const {
+        const int i = k - kofs;
+        base[poly * ps + ((long long)k << log_n) + idx] = mul_shoup(v, s[2 * i], s[2 * i + 1], mods[tbl].q);
+    }
+};
+
+// ---------------------------------------------------------------- pass launchers
+
+template <bool FWD, bool LAST, class Map, class Load, class Store>
+void col_pass(const Context &c, int blocks, Map m, Load ld, Store st, cudaStream_t s) {
+    dim3 grid((unsigned)(c.n / kTileElems), (unsigned)blocks);
+    const NttTables T = c.ntt();
+    switch (c.l1()) {
+        case 6: ntt_col_pass<6, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
+        case 7: ntt_col_pass<7, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
+        case 8: ntt_col_pass<8, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
+        default: break;
+    }
+}
+
+template <bool FWD, bool LAST, class Map, class Load, class Store>
+void row_pass(const Context &c, int blocks, Map m, Load ld, Store st, cudaStream_t s) {
+    dim3 grid((unsigned)(c.n / kTileElems), (unsigned)blocks);
+    const NttTables T = c.ntt();
+    switch (c.l2()) {
+        case 6: ntt_row_pass<6, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
+        case 7: ntt_row_pass<7, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
+        case 8: ntt_row_pass<8, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
+        case 9: ntt_row_pass<9, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
+        default: break;
+    }
+}
+
+// Forward transform: column pass (load functor) -> row pass (store functor); the
+// intermediate lazy values go to `mid` (which may alias the final destination).
+template <class Map, class Load, class Store>
+void ntt_fwd(const Context &c, int blocks, Map m, Load ld, PtrStore mid, Store st, cudaStream_t s) {
+    col_pass<true, false>(c, blocks, m, ld, mid, s);
+    row_pass<true, true>(c, blocks, m, PtrLoad{mid.base, mid.ps, mid.log_n}, st, s);
+}
+
+// Inverse transform: row pass (load functor) -> column pass (store functor).
+template <class Map, class Load, class Store>
+void ntt_inv(const Context &c, int blocks, Map m, Load ld, PtrStore mid, Store st, cudaStream_t s) {
+    row_pass<false, false>(c, blocks, m, ld, mid, s);
+    col_pass<false, true>(c, blocks, m, PtrLoad{mid.base, mid.ps, mid.log_n}, st, s);
+}
+
+}  // namespace pfg

@@ -1,0 +1,50 @@
+// ops.hpp — internal orchestration entry points behind the C ABI (capi.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "context.cuh"
+
+namespace pfg {
+
+// Caller-provided scratch; carved into regions by each operation.
+struct Workspace {
+    uint64_t *base = nullptr;
+    size_t words = 0;
+};
+
+size_t workspace_words(const Context &c);
+
+struct StepKey {  // one hoisted rotation: permutation table + key digits (device array)
+    const uint32_t *perm;
+    const uint64_t *const *key;
+};
+
+void ntt_forward(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s);
+void ntt_inverse(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s);
+
+// CKKS (NTT form).  l = number of Q limbs of the operands.
+void ckks_tensor(const Context &c, uint64_t *ct1, const uint64_t *ct2, int l, cudaStream_t s);
+void ckks_keyswitch(const Context &c, const Workspace &w, uint64_t *ct, const uint64_t *c2, int l,
+                    const uint64_t *const *evk, cudaStream_t s);
+void ckks_mul_relin(const Context &c, const Workspace &w, uint64_t *ct1, const uint64_t *ct2, int l,
+                    const uint64_t *const *rlk, cudaStream_t s);
+void ckks_mul_relin_rescale(const Context &c, const Workspace &w, const uint64_t *ct1, const uint64_t *ct2,
+                            uint64_t *out, int l, const uint64_t *const *rlk, cudaStream_t s);
+void ckks_rescale(const Context &c, const Workspace &w, const uint64_t *in, uint64_t *out, int size, int l,
+                  cudaStream_t s);
+void ckks_apply_galois(const Context &c, const Workspace &w, uint64_t *ct, int l, const uint32_t *perm,
+                       const uint64_t *const *gk, cudaStream_t s);
+void ckks_hoisting(const Context &c, const Workspace &w, uint64_t *ct, int l, const std::vector<StepKey> &steps,
+                   cudaStream_t s);
+
+// BFV (coefficient form).
+void bfv_keyswitch(const Context &c, const Workspace &w, uint64_t *ct, const uint64_t *c2, int l,
+                   const uint64_t *const *evk, cudaStream_t s);
+void bfv_mul_relin_hps(const Context &c, const Workspace &w, uint64_t *ct1, const uint64_t *ct2,
+                       const uint64_t *const *rlk, cudaStream_t s);
+void bfv_divide_round_q_last(const Context &c, const uint64_t *in, uint64_t *out, int size, int l, cudaStream_t s);
+
+}  // namespace pfg

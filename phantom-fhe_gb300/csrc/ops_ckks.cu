@@ -1,0 +1,505 @@
+// ops_ckks.cu — NTT entry points and the CKKS hybrid key-switching pipeline.
+//
+// Restates, with fused kernels, the reference's
+//   modup                 DRNSTool::modup                  src/rns_bconv.cu:530-628
+//   inner product         key_switch_inner_prod_c2_and_evk src/eval_key_switch.cu:14-69
+//   moddown               DRNSTool::moddown_from_NTT       src/rns_bconv.cu:776-828
+//   keyswitch_inplace                                      src/eval_key_switch.cu:95-182
+//   tensor product        tensor_prod_2x2_rns_poly         src/polymath.cu:463-497
+//   rescale               divide_and_round_q_last_ntt      src/rns.cu:1160-1184
+//   Galois                apply_galois_inplace / hoisting  src/evaluate.cu:1567-1865
+//
+// Pipeline of one key switch at level l (alpha = |P|, beta = ceil(l / alpha)):
+//   1. iNTT(c2) with the partQlHatInv scaling fused into the store          -> y   [l][N]
+//   2. forward NTT of every digit's complement limbs, the base conversion
+//      y -> complement limb computed in the column pass's load              -> tm  [beta][l+alpha][N]
+//      (the digit's own limbs are c2 itself and are never copied)
+//   3. inner product over digits, 128-bit accumulation, one reduction       -> cx  [2][l+alpha][N]
+//   4. iNTT of cx's P limbs with the PHatInv scaling fused into the store     (in place)
+//   5. forward NTT of delta_j = sum_k y_k (P/p_k) mod q_j, computed in the column pass's load,
+//      with (cx_j - NTT(delta_j)) * P^-1 + base fused into the row pass's store.
+// For HMult the tensor product is never written: step 1 loads a1*b1, step 3 recomputes it for
+// the own limbs, and step 5's "base" is a0*b0 / a0*b1 + a1*b0.  HMult + rescale additionally
+// folds the rescale's NTT into step 5 by linearity (see ckks_mul_relin_rescale).
+#include <stdexcept>
+
+#include "keyswitch.cuh"
+#include "launch.cuh"
+#include "ops.hpp"
+
+namespace pfg {
+
+size_t workspace_words(const Context &c) {
+    const size_t n = c.n, nQ = c.nQ, a = c.nP;
+    size_t w = 0;
+    if (a) {
+        const size_t beta = c.beta((int)nQ), qlp = nQ + a;
+        // y | tm | cx | g0,g1 (or acc0) | z
+        w = n * (nQ + beta * qlp + 2 * qlp + 2 * nQ + 2);
+    }
+    if (c.scheme == kSchemeBFV) {
+        const size_t qr = nQ + c.nR;
+        // ext(a), ext(b) [2][QR], t3 [3][QR], o3 [3][Q], r tmp [R], plus key switch scratch
+        const size_t bfv = n * (4 * qr + 3 * qr + 3 * nQ + c.nR) + w;
+        w = std::max(w, bfv);
+    }
+    // rescale / generic temporaries
+    w = std::max(w, n * (2 * nQ + 2));
+    return w;
+}
+
+// ------------------------------------------------------------------ NTT entry points
+
+void ntt_forward(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s) {
+    const long long ps = (long long)limbs << c.log_n;
+    PtrStore st{data, ps, c.log_n};
+    ntt_fwd(c, polys * limbs, SeqMap{limbs, start}, PtrLoad{data, ps, c.log_n}, st, st, s);
+}
+
+void ntt_inverse(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s) {
+    const long long ps = (long long)limbs << c.log_n;
+    PtrStore st{data, ps, c.log_n};
+    ntt_inv(c, polys * limbs, SeqMap{limbs, start}, PtrLoad{data, ps, c.log_n}, st, st, s);
+}
+
+// ------------------------------------------------------------------ functors
+
+// a1 * b1 mod q: the tensor product's d2 term (c2 of the relinearisation)
+struct TensorD2Load {
+    const uint64_t *a1, *b1;
+    const Mod *mods;
+    int log_n;
+    __device__ __forceinline__ uint64_t operator()(int, int k, int tbl, uint32_t idx) const {
+        const size_t o = ((size_t)k << log_n) + idx;
+        return mul_mod(a1[o], b1[o], mods[tbl]);
+    }
+};
+
+// Base conversion of one digit into a complement limb (bconv_matmul_padded_unroll2_kernel,
+// src/rns_bconv.cu:455-485): sum_i y[s+i] * M_d[jj][i] mod p_jj.
+struct BconvLoad {
+    const uint64_t *y, *mat;
+    const Mod *mods;
+    int log_n, l, alpha, qlp;
+    __device__ __forceinline__ uint64_t operator()(int d, int jj, int tbl, uint32_t idx) const {
+        const int s0 = d * alpha, sz = min(alpha, l - s0);
+        const uint64_t *m = mat + ((size_t)d * qlp + jj) * alpha;
+        u128 acc{0, 0};
+        for (int i = 0; i < sz; i++) mac(acc, y[((size_t)(s0 + i) << log_n) + idx], __ldg(m + i));
+        return reduce128(acc, mods[tbl]);
+    }
+};
+
+// P -> q_j base conversion of the mod-down (bConv_BEHZ, src/rns_bconv.cu:212-229): yp holds
+// [x_k * PHatInv_k]_{p_k} in the P limbs of cx.
+struct PBconvLoad {
+    const uint64_t *cx;
+    long long cps;
+    const uint64_t *pmat;
+    const Mod *mods;
+    int log_n, l, nP;
+    __device__ __forceinline__ uint64_t operator()(int t, int j, int tbl, uint32_t idx) const {
+        const uint64_t *yp = cx + t * cps + ((size_t)l << log_n) + idx;
+        const uint64_t *m = pmat + (size_t)j * nP;
+        u128 acc{0, 0};
+        for (int k = 0; k < nP; k++) mac(acc, yp[(size_t)k << log_n], __ldg(m + k));
+        return reduce128(acc, mods[tbl]);
+    }
+};
+
+// Bases added to the mod-down result.
+struct InplaceBase {  // the ciphertext itself (keyswitch_inplace's add_to_ct_kernel)
+    const uint64_t *ct;
+    long long ps;
+    int log_n;
+    __device__ __forceinline__ uint64_t operator()(int t, int j, const Mod &, uint32_t idx) const {
+        return ct[t * ps + ((long long)j << log_n) + idx];
+    }
+};
+
+struct TensorBase {  // t = 0: a0*b0, t = 1: a0*b1 + a1*b0
+    const uint64_t *a, *b;
+    long long ps;
+    int log_n;
+    __device__ __forceinline__ uint64_t operator()(int t, int j, const Mod &m, uint32_t idx) const {
+        const size_t o = ((size_t)j << log_n) + idx;
+        const uint64_t a0 = a[o], b0 = b[o];
+        if (t == 0) return mul_mod(a0, b0, m);
+        u128 acc = mul_wide(a0, b[ps + o]);
+        mac(acc, a[ps + o], b0);
+        return reduce128(acc, m);
+    }
+};
+
+struct FirstPolyBase {  // t = 0: g0, t = 1: 0 (Galois: c1 is wiped before the key switch)
+    const uint64_t *g0;
+    int log_n;
+    __device__ __forceinline__ uint64_t operator()(int t, int j, const Mod &, uint32_t idx) const {
+        return t == 0 ? g0[((size_t)j << log_n) + idx] : 0;
+    }
+};
+
+// Row-pass store of step 5: out_t[j] = base + (cx_t[j] - v) * P^-1 mod q_j
+template <class Base>
+struct ModdownStore {
+    uint64_t *out0, *out1;  // limb j is written at limb j - jofs
+    int jofs;
+    const uint64_t *cx;
+    long long cps;
+    const uint64_t *pinv;
+    const Mod *mods;
+    int log_n;
+    Base base;
+    __device__ __forceinline__ void operator()(int t, int j, int tbl, uint32_t idx, uint64_t v) const {
+        const Mod m = mods[tbl];
+        const size_t o = ((size_t)j << log_n) + idx;
+        const uint64_t r = mul_shoup(sub_mod(cx[t * cps + o], v, m.q), pinv[2 * j], pinv[2 * j + 1], m.q);
+        (t == 0 ? out0 : out1)[((size_t)(j - jofs) << log_n) + idx] = add_mod(base(t, j, m, idx), r, m.q);
+    }
+};
+
+static int grid_for(size_t work, int per_block) {
+    size_t b = (work + per_block - 1) / per_block;
+    return (int)std::min<size_t>(b, 152 * 16);
+}
+
+// ------------------------------------------------------------------ pipeline pieces
+
+struct KsBuffers {
+    uint64_t *y, *tm, *cx, *g, *z;
+};
+
+static KsBuffers ks_buffers(const Context &c, const Workspace &w) {
+    const size_t n = c.n, nQ = c.nQ, qlp = nQ + c.nP, beta = c.beta(c.nQ);
+    KsBuffers b;
+    b.y = w.base;
+    b.tm = b.y + nQ * n;
+    b.cx = b.tm + beta * qlp * n;
+    b.g = b.cx + 2 * qlp * n;
+    b.z = b.g + 2 * nQ * n;
+    return b;
+}
+
+// Steps 1-2: y = iNTT(c2) * partQlHatInv; tm = NTT(bconv(y)) for every digit.
+template <class C2Load>
+static void modup_ckks(const Context &c, const KsBuffers &b, C2Load c2ld, int l, cudaStream_t s) {
+    const LevelTables &lt = *c.levels[l];
+    const int alpha = c.nP, qlp = l + alpha, beta = lt.beta;
+    const long long yps = (long long)l << c.log_n;
+    PtrStore ys{b.y, yps, c.log_n};
+    ntt_inv(c, l, SeqMap{l, 0}, c2ld, ys,
+            ScaleStore{b.y, yps, c.log_n, 0, lt.part_hat_inv.as<uint64_t>(), c.d_mods.as<Mod>()}, s);
+    const long long tps = (long long)qlp << c.log_n;
+    PtrStore ts{b.tm, tps, c.log_n};
+    ModupMap mm{qlp, l, c.nQ, alpha, true};
+    BconvLoad bl{b.y, lt.modup_mat.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, l, alpha, qlp};
+    ntt_fwd(c, beta * qlp, mm, bl, ts, ts, s);
+}
+
+// Step 3
+template <class Own>
+static void inner_product(const Context &c, const KsBuffers &b, Own own, int l, const uint64_t *const *evk,
+                          cudaStream_t s) {
+    const int qlp = l + c.nP;
+    const size_t work = ((size_t)qlp << c.log_n) / 2;
+    ks_inner_product<Own, false><<<grid_for(work, 256), 256, 0, s>>>(b.cx, b.tm, own, evk, c.d_mods.as<Mod>(),
+                                                                      c.log_n, l, c.nQ, c.nP, c.beta(l),
+                                                                      c.nQ + c.nP);
+}
+
+// Step 4: P limbs of both cx polynomials back to coefficients, times PHatInv.
+static void moddown_intt_p(const Context &c, const KsBuffers &b, int l, cudaStream_t s) {
+    const int qlp = l + c.nP;
+    const long long cps = (long long)qlp << c.log_n;
+    PtrStore cs{b.cx, cps, c.log_n};
+    ntt_inv(c, 2 * c.nP, QlpMap{c.nP, l, l, c.nQ}, PtrLoad{b.cx, cps, c.log_n}, cs,
+            ScaleStore{b.cx, cps, c.log_n, l, c.p_hat_inv.as<uint64_t>(), c.d_mods.as<Mod>()}, s);
+}
+
+// Step 5 over limbs [k0, k0 + nl) of both polynomials (limb k0 lands at out[0]),
+// intermediate in `mid` ([2][l][N]).
+template <class Base>
+static void moddown_ntt(const Context &c, const KsBuffers &b, uint64_t *mid, int l, int k0, int nl, uint64_t *out0,
+                        uint64_t *out1, Base base, cudaStream_t s) {
+    const int qlp = l + c.nP;
+    const long long cps = (long long)qlp << c.log_n;
+    PtrStore ms{mid, (long long)l << c.log_n, c.log_n};
+    PBconvLoad pl{b.cx, cps, c.p_mat.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, l, c.nP};
+    ModdownStore<Base> st{out0, out1, k0, b.cx, cps, c.p_inv.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, base};
+    ntt_fwd(c, 2 * nl, QlpMap{nl, k0, l, c.nQ}, pl, ms, st, s);
+}
+
+void ckks_keyswitch(const Context &c, const Workspace &w, uint64_t *ct, const uint64_t *c2, int l,
+                    const uint64_t *const *evk, cudaStream_t s) {
+    const KsBuffers b = ks_buffers(c, w);
+    const long long lps = (long long)l << c.log_n;
+    modup_ckks(c, b, PtrLoad{c2, lps, c.log_n}, l, s);
+    inner_product(c, b, PlainOwn{c2, c.log_n}, l, evk, s);
+    moddown_intt_p(c, b, l, s);
+    moddown_ntt(c, b, b.tm, l, 0, l, ct, ct + lps, InplaceBase{ct, lps, c.log_n}, s);
+}
+
+void ckks_mul_relin(const Context &c, const Workspace &w, uint64_t *ct1, const uint64_t *ct2, int l,
+                    const uint64_t *const *rlk, cudaStream_t s) {
+    const KsBuffers b = ks_buffers(c, w);
+    const long long lps = (long long)l << c.log_n;
+    const uint64_t *a1 = ct1 + lps, *b1 = ct2 + lps;
+    modup_ckks(c, b, TensorD2Load{a1, b1, c.d_mods.as<Mod>(), c.log_n}, l, s);
+    inner_product(c, b, TensorOwn{a1, b1, c.log_n}, l, rlk, s);
+    moddown_intt_p(c, b, l, s);
+    // poly 0 goes to scratch first: poly 1's base still reads a0 at every position
+    moddown_ntt(c, b, b.tm, l, 0, l, b.g, ct1 + lps, TensorBase{ct1, ct2, lps, c.log_n}, s);
+    cudaMemcpyAsync(ct1, b.g, lps * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);
+}
+
+// ------------------------------------------------------------------ rescale
+
+struct ConstTblMap {  // block b = polynomial b, one limb at table `tbl`
+    int tbl;
+    __device__ __forceinline__ bool operator()(int b, int &poly, int &k, int &t) const {
+        poly = b;
+        k = 0;
+        t = tbl;
+        return true;
+    }
+};
+
+// z (coefficient form, mod q_last) reduced into q_j
+struct ZLoad {
+    const uint64_t *z;
+    int log_n;
+    const Mod *mods;
+    __device__ __forceinline__ uint64_t operator()(int p, int, int tbl, uint32_t idx) const {
+        return reduce64(z[((size_t)p << log_n) + idx], mods[tbl]);
+    }
+};
+
+struct RescaleStore {  // out = (in - v) * q_last^-1
+    const uint64_t *in;
+    uint64_t *out;
+    long long ips, ops;
+    const uint64_t *iq;
+    const Mod *mods;
+    int log_n;
+    __device__ __forceinline__ void operator()(int p, int j, int tbl, uint32_t idx, uint64_t v) const {
+        const uint64_t q = mods[tbl].q;
+        const size_t o = ((size_t)j << log_n) + idx;
+        out[p * ops + o] = mul_shoup(sub_mod(in[p * ips + o], v, q), iq[2 * j], iq[2 * j + 1], q);
+    }
+};
+
+void ckks_rescale(const Context &c, const Workspace &w, const uint64_t *in, uint64_t *out, int size, int l,
+                  cudaStream_t s) {
+    const LevelTables &lt = *c.levels[l];
+    uint64_t *z = w.base;  // [size][N]
+    const long long ips = (long long)l << c.log_n, ops = (long long)(l - 1) << c.log_n;
+    const long long zps = 1LL << c.log_n;
+    PtrStore zs{z, zps, c.log_n};
+    ntt_inv(c, size, ConstTblMap{l - 1}, PtrLoad{in + ((size_t)(l - 1) << c.log_n), ips, c.log_n}, zs, zs, s);
+    PtrStore ms{out, ops, c.log_n};
+    ntt_fwd(c, size * (l - 1), SeqMap{l - 1, 0}, ZLoad{z, c.log_n, c.d_mods.as<Mod>()}, ms,
+            RescaleStore{in, out, ips, ops, lt.inv_qlast.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n}, s);
+}
+
+// HMult + relinearise + rescale.  With out_j = d_j + (cx_j - NTT(delta_j)) P^-1 and
+// z = iNTT(out_{l-1}), the rescale is (out_j - NTT(z mod q_j)) q_last^-1, and by linearity
+// of the NTT   res_j = (d_j + cx_j P^-1 - NTT(delta_j P^-1 + z mod q_j)) q_last^-1,
+// so after the last limb is finished (2 limbs) one forward NTT over 2(l-1) limbs completes
+// the whole operation.  Every step is exact modular arithmetic, so the result equals the
+// reference's multiply_and_relin_inplace + rescale_to_next_inplace word for word.
+struct RescaleFusedLoad {
+    const uint64_t *cx;
+    long long cps;
+    const uint64_t *pmat, *pinv, *z;
+    const Mod *mods;
+    int log_n, l, nP;
+    __device__ __forceinline__ uint64_t operator()(int t, int j, int tbl, uint32_t idx) const {
+        const Mod m = mods[tbl];
+        const uint64_t *yp = cx + t * cps + ((size_t)l << log_n) + idx;
+        const uint64_t *pm = pmat + (size_t)j * nP;
+        u128 acc{0, 0};
+        for (int k = 0; k < nP; k++) mac(acc, yp[(size_t)k << log_n], __ldg(pm + k));
+        const uint64_t delta = reduce128(acc, m);
+        const uint64_t dp = mul_shoup(delta, pinv[2 * j], pinv[2 * j + 1], m.q);
+        return add_mod(dp, reduce64(z[((size_t)t << log_n) + idx], m), m.q);
+    }
+};
+
+struct RescaleFusedStore {
+    uint64_t *out;
+    long long ops;
+    const uint64_t *cx;
+    long long cps;
+    const uint64_t *pinv, *iq;
+    const Mod *mods;
+    int log_n;
+    TensorBase base;
+    __device__ __forceinline__ void operator()(int t, int j, int tbl, uint32_t idx, uint64_t v) const {
+        const Mod m = mods[tbl];
+        const size_t o = ((size_t)j << log_n) + idx;
+        const uint64_t cp = mul_shoup(cx[t * cps + o], pinv[2 * j], pinv[2 * j + 1], m.q);
+        const uint64_t x = sub_mod(add_mod(base(t, j, m, idx), cp, m.q), v, m.q);
+        out[t * ops + o] = mul_shoup(x, iq[2 * j], iq[2 * j + 1], m.q);
+    }
+};
+
+void ckks_mul_relin_rescale(const Context &c, const Workspace &w, const uint64_t *ct1, const uint64_t *ct2,
+                            uint64_t *out, int l, const uint64_t *const *rlk, cudaStream_t s) {
+    const KsBuffers b = ks_buffers(c, w);
+    const LevelTables &lt = *c.levels[l];
+    const long long lps = (long long)l << c.log_n, zps = 1LL << c.log_n;
+    const uint64_t *a1 = ct1 + lps, *b1 = ct2 + lps;
+    modup_ckks(c, b, TensorD2Load{a1, b1, c.d_mods.as<Mod>(), c.log_n}, l, s);
+    inner_product(c, b, TensorOwn{a1, b1, c.log_n}, l, rlk, s);
+    moddown_intt_p(c, b, l, s);
+    // last limb of the relinearised product, both polynomials -> z (then coefficient form)
+    uint64_t *z = b.z;
+    moddown_ntt(c, b, b.tm, l, l - 1, 1, z, z + zps, TensorBase{ct1, ct2, lps, c.log_n}, s);
+    PtrStore zs{z, zps, c.log_n};
+    ntt_inv(c, 2, ConstTblMap{l - 1}, PtrLoad{z, zps, c.log_n}, zs, zs, s);
+    // everything else in one forward NTT over 2(l-1) limbs
+    const int qlp = l + c.nP;
+    const long long cps = (long long)qlp << c.log_n, ops = (long long)(l - 1) << c.log_n;
+    PtrStore ms{b.tm, ops, c.log_n};
+    RescaleFusedLoad ld{b.cx, cps, c.p_mat.as<uint64_t>(), c.p_inv.as<uint64_t>(), z, c.d_mods.as<Mod>(),
+                        c.log_n, l, c.nP};
+    RescaleFusedStore st{out, ops, b.cx, cps, c.p_inv.as<uint64_t>(), lt.inv_qlast.as<uint64_t>(),
+                         c.d_mods.as<Mod>(), c.log_n, TensorBase{ct1, ct2, lps, c.log_n}};
+    ntt_fwd(c, 2 * (l - 1), QlpMap{l - 1, 0, l, c.nQ}, ld, ms, st, s);
+}
+
+void ckks_tensor(const Context &c, uint64_t *ct1, const uint64_t *ct2, int l, cudaStream_t s);
+
+// ------------------------------------------------------------------ Galois
+
+// g[p][k][i] = src[p][k][perm[i]] for 2 polynomials of l limbs
+__global__ void galois_permute(uint64_t *dst, const uint64_t *src, const uint32_t *perm, int log_n, size_t total) {
+    const uint32_t nmask = (1u << log_n) - 1;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t idx = (uint32_t)e & nmask;
+        dst[e] = src[(e & ~(size_t)nmask) + __ldg(perm + idx)];
+    }
+}
+
+void ckks_apply_galois(const Context &c, const Workspace &w, uint64_t *ct, int l, const uint32_t *perm,
+                       const uint64_t *const *gk, cudaStream_t s) {
+    const KsBuffers b = ks_buffers(c, w);
+    const long long lps = (long long)l << c.log_n;
+    const size_t total = 2 * (size_t)lps;
+    galois_permute<<<grid_for(total, 256), 256, 0, s>>>(b.g, ct, perm, c.log_n, total);
+    const uint64_t *g1 = b.g + lps;
+    modup_ckks(c, b, PtrLoad{g1, lps, c.log_n}, l, s);
+    inner_product(c, b, PlainOwn{g1, c.log_n}, l, gk, s);
+    moddown_intt_p(c, b, l, s);
+    moddown_ntt(c, b, b.tm, l, 0, l, ct, ct + lps, FirstPolyBase{b.g, c.log_n}, s);
+}
+
+// ------------------------------------------------------------------ hoisting
+
+constexpr int kMaxSteps = 32;
+struct HoistSteps {
+    const uint32_t *perm[kMaxSteps];
+    const uint64_t *const *key[kMaxSteps];
+    int count;
+};
+
+// acc_t[jj] (+)= sum_s sum_d T_d[jj][perm_s[i]] * key_s,d[t][twr(jj)][i]; own limbs read c1.
+__global__ void __launch_bounds__(256) ks_inner_product_hoisted(uint64_t *cx, const uint64_t *tm,
+                                                                const uint64_t *c1, HoistSteps steps,
+                                                                const Mod *mods, int log_n, int l, int nQ,
+                                                                int alpha, int beta, int qp, bool accumulate) {
+    const int qlp = l + alpha;
+    const size_t total = (size_t)qlp << log_n;
+    const uint32_t nmask = (1u << log_n) - 1;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int jj = (int)(e >> log_n);
+        const uint32_t idx = (uint32_t)e & nmask;
+        const int tbl = jj < l ? jj : nQ + (jj - l);
+        const Mod m = mods[tbl];
+        const int own_d = jj < l ? jj / alpha : -1;
+        uint64_t r0 = accumulate ? cx[e] : 0, r1 = accumulate ? cx[total + e] : 0;
+        for (int st = 0; st < steps.count; st++) {
+            const uint32_t src = __ldg(steps.perm[st] + idx);
+            u128 a{0, 0}, b{0, 0};
+            int terms = 0;
+            for (int d = 0; d < beta; d++) {
+                const uint64_t x = d == own_d ? c1[((size_t)jj << log_n) + src]
+                                              : tm[(((size_t)d * qlp + jj) << log_n) + src];
+                const uint64_t *key = steps.key[st][d];
+                if (terms == 7) {
+                    a = u128{reduce128(a, m), 0};
+                    b = u128{reduce128(b, m), 0};
+                    terms = 1;
+                }
+                mac(a, x, __ldg(key + ((size_t)tbl << log_n) + idx));
+                mac(b, x, __ldg(key + ((size_t)(qp + tbl) << log_n) + idx));
+                terms++;
+            }
+            r0 = add_mod(r0, reduce128(a, m), m.q);
+            r1 = add_mod(r1, reduce128(b, m), m.q);
+        }
+        cx[e] = r0;
+        cx[total + e] = r1;
+    }
+}
+
+// acc0[i] = sum_s c0[perm_s[i]]
+__global__ void galois_sum(uint64_t *dst, const uint64_t *src, HoistSteps steps, const Mod *mods, int log_n,
+                           size_t total, bool accumulate) {
+    const uint32_t nmask = (1u << log_n) - 1;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t idx = (uint32_t)e & nmask;
+        const uint64_t q = mods[e >> log_n].q;
+        const size_t base = e & ~(size_t)nmask;
+        uint64_t r = accumulate ? dst[e] : 0;
+        for (int st = 0; st < steps.count; st++) r = add_mod(r, src[base + __ldg(steps.perm[st] + idx)], q);
+        dst[e] = r;
+    }
+}
+
+void ckks_hoisting(const Context &c, const Workspace &w, uint64_t *ct, int l, const std::vector<StepKey> &steps,
+                   cudaStream_t s) {
+    const KsBuffers b = ks_buffers(c, w);
+    const long long lps = (long long)l << c.log_n;
+    const uint64_t *c1 = ct + lps;
+    uint64_t *acc0 = b.g;
+    modup_ckks(c, b, PtrLoad{c1, lps, c.log_n}, l, s);
+    const int qlp = l + c.nP;
+    for (size_t s0 = 0; s0 < steps.size(); s0 += kMaxSteps) {
+        HoistSteps hs{};
+        hs.count = (int)std::min<size_t>(kMaxSteps, steps.size() - s0);
+        for (int i = 0; i < hs.count; i++) {
+            hs.perm[i] = steps[s0 + i].perm;
+            hs.key[i] = steps[s0 + i].key;
+        }
+        const bool acc = s0 > 0;
+        galois_sum<<<grid_for((size_t)lps, 256), 256, 0, s>>>(acc0, ct, hs, c.d_mods.as<Mod>(), c.log_n,
+                                                              (size_t)lps, acc);
+        ks_inner_product_hoisted<<<grid_for((size_t)qlp << c.log_n, 256), 256, 0, s>>>(
+                b.cx, b.tm, c1, hs, c.d_mods.as<Mod>(), c.log_n, l, c.nQ, c.nP, c.beta(l), c.nQ + c.nP, acc);
+    }
+    moddown_intt_p(c, b, l, s);
+    moddown_ntt(c, b, b.tm, l, 0, l, ct, ct + lps, FirstPolyBase{acc0, c.log_n}, s);
+}
+
+// ------------------------------------------------------------------ tensor (standalone)
+
+__global__ void tensor_2x2(uint64_t *ct1, const uint64_t *ct2, const Mod *mods, int log_n, size_t lps, bool square) {
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < lps; e += (size_t)gridDim.x * blockDim.x) {
+        const Mod m = mods[e >> log_n];
+        const uint64_t a0 = ct1[e], a1 = ct1[lps + e];
+        const uint64_t b0 = square ? a0 : ct2[e], b1 = square ? a1 : ct2[lps + e];
+        u128 acc = mul_wide(a0, b1);
+        mac(acc, a1, b0);
+        ct1[e] = mul_mod(a0, b0, m);
+        ct1[lps + e] = reduce128(acc, m);
+        ct1[2 * lps + e] = mul_mod(a1, b1, m);
+    }
+}
+
+void ckks_tensor(const Context &c, uint64_t *ct1, const uint64_t *ct2, int l, cudaStream_t s) {
+    const size_t lps = (size_t)l << c.log_n;
+    tensor_2x2<<<grid_for(lps, 256), 256, 0, s>>>(ct1, ct2, c.d_mods.as<Mod>(), c.log_n, lps, ct1 == ct2);
+}
+
+}  // namespace pfg

@@ -1,0 +1,229 @@
+"""Python bindings of the GB300 RNS ciphertext-arithmetic library (C ABI in
+include/phantom_gb300.h, shared library phantom-fhe_gb300/_build/libphantom_gb300.so).
+
+Device buffers are torch CUDA tensors of dtype int64 holding the uint64 residues bit for
+bit; layouts follow PhantomFHE (ciphertext [size][limbs][N], key [dnum][2][QP][N]).  The
+library is the only compute path: importing this module fails loudly when the shared
+library is missing, and every call raises on a non-zero status.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(HERE, "_build", "libphantom_gb300.so")
+
+SCHEME_BFV, SCHEME_CKKS = 1, 2
+MUL_TECH_HPS = 2
+
+_vp = ctypes.c_void_p
+_sz = ctypes.c_size_t
+_u64 = ctypes.c_uint64
+
+
+class FheError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"status {code}: {msg}")
+        self.code = code
+
+
+class InvalidArgument(FheError, ValueError):
+    pass
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("scheme", ctypes.c_int), ("mul_tech", ctypes.c_int), ("poly_modulus_degree", _u64),
+                ("coeff_modulus", ctypes.POINTER(_u64)), ("coeff_modulus_size", _sz),
+                ("special_modulus_size", _sz), ("plain_modulus", _u64),
+                ("galois_elts", ctypes.POINTER(ctypes.c_uint32)), ("galois_elts_size", _sz)]
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is not built; run __graft_entry__.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    L.fhe_last_error.restype = ctypes.c_char_p
+    L.fhe_galois_elt_from_step.restype = ctypes.c_uint32
+    L.fhe_galois_elt_from_step.argtypes = [ctypes.c_int, _u64]
+    L.fhe_create_coeff_modulus.argtypes = [_u64, ctypes.POINTER(ctypes.c_int), _sz, ctypes.POINTER(_u64)]
+    L.fhe_context_create.argtypes = [ctypes.POINTER(_Params), ctypes.POINTER(_vp)]
+    L.fhe_context_destroy.argtypes = [_vp]
+    L.fhe_context_sizes.argtypes = [_vp] + [ctypes.POINTER(_u64)] + [ctypes.POINTER(_sz)] * 4
+    L.fhe_context_moduli.argtypes = [_vp, ctypes.POINTER(_u64)]
+    L.fhe_context_galois_elts.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(_sz)]
+    L.fhe_workspace_bytes.restype = _sz
+    L.fhe_workspace_bytes.argtypes = [_vp]
+    L.fhe_workspace_create.argtypes = [_vp, ctypes.POINTER(_vp)]
+    L.fhe_workspace_destroy.argtypes = [_vp]
+    for f in ("fhe_ntt_forward", "fhe_ntt_inverse"):
+        getattr(L, f).argtypes = [_vp, _vp, _sz, _sz, _sz, _vp]
+    L.fhe_ckks_multiply.argtypes = [_vp, _vp, _vp, _sz, _vp]
+    L.fhe_keyswitch.argtypes = [_vp, _vp, _vp, _vp, _sz, _vp, _vp]
+    L.fhe_relinearize.argtypes = [_vp, _vp, _vp, _sz, _vp, _vp]
+    L.fhe_multiply_and_relin.argtypes = [_vp, _vp, _vp, _vp, _sz, _vp, _vp]
+    L.fhe_rescale_to_next.argtypes = [_vp, _vp, _vp, _vp, _sz, _sz, _vp]
+    L.fhe_bfv_mod_switch_to_next.argtypes = [_vp, _vp, _vp, _sz, _sz, _vp]
+    L.fhe_ckks_multiply_relin_rescale.argtypes = [_vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]
+    L.fhe_apply_galois.argtypes = [_vp, _vp, _vp, _sz, ctypes.c_uint32, _vp, _vp]
+    L.fhe_rotate.argtypes = [_vp, _vp, _vp, _sz, ctypes.c_int, ctypes.POINTER(_vp), _vp]
+    L.fhe_hoisting.argtypes = [_vp, _vp, _vp, _sz, ctypes.POINTER(ctypes.c_int), _sz, ctypes.POINTER(_vp), _vp]
+    return L
+
+
+lib = _load()
+
+
+def _check(rc):
+    if rc != 0:
+        msg = lib.fhe_last_error().decode()
+        raise (InvalidArgument if rc == -1 else FheError)(rc, msg)
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(stream):
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def create_coeff_modulus(n, bits):
+    out = (_u64 * len(bits))()
+    _check(lib.fhe_create_coeff_modulus(n, (ctypes.c_int * len(bits))(*bits), len(bits), out))
+    return [int(x) for x in out]
+
+
+def elt_from_step(step, n):
+    return int(lib.fhe_galois_elt_from_step(step, n))
+
+
+def to_device(a):
+    """numpy uint64 array -> torch int64 CUDA tensor (same bits)."""
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint64).view(np.int64)).cuda()
+
+
+def to_host(t):
+    return t.cpu().numpy().view(np.uint64)
+
+
+class KeySwitchKey:
+    """A key-switching key [dnum][2][QP][N] on the device plus the device array of its dnum
+    digit pointers (the layout of PhantomRelinKey::public_keys_ptr())."""
+
+    def __init__(self, data):
+        import torch
+        self.data = data
+        ptrs = [data[d].data_ptr() for d in range(data.shape[0])]
+        self.ptrs = torch.tensor(ptrs, dtype=torch.int64, device=data.device)
+
+    @property
+    def ptr(self):
+        return ctypes.c_void_p(self.ptrs.data_ptr())
+
+
+class Context:
+    """PhantomContext equivalent: QP = Q (data primes) then P (special primes)."""
+
+    def __init__(self, n, coeff_modulus, special_modulus_size, scheme=SCHEME_CKKS, plain_modulus=0,
+                 galois_elts=None, mul_tech=MUL_TECH_HPS):
+        mods = (_u64 * len(coeff_modulus))(*coeff_modulus)
+        elts = list(galois_elts or [])
+        p = _Params(scheme, mul_tech, n, mods, len(coeff_modulus), special_modulus_size, plain_modulus,
+                    (ctypes.c_uint32 * max(1, len(elts)))(*elts), len(elts))
+        h = _vp()
+        _check(lib.fhe_context_create(ctypes.byref(p), ctypes.byref(h)))
+        self._h = h
+        self.n = n
+        sizes = [_u64()] + [_sz() for _ in range(4)]
+        _check(lib.fhe_context_sizes(h, *[ctypes.byref(x) for x in sizes]))
+        self.size_q, self.size_p, self.size_r, self.dnum = (int(x.value) for x in sizes[1:])
+        out = (_u64 * (self.size_q + self.size_p + self.size_r))()
+        _check(lib.fhe_context_moduli(h, out))
+        self.moduli = [int(x) for x in out]
+        cnt = _sz()
+        _check(lib.fhe_context_galois_elts(h, None, ctypes.byref(cnt)))
+        e = (ctypes.c_uint32 * max(1, cnt.value))()
+        _check(lib.fhe_context_galois_elts(h, e, ctypes.byref(cnt)))
+        self.galois_elts = [int(x) for x in e[: cnt.value]]
+        self.scheme = scheme
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib.fhe_context_destroy(self._h)
+            self._h = None
+
+    def level(self, chain_index):
+        return self.size_q - (chain_index - 1)
+
+    def workspace_bytes(self):
+        return int(lib.fhe_workspace_bytes(self._h))
+
+    def workspace(self):
+        return Workspace(self)
+
+    # --- NTT
+    def ntt_forward(self, data, num_polys, limbs, start=0, stream=None):
+        _check(lib.fhe_ntt_forward(self._h, _ptr(data), num_polys, limbs, start, _stream(stream)))
+
+    def ntt_inverse(self, data, num_polys, limbs, start=0, stream=None):
+        _check(lib.fhe_ntt_inverse(self._h, _ptr(data), num_polys, limbs, start, _stream(stream)))
+
+    # --- evaluator
+    def ckks_multiply(self, ct1, ct2, chain_index, stream=None):
+        _check(lib.fhe_ckks_multiply(self._h, _ptr(ct1), _ptr(ct2), chain_index, _stream(stream)))
+
+    def keyswitch(self, ws, ct, c2, chain_index, key, stream=None):
+        _check(lib.fhe_keyswitch(self._h, ws._h, _ptr(ct), _ptr(c2), chain_index, key.ptr, _stream(stream)))
+
+    def relinearize(self, ws, ct, chain_index, key, stream=None):
+        _check(lib.fhe_relinearize(self._h, ws._h, _ptr(ct), chain_index, key.ptr, _stream(stream)))
+
+    def multiply_and_relin(self, ws, ct1, ct2, chain_index, key, stream=None):
+        _check(lib.fhe_multiply_and_relin(self._h, ws._h, _ptr(ct1), _ptr(ct2), chain_index, key.ptr,
+                                          _stream(stream)))
+
+    def rescale_to_next(self, ws, src, dst, size, chain_index, stream=None):
+        _check(lib.fhe_rescale_to_next(self._h, ws._h, _ptr(src), _ptr(dst), size, chain_index, _stream(stream)))
+
+    def bfv_mod_switch_to_next(self, src, dst, size, chain_index, stream=None):
+        _check(lib.fhe_bfv_mod_switch_to_next(self._h, _ptr(src), _ptr(dst), size, chain_index, _stream(stream)))
+
+    def multiply_relin_rescale(self, ws, ct1, ct2, out, chain_index, key, stream=None):
+        _check(lib.fhe_ckks_multiply_relin_rescale(self._h, ws._h, _ptr(ct1), _ptr(ct2), _ptr(out), chain_index,
+                                                   key.ptr, _stream(stream)))
+
+    def apply_galois(self, ws, ct, chain_index, elt, key, stream=None):
+        _check(lib.fhe_apply_galois(self._h, ws._h, _ptr(ct), chain_index, elt, key.ptr, _stream(stream)))
+
+    def _gk_array(self, galois_keys):
+        arr = (_vp * len(self.galois_elts))()
+        for i, k in enumerate(galois_keys):
+            arr[i] = None if k is None else k.ptrs.data_ptr()
+        return arr
+
+    def rotate(self, ws, ct, chain_index, step, galois_keys, stream=None):
+        _check(lib.fhe_rotate(self._h, ws._h, _ptr(ct), chain_index, step, self._gk_array(galois_keys),
+                              _stream(stream)))
+
+    def hoisting(self, ws, ct, chain_index, steps, galois_keys, stream=None):
+        st = (ctypes.c_int * len(steps))(*steps)
+        _check(lib.fhe_hoisting(self._h, ws._h, _ptr(ct), chain_index, st, len(steps), self._gk_array(galois_keys),
+                                _stream(stream)))
+
+
+class Workspace:
+    def __init__(self, ctx):
+        h = _vp()
+        _check(lib.fhe_workspace_create(ctx._h, ctypes.byref(h)))
+        self._h = h
+        self.ctx = ctx
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib.fhe_workspace_destroy(self._h)
+            self._h = None

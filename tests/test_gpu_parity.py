@@ -1,0 +1,324 @@
+"""GPU library vs the CPU oracle, word for word, through the C ABI (sm_103a).
+
+Inputs are seeded uniform residues; keys are uniform residues of the key layout
+[dnum][2][QP][N] (parity does not need well-formed keys — tests/test_oracle.py checks the
+key-switch algebra with real keys)."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+from oracle import oracle as O  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import phantom_gb300
+    return phantom_gb300
+
+
+def _ckks(pg, n, bits, special, galois_elts=None):
+    mods = pg.create_coeff_modulus(n, bits)
+    nq = len(bits) - special
+    ctx = pg.Context(n, mods, special, galois_elts=galois_elts)
+    oc = O.Context(n.bit_length() - 1, mods, nq, special)
+    return ctx, oc, mods, nq
+
+
+@pytest.fixture(scope="module")
+def small(pg):
+    ctx, oc, mods, nq = _ckks(pg, 4096, [60, 40, 40, 40, 40, 40, 60, 60], 2)
+    return ctx, oc, mods, nq, ctx.workspace()
+
+
+def _key(rng, mods, dnum, n):
+    return O.random_residues(rng, mods, n, 2 * dnum).reshape(dnum, 2, len(mods), n)
+
+
+def _eq(got_t, want, what):
+    got = got_t if isinstance(got_t, np.ndarray) else got_t.cpu().numpy().view(np.uint64)
+    want = np.asarray(want, dtype=np.uint64).reshape(got.shape)
+    bad = int((got != want).sum())
+    assert bad == 0, f"{what}: {bad} of {got.size} words differ"
+
+
+@pytest.mark.parametrize("log_n", [12, 13, 14, 15, 16, 17])
+def test_ntt_matches_oracle_all_degrees(pg, log_n):
+    n = 1 << log_n
+    mods = pg.create_coeff_modulus(n, [60, 50, 40])
+    ctx = pg.Context(n, mods, 1)
+    oc = O.Context(log_n, mods, 2, 1)
+    rng = np.random.default_rng(log_n)
+    a = O.random_residues(rng, mods, n, 2)
+    t = pg.to_device(a)
+    ctx.ntt_forward(t, 2, 3, 0)
+    want = np.stack([oc.ntt_fwd(a[p]) for p in range(2)])
+    _eq(t, want, "forward NTT")
+    ctx.ntt_inverse(t, 2, 3, 0)
+    _eq(t, a, "inverse NTT round trip")
+    b = pg.to_device(want)
+    ctx.ntt_inverse(b, 2, 3, 0)
+    _eq(b, a, "inverse NTT")
+
+
+def test_ntt_start_index_and_constant_inputs(small, pg):
+    ctx, oc, mods, nq, ws = small
+    n = ctx.n
+    for const in (1, 2):  # the reference's own round-trip test (test/ntt_test.cu:102-121)
+        a = np.full((1, 3, n), const, dtype=np.uint64)
+        t = pg.to_device(a)
+        ctx.ntt_forward(t, 1, 3, 4)
+        _eq(t, oc.ntt_fwd(a[0], [4, 5, 6]), "forward NTT from start index 4")
+        ctx.ntt_inverse(t, 1, 3, 4)
+        _eq(t, a, "round trip")
+
+
+def test_tensor(small, pg):
+    ctx, oc, mods, nq, ws = small
+    rng = np.random.default_rng(1)
+    for chain in (1, 3):
+        l = ctx.level(chain)
+        a = O.random_residues(rng, mods[:l], ctx.n, 2)
+        b = O.random_residues(rng, mods[:l], ctx.n, 2)
+        t1 = torch.zeros((3, l, ctx.n), dtype=torch.int64, device="cuda")
+        t1[:2] = pg.to_device(a)
+        ctx.ckks_multiply(t1, pg.to_device(b), chain)
+        _eq(t1, oc.tensor(l, a, b), "tensor")
+        t2 = torch.zeros((3, l, ctx.n), dtype=torch.int64, device="cuda")
+        t2[:2] = pg.to_device(a)
+        ctx.ckks_multiply(t2, t2, chain)
+        _eq(t2, oc.tensor(l, a, a), "square")
+
+
+@pytest.mark.parametrize("chain", [1, 2, 3, 4, 5, 6])
+def test_keyswitch_every_level(small, pg, chain):
+    ctx, oc, mods, nq, ws = small
+    l = ctx.level(chain)
+    rng = np.random.default_rng(10 + chain)
+    ct = O.random_residues(rng, mods[:l], ctx.n, 2)
+    c2 = O.random_residues(rng, mods[:l], ctx.n, 1)[0]
+    key = _key(rng, mods, ctx.dnum, ctx.n)
+    t = pg.to_device(ct)
+    ctx.keyswitch(ws, t, pg.to_device(c2), chain, pg.KeySwitchKey(pg.to_device(key)))
+    _eq(t, oc.keyswitch(l, ct, c2, key), f"keyswitch chain {chain}")
+
+
+def test_relinearize_and_multiply_and_relin(small, pg):
+    ctx, oc, mods, nq, ws = small
+    rng = np.random.default_rng(20)
+    key = _key(rng, mods, ctx.dnum, ctx.n)
+    k = pg.KeySwitchKey(pg.to_device(key))
+    for chain in (1, 4):
+        l = ctx.level(chain)
+        ct3 = O.random_residues(rng, mods[:l], ctx.n, 3)
+        t = pg.to_device(ct3)
+        ctx.relinearize(ws, t, chain, k)
+        _eq(t[:2], oc.relinearize(l, ct3, key), "relinearize")
+        a = O.random_residues(rng, mods[:l], ctx.n, 2)
+        b = O.random_residues(rng, mods[:l], ctx.n, 2)
+        ta = pg.to_device(a)
+        ctx.multiply_and_relin(ws, ta, pg.to_device(b), chain, k)
+        _eq(ta, oc.ckks_mul_relin(l, a, b, key), "multiply_and_relin")
+        ts = pg.to_device(a)
+        ctx.multiply_and_relin(ws, ts, ts, chain, k)
+        _eq(ts, oc.ckks_mul_relin(l, a, a, key), "square_and_relin")
+
+
+def test_rescale(small, pg):
+    ctx, oc, mods, nq, ws = small
+    rng = np.random.default_rng(30)
+    for chain, size in ((1, 2), (2, 3), (5, 2)):
+        l = ctx.level(chain)
+        ct = O.random_residues(rng, mods[:l], ctx.n, size)
+        out = torch.empty((size, l - 1, ctx.n), dtype=torch.int64, device="cuda")
+        ctx.rescale_to_next(ws, pg.to_device(ct), out, size, chain)
+        _eq(out, oc.rescale(l, ct), f"rescale chain {chain}")
+
+
+def test_multiply_relin_rescale_fused_equals_sequence(small, pg):
+    ctx, oc, mods, nq, ws = small
+    rng = np.random.default_rng(40)
+    key = _key(rng, mods, ctx.dnum, ctx.n)
+    k = pg.KeySwitchKey(pg.to_device(key))
+    for chain in (1, 3, 5):
+        l = ctx.level(chain)
+        a = O.random_residues(rng, mods[:l], ctx.n, 2)
+        b = O.random_residues(rng, mods[:l], ctx.n, 2)
+        out = torch.empty((2, l - 1, ctx.n), dtype=torch.int64, device="cuda")
+        ctx.multiply_relin_rescale(ws, pg.to_device(a), pg.to_device(b), out, chain, k)
+        want = oc.rescale(l, oc.ckks_mul_relin(l, a, b, key))
+        _eq(out, want, "fused multiply+relin+rescale vs oracle")
+        ta = pg.to_device(a)
+        ctx.multiply_and_relin(ws, ta, pg.to_device(b), chain, k)
+        out2 = torch.empty_like(out)
+        ctx.rescale_to_next(ws, ta, out2, 2, chain)
+        assert torch.equal(out, out2)
+
+
+def test_apply_galois_rotate_and_naf(small, pg):
+    ctx, oc, mods, nq, ws = small
+    rng = np.random.default_rng(50)
+    keys = [_key(rng, mods, ctx.dnum, ctx.n) for _ in ctx.galois_elts]
+    gks = [pg.KeySwitchKey(pg.to_device(k)) for k in keys]
+    for chain in (1, 3):
+        l = ctx.level(chain)
+        ct = O.random_residues(rng, mods[:l], ctx.n, 2)
+        for step in (1, -1, 2, 0):
+            elt = pg.elt_from_step(step, ctx.n)
+            idx = ctx.galois_elts.index(elt)
+            t = pg.to_device(ct)
+            ctx.rotate(ws, t, chain, step, gks)
+            _eq(t, oc.ckks_apply_galois(l, ct, elt, keys[idx]), f"rotate {step}")
+        # step 3 has no key: NAF 3 = 4 - 1 applies the -1 then the 4 rotation
+        t = pg.to_device(ct)
+        ctx.rotate(ws, t, chain, 3, gks)
+        want = ct
+        for s in (-1, 4):
+            elt = pg.elt_from_step(s, ctx.n)
+            want = oc.ckks_apply_galois(l, want, elt, keys[ctx.galois_elts.index(elt)])
+        _eq(t, want, "rotate 3 through NAF")
+
+
+def test_hoisting(small, pg):
+    ctx, oc, mods, nq, ws = small
+    rng = np.random.default_rng(60)
+    keys = [_key(rng, mods, ctx.dnum, ctx.n) for _ in ctx.galois_elts]
+    gks = [pg.KeySwitchKey(pg.to_device(k)) for k in keys]
+    steps = [1, 2, 4, -1]
+    for chain in (1, 2):
+        l = ctx.level(chain)
+        ct = O.random_residues(rng, mods[:l], ctx.n, 2)
+        t = pg.to_device(ct)
+        ctx.hoisting(ws, t, chain, steps, gks)
+        elts = [pg.elt_from_step(s, ctx.n) for s in steps]
+        want = oc.ckks_hoisting(l, ct, elts, [keys[ctx.galois_elts.index(e)] for e in elts])
+        _eq(t, want, "hoisting")
+
+
+def test_errors_are_reported_not_crashed(small, pg):
+    ctx, oc, mods, nq, ws = small
+    t = torch.zeros((2, nq, ctx.n), dtype=torch.int64, device="cuda")
+    with pytest.raises(pg.InvalidArgument):
+        ctx.rescale_to_next(ws, t, t, 2, nq)  # chain index nq has one limb: end of chain
+    with pytest.raises(pg.InvalidArgument):
+        ctx.ckks_multiply(t, t, 0)  # key level is not a data level
+    with pytest.raises(pg.FheError):
+        ctx.bfv_mod_switch_to_next(t, t, 2, 1)
+    with pytest.raises(pg.InvalidArgument):
+        pg.Context(4096, [97, 193], 1)  # not NTT-friendly for N = 4096
+
+
+# ---------------------------------------------------------------- BFV (HPS)
+
+@pytest.fixture(scope="module")
+def bfv_small(pg):
+    n, bits, special = 4096, [50, 50, 50, 50, 60, 60], 2
+    mods = pg.create_coeff_modulus(n, bits)
+    ctx = pg.Context(n, mods, special, scheme=pg.SCHEME_BFV, plain_modulus=65537)
+    oc = O.Context(12, mods, 4, special, 65537)
+    assert ctx.moduli[6:] == oc.r_moduli
+    return ctx, oc, mods, 4, ctx.workspace()
+
+
+def test_bfv_mul_relin_hps(bfv_small, pg):
+    ctx, oc, mods, nq, ws = bfv_small
+    rng = np.random.default_rng(70)
+    key = _key(rng, mods, ctx.dnum, ctx.n)
+    k = pg.KeySwitchKey(pg.to_device(key))
+    a = O.random_residues(rng, mods[:nq], ctx.n, 2)
+    b = O.random_residues(rng, mods[:nq], ctx.n, 2)
+    ta = pg.to_device(a)
+    ctx.multiply_and_relin(ws, ta, pg.to_device(b), 1, k)
+    _eq(ta, oc.bfv_mul_relin_hps(a, b, key), "BFV HPS multiply_and_relin")
+    ts = pg.to_device(a)
+    ctx.multiply_and_relin(ws, ts, ts, 1, k)
+    _eq(ts, oc.bfv_mul_relin_hps(a, a, key), "BFV HPS square_and_relin")
+
+
+def test_bfv_keyswitch_and_mod_switch(bfv_small, pg):
+    ctx, oc, mods, nq, ws = bfv_small
+    rng = np.random.default_rng(71)
+    key = _key(rng, mods, ctx.dnum, ctx.n)
+    ct = O.random_residues(rng, mods[:nq], ctx.n, 2)
+    c2 = O.random_residues(rng, mods[:nq], ctx.n, 1)[0]
+    t = pg.to_device(ct)
+    ctx.keyswitch(ws, t, pg.to_device(c2), 1, pg.KeySwitchKey(pg.to_device(key)))
+    _eq(t, oc.keyswitch(nq, ct, c2, key, scheme=1), "BFV keyswitch")
+    out = torch.empty((2, nq - 1, ctx.n), dtype=torch.int64, device="cuda")
+    ctx.bfv_mod_switch_to_next(pg.to_device(ct), out, 2, 1)
+    _eq(out, oc.divide_round_q_last(nq, ct), "BFV mod switch")
+
+
+def test_ntt_over_hps_r_base(bfv_small, pg):
+    ctx, oc, mods, nq, ws = bfv_small
+    rng = np.random.default_rng(72)
+    r = oc.r_moduli
+    a = O.random_residues(rng, r, ctx.n, 1)
+    t = pg.to_device(a)
+    ctx.ntt_forward(t, 1, len(r), nq + 2)
+    full = np.zeros((nq + len(r), ctx.n), dtype=np.uint64)
+    full[nq:] = a[0]
+    _eq(t, oc.ntt_fwd_qr(full)[nq:], "forward NTT over R")
+
+
+# ---------------------------------------------------------------- full-size parameter sets
+
+@pytest.fixture(scope="module")
+def ckks16(pg):
+    ctx, oc, mods, nq = _ckks(pg, 1 << 16, [60] + [40] * 29 + [60] * 5, 5)
+    return ctx, oc, mods, nq, ctx.workspace()
+
+
+def test_n16_l30_multiply_relin_rescale_matches_oracle(ckks16, pg):
+    ctx, oc, mods, nq, ws = ckks16
+    rng = np.random.default_rng(80)
+    key = _key(rng, mods, ctx.dnum, ctx.n)
+    l = nq
+    a = O.random_residues(rng, mods[:l], ctx.n, 2)
+    b = O.random_residues(rng, mods[:l], ctx.n, 2)
+    out = torch.empty((2, l - 1, ctx.n), dtype=torch.int64, device="cuda")
+    ctx.multiply_relin_rescale(ws, pg.to_device(a), pg.to_device(b), out, 1, pg.KeySwitchKey(pg.to_device(key)))
+    _eq(out, oc.rescale(l, oc.ckks_mul_relin(l, a, b, key)), "N=2^16 l=30 multiply+relin+rescale")
+
+
+def test_n16_rotate_matches_oracle(ckks16, pg):
+    ctx, oc, mods, nq, ws = ckks16
+    rng = np.random.default_rng(81)
+    elt = pg.elt_from_step(1, ctx.n)
+    idx = ctx.galois_elts.index(elt)
+    key = _key(rng, mods, ctx.dnum, ctx.n)
+    gks = [None] * len(ctx.galois_elts)
+    gks[idx] = pg.KeySwitchKey(pg.to_device(key))
+    chain = 8
+    l = ctx.level(chain)
+    ct = O.random_residues(rng, mods[:l], ctx.n, 2)
+    t = pg.to_device(ct)
+    ctx.rotate(ws, t, chain, 1, gks)
+    _eq(t, oc.ckks_apply_galois(l, ct, elt, key), "N=2^16 rotate(1)")
+
+
+def test_n16_ntt_round_trip_all_35_limbs(ckks16, pg):
+    ctx, oc, mods, nq, ws = ckks16
+    rng = np.random.default_rng(82)
+    a = O.random_residues(rng, mods, ctx.n, 2)
+    t = pg.to_device(a)
+    ctx.ntt_forward(t, 2, len(mods), 0)
+    ctx.ntt_inverse(t, 2, len(mods), 0)
+    _eq(t, a, "N=2^16 round trip")
+
+
+def test_n15_bfv_hps_multiply_relin_matches_oracle(pg):
+    n, bits, special = 1 << 15, [50] * 16 + [60, 60], 2
+    mods = pg.create_coeff_modulus(n, bits)
+    ctx = pg.Context(n, mods, special, scheme=pg.SCHEME_BFV, plain_modulus=65537)
+    oc = O.Context(15, mods, 16, special, 65537)
+    ws = ctx.workspace()
+    rng = np.random.default_rng(83)
+    key = _key(rng, mods, ctx.dnum, n)
+    a = O.random_residues(rng, mods[:16], n, 2)
+    b = O.random_residues(rng, mods[:16], n, 2)
+    ta = pg.to_device(a)
+    ctx.multiply_and_relin(ws, ta, pg.to_device(b), 1, pg.KeySwitchKey(pg.to_device(key)))
+    _eq(ta, oc.bfv_mul_relin_hps(a, b, key), "N=2^15 BFV HPS multiply_and_relin")
