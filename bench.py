@@ -1,0 +1,329 @@
+#!/usr/bin/env python3
+"""Benchmark: CKKS HMult + relinearise + rescale at N = 2^16, 30 data primes (1x60 + 29x40),
+5 special primes (dnum = 6), on one GB300 per rank.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one HMult+relin+rescale of one ciphertext pair at chain index 1 (l = 30), batch 1,
+through the library's C ABI (fhe_ckks_multiply_relin_rescale).  The per-step working set is
+283 MB (2 ciphertexts + the 220 MB relinearisation key) > the 129 MB L2, and 4 ciphertext
+pairs are cycled.  Inputs are seeded synthetic residues (uniform in [0, q_i)); keys are
+uniform residues of the key layout.  `--impl reference` times the CPU restatement of the
+same operation (the reference has no CPU implementation of this path) on the host cores.
+Multi-GPU runs are independent replicas (the path has no cross-GPU exchange).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "phantom-fhe_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+N = 1 << 16
+BITS = [60] + [40] * 29 + [60] * 5
+SPECIAL = 5
+CHAIN = 1
+PAIRS = 4
+METRIC = "CKKS HMult+relin+rescale ops/s (N=2^16, l=30, dnum=6, bit-exact)"
+CONFIG = {"workload": "ckks_hmult_relin_rescale", "poly_degree": N, "data_primes": "1x60+29x40",
+          "special_primes": "5x60", "dnum": 6, "level": 30, "batch": 1,
+          "l2": "per-step working set 283 MB (> 129 MB L2); 4 ciphertext pairs cycled"}
+
+
+def dist_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def random_residues(rng, moduli, n, polys):
+    out = np.empty((polys, len(moduli), n), dtype=np.uint64)
+    for k, q in enumerate(moduli):
+        out[:, k, :] = rng.integers(0, q, size=(polys, n), dtype=np.uint64)
+    return out
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+class Clocks:
+    """nvidia-smi sampler running while the timed regions run."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                       "-lms", "100", "-i", str(gpu)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() in ("active", "1"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_baseline_sample(mods, nq, threads):
+    """One full HMult+relin+rescale on the host cores with the CPU restatement."""
+    from oracle import oracle as O
+    O.set_threads(threads)
+    oc = O.Context(16, mods, nq, SPECIAL)
+    rng = np.random.default_rng(7)
+    l = nq
+    a = random_residues(rng, mods[:l], N, 2)
+    b = random_residues(rng, mods[:l], N, 2)
+    dnum = (nq + SPECIAL - 1) // SPECIAL
+    key = random_residues(rng, mods, N, 2 * dnum).reshape(dnum, 2, len(mods), N)
+    oc.rescale(l, oc.ckks_mul_relin(l, a, b, key))  # warm-up (page-in, thread pool)
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        oc.rescale(l, oc.ckks_mul_relin(l, a, b, key))
+        reps += 1
+        if time.perf_counter() - t0 > 10.0 or reps >= 8:
+            break
+    dt = time.perf_counter() - t0
+    return reps / dt, reps, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    mods = O.create_coeff_modulus(N, BITS)
+    nq = len(BITS) - SPECIAL
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    oc = O.Context(16, mods, nq, SPECIAL)
+    rng = np.random.default_rng(7)
+    l = nq
+    a = random_residues(rng, mods[:l], N, 2)
+    b = random_residues(rng, mods[:l], N, 2)
+    dnum = (nq + SPECIAL - 1) // SPECIAL
+    key = random_residues(rng, mods, N, 2 * dnum).reshape(dnum, 2, len(mods), N)
+    for _ in range(min(args.warmup, 1)):
+        oc.rescale(l, oc.ckks_mul_relin(l, a, b, key))
+    # each step is the full operation; the step count is capped so the run stays bounded
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < args.steps:
+        oc.rescale(l, oc.ckks_mul_relin(l, a, b, key))
+        steps += 1
+        if time.perf_counter() - t0 > 60.0:
+            break
+    dt = time.perf_counter() - t0
+    value = steps / dt
+    sample = f"{steps} full HMult+relin+rescale ops at N=2^16, l=30 (of {args.steps} requested)"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "ops/s", "n_gpus": world,
+            "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1000 * dt / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic", "config": CONFIG,
+            "cpu_baseline": {"value": value, "unit": "ops/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "ops/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import phantom_gb300 as pg
+    lib = pg.lib
+    lib.fhe_kernel_launches.restype = ctypes.c_uint64
+
+    mods = pg.create_coeff_modulus(N, BITS)
+    nq = len(BITS) - SPECIAL
+    l = nq
+    ctx = pg.Context(N, mods, SPECIAL)
+    ws = ctx.workspace()
+    rng = np.random.default_rng(1000 + rank)
+    key = pg.KeySwitchKey(pg.to_device(random_residues(rng, mods, N, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), N)))
+    elt1 = pg.elt_from_step(1, N)
+    gks = [None] * len(ctx.galois_elts)
+    gks[ctx.galois_elts.index(elt1)] = key
+    a = [pg.to_device(random_residues(rng, mods[:l], N, 2)) for _ in range(PAIRS)]
+    b = [pg.to_device(random_residues(rng, mods[:l], N, 2)) for _ in range(PAIRS)]
+    out = [torch.empty((2, l - 1, N), dtype=torch.int64, device="cuda") for _ in range(PAIRS)]
+    stream = torch.cuda.current_stream()
+
+    def step(i):
+        ctx.multiply_relin_rescale(ws, a[i % PAIRS], b[i % PAIRS], out[i % PAIRS], CHAIN, key, stream)
+
+    def timed(fn, k):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for i in range(k):
+            fn(i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1000.0
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    if args.case == "ntt":  # profiling case: forward NTT of 8 polys x 35 limbs (147 MB)
+        big = torch.randint(0, 1 << 40, (8, len(mods), N), dtype=torch.int64, device="cuda")
+        for _ in range(args.warmup + args.steps):
+            ctx.ntt_forward(big, 8, len(mods), 0, stream)
+        torch.cuda.synchronize()
+        return
+    for i in range(max(args.warmup, 3)):
+        step(i)
+    torch.cuda.synchronize()
+    if args.case == "hmult":  # profiling case: HMult+relin+rescale steps only
+        for i in range(args.steps):
+            step(i)
+        torch.cuda.synchronize()
+        return
+
+    clocks = Clocks(local)
+    time.sleep(0.3)
+    barrier()
+    l0 = lib.fhe_kernel_launches()
+    t = timed(step, args.steps)
+    launches = lib.fhe_kernel_launches() - l0
+    barrier()
+    if world > 1:
+        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    value = args.steps * world / t
+
+    # companion measurements on the same parameters (same timing rules)
+    k2 = max(args.steps // 2, 10)
+    ct = pg.to_device(random_residues(rng, mods[:l], N, 2))
+    c2 = pg.to_device(random_residues(rng, mods[:l], N, 1)[0])
+    t_rot = timed(lambda i: ctx.rotate(ws, ct, CHAIN, 1, gks, stream), k2)
+    t_ks = timed(lambda i: ctx.keyswitch(ws, ct, c2, CHAIN, key, stream), k2)
+    # NTT throughput: 64 polynomials x 35 limbs (1.17 GB > 4x L2), forward transform
+    polys, limbs = 64, len(mods)
+    big = torch.randint(0, 1 << 40, (polys, limbs, N), dtype=torch.int64, device="cuda")
+    ctx.ntt_forward(big, polys, limbs, 0, stream)
+    kn = 10
+    t_ntt = timed(lambda i: ctx.ntt_forward(big, polys, limbs, 0, stream), kn) / kn
+    ntt_bytes = 16 * N * limbs * polys
+    ntt_gbs = ntt_bytes / t_ntt / 1e9
+    del big
+
+    # end to end through the C ABI with host buffers: H2D of both inputs, D2H of the result
+    pin_a = [torch.empty((2, l, N), dtype=torch.int64).pin_memory() for _ in range(PAIRS)]
+    pin_b = [torch.empty((2, l, N), dtype=torch.int64).pin_memory() for _ in range(PAIRS)]
+    pin_o = [torch.empty((2, l - 1, N), dtype=torch.int64).pin_memory() for _ in range(PAIRS)]
+    for i in range(PAIRS):
+        pin_a[i].copy_(a[i].cpu())
+        pin_b[i].copy_(b[i].cpu())
+    da = torch.empty((2, l, N), dtype=torch.int64, device="cuda")
+    db = torch.empty((2, l, N), dtype=torch.int64, device="cuda")
+    do = torch.empty((2, l - 1, N), dtype=torch.int64, device="cuda")
+
+    def e2e_step(i):
+        da.copy_(pin_a[i % PAIRS], non_blocking=True)
+        db.copy_(pin_b[i % PAIRS], non_blocking=True)
+        ctx.multiply_relin_rescale(ws, da, db, do, CHAIN, key, stream)
+        pin_o[i % PAIRS].copy_(do, non_blocking=True)
+
+    for i in range(3):
+        e2e_step(i)
+    barrier()
+    t_e2e = timed(e2e_step, args.steps)
+    barrier()
+    if world > 1:
+        tt = torch.tensor([t_e2e], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    ck = clocks.stop()
+
+    peak, peak_kind = measured_peaks()
+    traffic = profile_traffic().get("ntt_forward_64x35_n16")
+    line = {"metric": METRIC, "value": value, "unit": "ops/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": 1000 * t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic", "config": CONFIG,
+            "clocks": ck,
+            "e2e": {"value": args.steps * world / t_e2e, "unit": "ops/s",
+                    "h2d_bytes_per_step": 2 * 2 * l * N * 8, "d2h_bytes_per_step": 2 * (l - 1) * N * 8},
+            "gpu_launches": int(launches),
+            "roofline": {"kernel": "ntt forward (column + row pass), 64 polys x 35 limbs, N=2^16",
+                         "bound": "hbm", "achieved": ntt_gbs, "peak": peak, "unit": "GB/s",
+                         "frac": ntt_gbs / peak, "peak_source": peak_kind,
+                         "algorithmic_bytes": ntt_bytes, "traffic": traffic},
+            "extra": {"hrotate_step1_per_s": k2 * world / t_rot, "keyswitch_per_s": k2 * world / t_ks,
+                      "ntt_forward_ms_64x35": 1000 * t_ntt,
+                      "hmult_relin_rescale_algorithmic_bytes": 313524224,
+                      "hmult_hbm_frac": 313524224 * value / world / 1e9 / peak,
+                      "launches_per_step": launches / args.steps}}
+    if rank == 0 and world == 1:
+        v, reps, dt = cpu_baseline_sample(mods, nq, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": v, "unit": "ops/s", "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": f"{reps} full HMult+relin+rescale ops at N=2^16, l=30 in {dt:.1f} s"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--case", choices=["full", "hmult", "ntt"], default="full",
+                    help="hmult / ntt: run only that part (for profiler captures), print nothing")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

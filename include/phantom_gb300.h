@@ -62,6 +62,10 @@ typedef struct fhe_params {
 
 const char *fhe_last_error(void);
 
+/* Number of CUDA kernels this library has launched so far in the process (all threads).
+ * No counterpart in the reference; used to report launches per operation. */
+uint64_t fhe_kernel_launches(void);
+
 /* CoeffModulus::Create (include/host/modulus.h:295, src/host/modulus.cu:80-111). */
 int fhe_create_coeff_modulus(uint64_t poly_modulus_degree, const int *bit_sizes, size_t count, uint64_t *out);
 

@@ -1,6 +1,7 @@
 // capi.cu — the extern "C" boundary (include/phantom_gb300.h): argument checks with the
 // reference's error classes, chain-index bookkeeping, and dispatch to the kernels.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <new>
 #include <stdexcept>
@@ -92,9 +93,16 @@ cudaStream_t st(void *s) { return static_cast<cudaStream_t>(s); }
 
 }  // namespace
 
+namespace pfg {
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+}  // namespace pfg
+
 extern "C" {
 
 const char *fhe_last_error(void) { return g_last_error.c_str(); }
+
+uint64_t fhe_kernel_launches(void) { return pfg::g_launches.load(std::memory_order_relaxed); }
 
 int fhe_create_coeff_modulus(uint64_t poly_modulus_degree, const int *bit_sizes, size_t count, uint64_t *out) {
     return guarded([&] {

@@ -7,6 +7,9 @@
 
 namespace pfg {
 
+// Kernel launches issued by this library (all threads), for the benchmark's launch count.
+void count_launch(unsigned n = 1);
+
 // ---------------------------------------------------------------- limb maps
 // A map turns blockIdx.y into (poly, limb k, prime table index) and may idle a block.
 
@@ -85,6 +88,7 @@ template <bool FWD, bool LAST, class Map, class Load, class Store>
 void col_pass(const Context &c, int blocks, Map m, Load ld, Store st, cudaStream_t s) {
     dim3 grid((unsigned)(c.n / kTileElems), (unsigned)blocks);
     const NttTables T = c.ntt();
+    count_launch();
     switch (c.l1()) {
         case 6: ntt_col_pass<6, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
         case 7: ntt_col_pass<7, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
@@ -97,6 +101,7 @@ template <bool FWD, bool LAST, class Map, class Load, class Store>
 void row_pass(const Context &c, int blocks, Map m, Load ld, Store st, cudaStream_t s) {
     dim3 grid((unsigned)(c.n / kTileElems), (unsigned)blocks);
     const NttTables T = c.ntt();
+    count_launch();
     switch (c.l2()) {
         case 6: ntt_row_pass<6, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
         case 7: ntt_row_pass<7, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;

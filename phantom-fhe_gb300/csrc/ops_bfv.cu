@@ -215,6 +215,7 @@ static void bfv_keyswitch_to(const Context &c, uint64_t *scratch, uint64_t *out,
                     l, alpha, qlp};
     ntt_fwd(c, beta * qlp, ModupMap{qlp, l, c.nQ, alpha, false}, bl, ts, ts, s);
     const size_t work = ((size_t)qlp << c.log_n) / 2;
+    count_launch();
     ks_inner_product<NoOwn, true><<<grid_for_bfv(work, 256), 256, 0, s>>>(cx, tm, NoOwn{}, evk, c.d_mods.as<Mod>(),
                                                                           c.log_n, l, c.nQ, alpha, beta,
                                                                           c.nQ + c.nP);
@@ -222,6 +223,7 @@ static void bfv_keyswitch_to(const Context &c, uint64_t *scratch, uint64_t *out,
     ntt_inv(c, 2 * qlp, QlpMap{qlp, 0, l, c.nQ}, PtrLoad{cx, tps, c.log_n}, cs,
             BfvCxStore{cx, tps, c.log_n, l, c.p_hat_inv.as<uint64_t>(), c.d_mods.as<Mod>()}, s);
     const long long lps = (long long)l << c.log_n;
+    count_launch();
     bfv_moddown_combine<<<grid_for_bfv((size_t)2 * lps, 256), 256, 0, s>>>(
             out, lps, base, lps, cx, tps, c.p_mat.as<uint64_t>(), c.p_inv.as<uint64_t>(), c.d_mods.as<Mod>(), l,
             c.nP, c.log_n);
@@ -247,12 +249,14 @@ void bfv_mul_relin_hps(const Context &c, const Workspace &w, uint64_t *ct1, cons
     if (sm_q > 48 * 1024) cudaFuncSetAttribute(hps_bconv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_q);
     if (sm_r > 48 * 1024)
         cudaFuncSetAttribute(hps_scale_round_to_q, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_r);
+    count_launch();
     hps_bconv<<<g, 128, sm_q, s>>>(ea + qps, qrps, ct1, qps, mods, 0, nQ, rbase, nR, c.hps_q_hat_inv.as<uint64_t>(),
                                    c.hps_q_inv.as<double>(), c.hps_q2r_mat.as<uint64_t>(),
                                    c.hps_q2r_alpha.as<uint64_t>(), c.log_n);
     const uint64_t *ebp = ea;
     if (!square) {
         cudaMemcpy2DAsync(eb, qrps * 8, ct2, qps * 8, qps * 8, 2, cudaMemcpyDeviceToDevice, s);
+        count_launch();
         hps_bconv<<<g, 128, sm_q, s>>>(eb + qps, qrps, ct2, qps, mods, 0, nQ, rbase, nR,
                                        c.hps_q_hat_inv.as<uint64_t>(), c.hps_q_inv.as<double>(),
                                        c.hps_q2r_mat.as<uint64_t>(), c.hps_q2r_alpha.as<uint64_t>(), c.log_n);
@@ -266,6 +270,7 @@ void bfv_mul_relin_hps(const Context &c, const Workspace &w, uint64_t *ct1, cons
     ntt_inv(c, 3 * qr, qm, TensorQrLoad{ea, ebp, qrps, mods, c.log_n}, t3s, t3s, s);
     // 3. scale and round to R, then back to Q
     dim3 g3((unsigned)(n / 128), 3);
+    count_launch();
     hps_scale_round_to_q<<<g3, 128, sm_r, s>>>(o3, qps, t3, qrps, mods, nQ, rbase, nR, c.hps_frac.as<double>(),
                                                 c.hps_modr.as<uint64_t>(), c.hps_r_hat_inv.as<uint64_t>(),
                                                 c.hps_r_inv.as<double>(), c.hps_r2q_mat.as<uint64_t>(),
@@ -291,6 +296,7 @@ __global__ void divide_round_q_last(uint64_t *out, const uint64_t *in, const uin
 
 void bfv_divide_round_q_last(const Context &c, const uint64_t *in, uint64_t *out, int size, int l, cudaStream_t s) {
     const size_t total = (size_t)size * ((size_t)(l - 1) << c.log_n);
+    count_launch();
     divide_round_q_last<<<grid_for_bfv(total, 256), 256, 0, s>>>(out, in, c.levels[l]->inv_qlast.as<uint64_t>(),
                                                                   c.d_mods.as<Mod>(), l, c.log_n, total);
 }

@@ -202,6 +202,7 @@ static void inner_product(const Context &c, const KsBuffers &b, Own own, int l, 
                           cudaStream_t s) {
     const int qlp = l + c.nP;
     const size_t work = ((size_t)qlp << c.log_n) / 2;
+    count_launch();
     ks_inner_product<Own, false><<<grid_for(work, 256), 256, 0, s>>>(b.cx, b.tm, own, evk, c.d_mods.as<Mod>(),
                                                                       c.log_n, l, c.nQ, c.nP, c.beta(l),
                                                                       c.nQ + c.nP);
@@ -386,6 +387,7 @@ void ckks_apply_galois(const Context &c, const Workspace &w, uint64_t *ct, int l
     const KsBuffers b = ks_buffers(c, w);
     const long long lps = (long long)l << c.log_n;
     const size_t total = 2 * (size_t)lps;
+    count_launch();
     galois_permute<<<grid_for(total, 256), 256, 0, s>>>(b.g, ct, perm, c.log_n, total);
     const uint64_t *g1 = b.g + lps;
     modup_ckks(c, b, PtrLoad{g1, lps, c.log_n}, l, s);
@@ -473,8 +475,10 @@ void ckks_hoisting(const Context &c, const Workspace &w, uint64_t *ct, int l, co
             hs.key[i] = steps[s0 + i].key;
         }
         const bool acc = s0 > 0;
+        count_launch();
         galois_sum<<<grid_for((size_t)lps, 256), 256, 0, s>>>(acc0, ct, hs, c.d_mods.as<Mod>(), c.log_n,
                                                               (size_t)lps, acc);
+        count_launch();
         ks_inner_product_hoisted<<<grid_for((size_t)qlp << c.log_n, 256), 256, 0, s>>>(
                 b.cx, b.tm, c1, hs, c.d_mods.as<Mod>(), c.log_n, l, c.nQ, c.nP, c.beta(l), c.nQ + c.nP, acc);
     }
@@ -499,6 +503,7 @@ __global__ void tensor_2x2(uint64_t *ct1, const uint64_t *ct2, const Mod *mods, 
 
 void ckks_tensor(const Context &c, uint64_t *ct1, const uint64_t *ct2, int l, cudaStream_t s) {
     const size_t lps = (size_t)l << c.log_n;
+    count_launch();
     tensor_2x2<<<grid_for(lps, 256), 256, 0, s>>>(ct1, ct2, c.d_mods.as<Mod>(), c.log_n, lps, ct1 == ct2);
 }
 
