@@ -44,106 +44,128 @@ __host__ __device__ constexpr int ntt_phase_start(int lm, int ph) {
 }
 __host__ __device__ constexpr int pad_idx(int x) { return x + (x >> 4); }
 
-// One register phase of the forward transform on vector `vec` (padded shared memory):
-// local stages [sa, sa + K).  tb(s) = twiddle-table base for local stage s:
-// (1 << (loff + s)) + (row << s).
+// Position inside the vector of member j of thread u's gg-th butterfly group in the phase
+// covering local stages [SA, SA + K): groups are {(hi * 2^K + j) * tmin + lo}, tmin = M >> (SA+K).
 template <int LM, int K, int SA>
-__device__ __forceinline__ void fwd_phase(uint64_t *vec, int u, const TwPair *tw, int loff, uint32_t row,
-                                          uint64_t q) {
-    constexpr int sa = SA;
-    constexpr int M = 1 << LM;
-    constexpr int TPV = M / 16;  // threads per vector
-    constexpr int G = 16 >> K;   // butterfly groups per thread
-    constexpr int GS = 1 << K;   // group size
-    const int tmin = M >> (sa + K);
+__device__ __forceinline__ int grp_elem(int u, int gg, int j) {
+    constexpr int M = 1 << LM, TPV = M / 16, TMIN = M >> (SA + K);
+    const int g = u + gg * TPV;
+    return ((g / TMIN) * (1 << K) + j) * TMIN + (g % TMIN);
+}
+
+// Forward (Cooley-Tukey, Harvey lazy: inputs < 4q, outputs < 4q) stages [SA, SA+K) on the
+// 16 registers of thread u.  Twiddle for local stage s of vector `row`:
+// tw[(1 << (loff + s)) + (row << s) + (element >> (LM - s))].  All of a group's twiddle pairs
+// are fetched before its butterflies so their latency overlaps.
+template <int LM, int K, int SA>
+__device__ __forceinline__ void fwd_regs(uint64_t (&x)[16], int u, const TwPair *tw, int loff, uint32_t row,
+                                         uint64_t q) {
+    constexpr int M = 1 << LM, TPV = M / 16, G = 16 >> K, GS = 1 << K, TMIN = M >> (SA + K);
     const uint64_t q2 = 2 * q;
 #pragma unroll
     for (int gg = 0; gg < G; gg++) {
-        const int g = u + gg * TPV;
-        const int hi = g / tmin, lo = g % tmin;
-        uint64_t x[GS];
+        const uint32_t hi = (uint32_t)((u + gg * TPV) / TMIN);
+        TwPair w[GS - 1];
 #pragma unroll
-        for (int j = 0; j < GS; j++) x[j] = vec[pad_idx((hi * GS + j) * tmin + lo)];
+        for (int k = 0; k < K; k++)
+#pragma unroll
+            for (int m = 0; m < (1 << k); m++)
+                w[(1 << k) - 1 + m] = ld_tw(tw, (1u << (loff + SA + k)) + (row << (SA + k)) + (hi << k) + m);
+        uint64_t *y = x + gg * GS;
 #pragma unroll
         for (int k = 0; k < K; k++) {
             const int h = GS >> (k + 1);
-            const uint32_t tb = (1u << (loff + sa + k)) + (row << (sa + k)) + ((uint32_t)hi << k);
 #pragma unroll
             for (int j = 0; j < GS; j++) {
                 if (j & h) continue;
-                const TwPair w = ld_tw(tw, tb + (j >> (K - k)));
-                uint64_t a = csub(x[j], q2);
-                uint64_t t = mul_shoup_lazy(x[j + h], w.w, w.ws, q);
-                x[j] = a + t;
-                x[j + h] = a - t + q2;
+                const TwPair t = w[(1 << k) - 1 + (j >> (K - k))];
+                const uint64_t a = csub(y[j], q2);
+                const uint64_t b = mul_shoup_lazy(y[j + h], t.w, t.ws, q);
+                y[j] = a + b;
+                y[j + h] = a - b + q2;
             }
         }
-#pragma unroll
-        for (int j = 0; j < GS; j++) vec[pad_idx((hi * GS + j) * tmin + lo)] = x[j];
     }
 }
 
-// One register phase of the inverse transform: local stages sa+K-1 down to sa.
-// glob0 = global stage index of local stage 0; the global stage 0 butterfly applies n^-1
-// to its sum output (its difference twiddle already carries n^-1).
+// Inverse (Gentleman-Sande, inputs < 2q, outputs < 2q) stages SA+K-1 .. SA.  The global
+// stage-0 butterfly (loff == 0, local stage 0) scales its sum by n^-1; its difference twiddle
+// already carries n^-1 (src/host/ntt.cu:53-55).
 template <int LM, int K, int SA>
-__device__ __forceinline__ void inv_phase(uint64_t *vec, int u, const TwPair *itw, int loff, uint32_t row,
-                                          uint64_t q, uint64_t ninv, uint64_t ninv_s) {
-    constexpr int sa = SA;
-    constexpr int M = 1 << LM;
-    constexpr int TPV = M / 16;
-    constexpr int G = 16 >> K;
-    constexpr int GS = 1 << K;
-    const int tmin = M >> (sa + K);
+__device__ __forceinline__ void inv_regs(uint64_t (&x)[16], int u, const TwPair *itw, int loff, uint32_t row,
+                                         uint64_t q, uint64_t ninv, uint64_t ninv_s) {
+    constexpr int M = 1 << LM, TPV = M / 16, G = 16 >> K, GS = 1 << K, TMIN = M >> (SA + K);
     const uint64_t q2 = 2 * q;
 #pragma unroll
     for (int gg = 0; gg < G; gg++) {
-        const int g = u + gg * TPV;
-        const int hi = g / tmin, lo = g % tmin;
-        uint64_t x[GS];
+        const uint32_t hi = (uint32_t)((u + gg * TPV) / TMIN);
+        TwPair w[GS - 1];
 #pragma unroll
-        for (int j = 0; j < GS; j++) x[j] = vec[pad_idx((hi * GS + j) * tmin + lo)];
+        for (int k = 0; k < K; k++)
+#pragma unroll
+            for (int m = 0; m < (1 << k); m++)
+                w[(1 << k) - 1 + m] = ld_tw(itw, (1u << (loff + SA + k)) + (row << (SA + k)) + (hi << k) + m);
+        uint64_t *y = x + gg * GS;
 #pragma unroll
         for (int k = K - 1; k >= 0; k--) {
             const int h = GS >> (k + 1);
-            const uint32_t tb = (1u << (loff + sa + k)) + (row << (sa + k)) + ((uint32_t)hi << k);
-            const bool first_stage = (sa + k == 0) && (loff == 0);
+            const bool first_stage = (SA + k == 0) && (loff == 0);
 #pragma unroll
             for (int j = 0; j < GS; j++) {
                 if (j & h) continue;
-                const TwPair w = ld_tw(itw, tb + (j >> (K - k)));
-                uint64_t a = x[j], b = x[j + h];
-                uint64_t s = a + b;
-                if (first_stage)
-                    s = mul_shoup_lazy(s, ninv, ninv_s, q);
-                else
-                    s = csub(s, q2);
-                x[j] = s;
-                x[j + h] = mul_shoup_lazy(a - b + q2, w.w, w.ws, q);
+                const TwPair t = w[(1 << k) - 1 + (j >> (K - k))];
+                const uint64_t a = y[j], b = y[j + h];
+                const uint64_t s = a + b;
+                y[j] = first_stage ? mul_shoup_lazy(s, ninv, ninv_s, q) : csub(s, q2);
+                y[j + h] = mul_shoup_lazy(a - b + q2, t.w, t.ws, q);
             }
         }
+    }
+}
+
+template <int LM, int K, int SA>
+__device__ __forceinline__ void grp_store(const uint64_t (&x)[16], uint64_t *vec, int u) {
+    constexpr int G = 16 >> K, GS = 1 << K;
 #pragma unroll
-        for (int j = 0; j < GS; j++) vec[pad_idx((hi * GS + j) * tmin + lo)] = x[j];
-    }
+    for (int gg = 0; gg < G; gg++)
+#pragma unroll
+        for (int j = 0; j < GS; j++) vec[pad_idx(grp_elem<LM, K, SA>(u, gg, j))] = x[gg * GS + j];
 }
 
-template <int LM, int PH>
-__device__ __forceinline__ void fwd_phases(uint64_t *vec, int u, const TwPair *tw, int loff, uint32_t row,
-                                           uint64_t q) {
-    if constexpr (PH < ntt_num_phases(LM)) {
-        fwd_phase<LM, ntt_phase_len(LM, PH), ntt_phase_start(LM, PH)>(vec, u, tw, loff, row, q);
-        __syncthreads();
-        fwd_phases<LM, PH + 1>(vec, u, tw, loff, row, q);
-    }
+template <int LM, int K, int SA>
+__device__ __forceinline__ void grp_load(uint64_t (&x)[16], const uint64_t *vec, int u) {
+    constexpr int G = 16 >> K, GS = 1 << K;
+#pragma unroll
+    for (int gg = 0; gg < G; gg++)
+#pragma unroll
+        for (int j = 0; j < GS; j++) x[gg * GS + j] = vec[pad_idx(grp_elem<LM, K, SA>(u, gg, j))];
 }
 
-template <int LM, int PH>
-__device__ __forceinline__ void inv_phases(uint64_t *vec, int u, const TwPair *itw, int loff, uint32_t row,
-                                           uint64_t q, uint64_t ninv, uint64_t ninv_s) {
-    if constexpr (PH >= 0) {
-        inv_phase<LM, ntt_phase_len(LM, PH), ntt_phase_start(LM, PH)>(vec, u, itw, loff, row, q, ninv, ninv_s);
+// Phase order: forward runs phases 0..NPH-1, inverse NPH-1..0.
+template <int LM, bool FWD, int PI>
+struct PhaseAt {
+    static constexpr int NPH = ntt_num_phases(LM);
+    static constexpr int PH = FWD ? PI : NPH - 1 - PI;
+    static constexpr int K = ntt_phase_len(LM, PH);
+    static constexpr int SA = ntt_phase_start(LM, PH);
+};
+
+// Runs processing steps PI..NPH-1 on the registers; between steps the vector goes through
+// shared memory (group_store, barrier, group_load of the next step's groups).
+template <int LM, bool FWD, int PI>
+__device__ __forceinline__ void run_phases(uint64_t (&x)[16], uint64_t *vec, int u, const TwPair *tw, int loff,
+                                           uint32_t row, uint64_t q, uint64_t ninv, uint64_t ninv_s) {
+    using P = PhaseAt<LM, FWD, PI>;
+    if constexpr (FWD)
+        fwd_regs<LM, P::K, P::SA>(x, u, tw, loff, row, q);
+    else
+        inv_regs<LM, P::K, P::SA>(x, u, tw, loff, row, q, ninv, ninv_s);
+    if constexpr (PI + 1 < P::NPH) {
+        using Q = PhaseAt<LM, FWD, PI + 1>;
+        grp_store<LM, P::K, P::SA>(x, vec, u);
         __syncthreads();
-        inv_phases<LM, PH - 1>(vec, u, itw, loff, row, q, ninv, ninv_s);
+        grp_load<LM, Q::K, Q::SA>(x, vec, u);
+        run_phases<LM, FWD, PI + 1>(x, vec, u, tw, loff, row, q, ninv, ninv_s);
     }
 }
 
@@ -165,79 +187,104 @@ struct NttTables {
 // the last of its transform stores lazy values ([0, 4q) forward, [0, 2q) inverse); the last
 // pass hands canonical values to its Store functor.
 
-// Column pass: vectors are V consecutive columns, each of M = N1 elements (stride N2).
+// Column pass: vectors are V consecutive columns, each of M = N1 elements (stride N2).  Thread
+// t works on column t % V, so every global access of a warp covers whole 128-byte row
+// segments; the first and last register phases load and store global memory directly.
 template <int LM, bool FWD, bool LAST, class Map, class Load, class Store>
-__global__ void __launch_bounds__(kNttThreads) ntt_col_pass(NttTables T, Map map, Load ld, Store st) {
+__global__ void __launch_bounds__(kNttThreads, 3) ntt_col_pass(NttTables T, Map map, Load ld, Store st) {
     constexpr int M = 1 << LM;
-    constexpr int TPV = M / 16;
     constexpr int V = kTileElems / M;
     constexpr int VP = M + M / 16 + 1;  // padded vector length (odd: column sweeps hit distinct banks)
+    using F = PhaseAt<LM, FWD, 0>;
+    using L = PhaseAt<LM, FWD, F::NPH - 1>;
     __shared__ uint64_t sm[V * VP];
     int poly, k, tbl;
     if (!map((int)blockIdx.y, poly, k, tbl)) return;  // uniform per block, before any barrier
     const uint64_t q = T.mods[tbl].q;
     const int n2 = 1 << T.l2;
-    const int c0 = blockIdx.x * V;
-    // coalesced tile load: thread handles column c0 + (i % V), row i / V
-    for (int i = threadIdx.x; i < V * M; i += kNttThreads) {
-        const int v = i % V, r = i / V;
-        sm[v * VP + pad_idx(r)] = ld(poly, k, tbl, (uint32_t)(r * n2 + c0 + v));
+    const int v = threadIdx.x % V, u = threadIdx.x / V;
+    const uint32_t col = blockIdx.x * V + v;
+    uint64_t x[16];
+#pragma unroll
+    for (int gg = 0; gg < (16 >> F::K); gg++)
+#pragma unroll
+        for (int j = 0; j < (1 << F::K); j++)
+            x[gg * (1 << F::K) + j] = ld(poly, k, tbl, (uint32_t)grp_elem<LM, F::K, F::SA>(u, gg, j) * n2 + col);
+    uint64_t ni = 0, nis = 0;
+    if constexpr (!FWD) {
+        ni = T.ninv[2 * tbl];
+        nis = T.ninv[2 * tbl + 1];
     }
-    __syncthreads();
-    const int vv = threadIdx.x / TPV, u = threadIdx.x % TPV;
-    uint64_t *vec = sm + vv * VP;
-    if constexpr (FWD) {
-        fwd_phases<LM, 0>(vec, u, T.tw + (size_t)tbl * (1 << T.log_n), 0, 0u, q);
-    } else {
-        const uint64_t ni = T.ninv[2 * tbl], nis = T.ninv[2 * tbl + 1];
-        inv_phases<LM, ntt_num_phases(LM) - 1>(vec, u, T.itw + (size_t)tbl * (1 << T.log_n), 0, 0u, q, ni, nis);
-    }
-    for (int i = threadIdx.x; i < V * M; i += kNttThreads) {
-        const int v = i % V, r = i / V;
-        uint64_t x = sm[v * VP + pad_idx(r)];
-        if (LAST) {
-            if (FWD) x = csub(x, 2 * q);
-            x = csub(x, q);
+    run_phases<LM, FWD, 0>(x, sm + v * VP, u, (FWD ? T.tw : T.itw) + ((size_t)tbl << T.log_n), 0, 0u, q, ni, nis);
+#pragma unroll
+    for (int gg = 0; gg < (16 >> L::K); gg++)
+#pragma unroll
+        for (int j = 0; j < (1 << L::K); j++) {
+            uint64_t y = x[gg * (1 << L::K) + j];
+            if (LAST) {
+                if (FWD) y = csub(y, 2 * q);
+                y = csub(y, q);
+            }
+            st(poly, k, tbl, (uint32_t)grp_elem<LM, L::K, L::SA>(u, gg, j) * n2 + col, y);
         }
-        st(poly, k, tbl, (uint32_t)(r * n2 + c0 + v), x);
-    }
 }
 
-// Row pass: vectors are V consecutive rows of M = N2 contiguous elements.
+// Row pass: vectors are V consecutive rows of M = N2 contiguous elements.  The forward pass
+// loads its first phase directly (lane-contiguous) and stores through a coalesced sweep;
+// the inverse pass loads through the sweep and stores its last phase directly.
 template <int LM, bool FWD, bool LAST, class Map, class Load, class Store>
-__global__ void __launch_bounds__(kNttThreads) ntt_row_pass(NttTables T, Map map, Load ld, Store st) {
+__global__ void __launch_bounds__(kNttThreads, 3) ntt_row_pass(NttTables T, Map map, Load ld, Store st) {
     constexpr int M = 1 << LM;
     constexpr int TPV = M / 16;
     constexpr int V = kTileElems / M;
     constexpr int VP = M + M / 16 + 1;
+    using F = PhaseAt<LM, FWD, 0>;
+    using L = PhaseAt<LM, FWD, F::NPH - 1>;
     __shared__ uint64_t sm[V * VP];
     int poly, k, tbl;
     if (!map((int)blockIdx.y, poly, k, tbl)) return;  // uniform per block, before any barrier
     const uint64_t q = T.mods[tbl].q;
     const uint32_t base = blockIdx.x * kTileElems;
-    for (int i = threadIdx.x; i < V * M; i += kNttThreads) {
-        const int v = i / M, e = i % M;
-        sm[v * VP + pad_idx(e)] = ld(poly, k, tbl, base + i);
-    }
-    __syncthreads();
     const int vv = threadIdx.x / TPV, u = threadIdx.x % TPV;
     const uint32_t row = blockIdx.x * V + vv;
     uint64_t *vec = sm + vv * VP;
+    uint64_t x[16];
     if constexpr (FWD) {
-        fwd_phases<LM, 0>(vec, u, T.tw + (size_t)tbl * (1 << T.log_n), T.l1, row, q);
+#pragma unroll
+        for (int gg = 0; gg < (16 >> F::K); gg++)
+#pragma unroll
+            for (int j = 0; j < (1 << F::K); j++)
+                x[gg * (1 << F::K) + j] = ld(poly, k, tbl, base + vv * M + grp_elem<LM, F::K, F::SA>(u, gg, j));
     } else {
-        const uint64_t ni = T.ninv[2 * tbl], nis = T.ninv[2 * tbl + 1];
-        inv_phases<LM, ntt_num_phases(LM) - 1>(vec, u, T.itw + (size_t)tbl * (1 << T.log_n), T.l1, row, q, ni,
-                                               nis);
+#pragma unroll 4
+        for (int i = threadIdx.x; i < V * M; i += kNttThreads) sm[(i / M) * VP + pad_idx(i % M)] = ld(poly, k, tbl, base + i);
+        __syncthreads();
+        grp_load<LM, F::K, F::SA>(x, vec, u);
     }
-    for (int i = threadIdx.x; i < V * M; i += kNttThreads) {
-        const int v = i / M, e = i % M;
-        uint64_t x = sm[v * VP + pad_idx(e)];
-        if (LAST) {
-            if (FWD) x = csub(x, 2 * q);
-            x = csub(x, q);
+    uint64_t ni = 0, nis = 0;
+    if constexpr (!FWD) {
+        ni = T.ninv[2 * tbl];
+        nis = T.ninv[2 * tbl + 1];
+    }
+    run_phases<LM, FWD, 0>(x, vec, u, (FWD ? T.tw : T.itw) + ((size_t)tbl << T.log_n), T.l1, row, q, ni, nis);
+    if constexpr (FWD) {
+        grp_store<LM, L::K, L::SA>(x, vec, u);
+        __syncthreads();
+#pragma unroll 4
+        for (int i = threadIdx.x; i < V * M; i += kNttThreads) {
+            uint64_t y = sm[(i / M) * VP + pad_idx(i % M)];
+            if (LAST) y = csub(csub(y, 2 * q), q);
+            st(poly, k, tbl, base + i, y);
         }
-        st(poly, k, tbl, base + i, x);
+    } else {
+#pragma unroll
+        for (int gg = 0; gg < (16 >> L::K); gg++)
+#pragma unroll
+            for (int j = 0; j < (1 << L::K); j++) {
+                uint64_t y = x[gg * (1 << L::K) + j];
+                if (LAST) y = csub(y, q);
+                st(poly, k, tbl, base + vv * M + grp_elem<LM, L::K, L::SA>(u, gg, j), y);
+            }
     }
 }
 

@@ -12,6 +12,7 @@
 //      (...(alpha mod r_0)... ) mod r_j; this is reproduced;
 //   4. relinearisation of c2 in the coefficient domain (DRNSTool::modup / moddown_from_NTT BFV
 //      branches, src/rns_bconv.cu:530-628, 776-828).
+#include "bconv.cuh"
 #include "keyswitch.cuh"
 #include "launch.cuh"
 #include "ops.hpp"
@@ -210,10 +211,14 @@ static void bfv_keyswitch_to(const Context &c, uint64_t *scratch, uint64_t *out,
     uint64_t *tm = scratch;
     uint64_t *cx = tm + ((size_t)beta * qlp << c.log_n);
     const long long tps = (long long)qlp << c.log_n;
+    with_digit_bound(alpha, [&]<int A>() {
+        count_launch();
+        modup_bconv<A, true><<<dim3((unsigned)std::max<uint64_t>(1, c.n / 512), beta), 256, 0, s>>>(
+                tm, c2, lt.part_hat_inv.as<uint64_t>(), lt.modup_mat.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, l,
+                c.nQ, alpha);
+    });
     PtrStore ts{tm, tps, c.log_n};
-    BfvBconvLoad bl{c2, lt.part_hat_inv.as<uint64_t>(), lt.modup_mat.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n,
-                    l, alpha, qlp};
-    ntt_fwd(c, beta * qlp, ModupMap{qlp, l, c.nQ, alpha, false}, bl, ts, ts, s);
+    ntt_fwd(c, beta * qlp, ModupMap{qlp, l, c.nQ, alpha, false}, PtrLoad{tm, tps, c.log_n}, ts, ts, s);
     const size_t work = ((size_t)qlp << c.log_n) / 2;
     count_launch();
     ks_inner_product<NoOwn, true><<<grid_for_bfv(work, 256), 256, 0, s>>>(cx, tm, NoOwn{}, evk, c.d_mods.as<Mod>(),

@@ -23,6 +23,7 @@
 // folds the rescale's NTT into step 5 by linearity (see ckks_mul_relin_rescale).
 #include <stdexcept>
 
+#include "bconv.cuh"
 #include "keyswitch.cuh"
 #include "launch.cuh"
 #include "ops.hpp"
@@ -34,8 +35,8 @@ size_t workspace_words(const Context &c) {
     size_t w = 0;
     if (a) {
         const size_t beta = c.beta((int)nQ), qlp = nQ + a;
-        // y | tm | cx | g0,g1 (or acc0) | z
-        w = n * (nQ + beta * qlp + 2 * qlp + 2 * nQ + 2);
+        // y | tm | cx | g0,g1 (or acc0) | z (4 limbs)
+        w = n * (nQ + beta * qlp + 2 * qlp + 2 * nQ + 4);
     }
     if (c.scheme == kSchemeBFV) {
         const size_t qr = nQ + c.nR;
@@ -181,6 +182,8 @@ static KsBuffers ks_buffers(const Context &c, const Workspace &w) {
 }
 
 // Steps 1-2: y = iNTT(c2) * partQlHatInv; tm = NTT(bconv(y)) for every digit.
+static unsigned bconv_blocks(const Context &c) { return (unsigned)std::max<uint64_t>(1, c.n / 2 / 256); }
+
 template <class C2Load>
 static void modup_ckks(const Context &c, const KsBuffers &b, C2Load c2ld, int l, cudaStream_t s) {
     const LevelTables &lt = *c.levels[l];
@@ -190,10 +193,14 @@ static void modup_ckks(const Context &c, const KsBuffers &b, C2Load c2ld, int l,
     ntt_inv(c, l, SeqMap{l, 0}, c2ld, ys,
             ScaleStore{b.y, yps, c.log_n, 0, lt.part_hat_inv.as<uint64_t>(), c.d_mods.as<Mod>()}, s);
     const long long tps = (long long)qlp << c.log_n;
+    dim3 g(bconv_blocks(c), beta);
+    with_digit_bound(alpha, [&]<int A>() {
+        count_launch();
+        modup_bconv<A, false><<<g, 256, 0, s>>>(b.tm, b.y, nullptr, lt.modup_mat.as<uint64_t>(), c.d_mods.as<Mod>(),
+                                                 c.log_n, l, c.nQ, alpha);
+    });
     PtrStore ts{b.tm, tps, c.log_n};
-    ModupMap mm{qlp, l, c.nQ, alpha, true};
-    BconvLoad bl{b.y, lt.modup_mat.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, l, alpha, qlp};
-    ntt_fwd(c, beta * qlp, mm, bl, ts, ts, s);
+    ntt_fwd(c, beta * qlp, ModupMap{qlp, l, c.nQ, alpha, true}, PtrLoad{b.tm, tps, c.log_n}, ts, ts, s);
 }
 
 // Step 3
@@ -224,10 +231,15 @@ static void moddown_ntt(const Context &c, const KsBuffers &b, uint64_t *mid, int
                         uint64_t *out1, Base base, cudaStream_t s) {
     const int qlp = l + c.nP;
     const long long cps = (long long)qlp << c.log_n;
-    PtrStore ms{mid, (long long)l << c.log_n, c.log_n};
-    PBconvLoad pl{b.cx, cps, c.p_mat.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, l, c.nP};
+    const long long mps = (long long)l << c.log_n;
+    with_digit_bound(c.nP, [&]<int A>() {
+        count_launch();
+        moddown_bconv<A><<<dim3(bconv_blocks(c), 2), 256, 0, s>>>(mid, mps, b.cx, cps, c.p_mat.as<uint64_t>(),
+                                                                   c.d_mods.as<Mod>(), c.log_n, l, c.nP);
+    });
+    PtrStore ms{mid, mps, c.log_n};
     ModdownStore<Base> st{out0, out1, k0, b.cx, cps, c.p_inv.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, base};
-    ntt_fwd(c, 2 * nl, QlpMap{nl, k0, l, c.nQ}, pl, ms, st, s);
+    ntt_fwd(c, 2 * nl, QlpMap{nl, k0, l, c.nQ}, PtrLoad{mid, mps, c.log_n}, ms, st, s);
 }
 
 void ckks_keyswitch(const Context &c, const Workspace &w, uint64_t *ct, const uint64_t *c2, int l,
@@ -302,27 +314,76 @@ void ckks_rescale(const Context &c, const Workspace &w, const uint64_t *in, uint
             RescaleStore{in, out, ips, ops, lt.inv_qlast.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n}, s);
 }
 
-// HMult + relinearise + rescale.  With out_j = d_j + (cx_j - NTT(delta_j)) P^-1 and
-// z = iNTT(out_{l-1}), the rescale is (out_j - NTT(z mod q_j)) q_last^-1, and by linearity
-// of the NTT   res_j = (d_j + cx_j P^-1 - NTT(delta_j P^-1 + z mod q_j)) q_last^-1,
-// so after the last limb is finished (2 limbs) one forward NTT over 2(l-1) limbs completes
-// the whole operation.  Every step is exact modular arithmetic, so the result equals the
-// reference's multiply_and_relin_inplace + rescale_to_next_inplace word for word.
+// HMult + relinearise + rescale.  With out_j = d_j + (cx_j - NTT(delta_j)) P^-1 the
+// relinearised product, the rescale is (out_j - NTT(z mod q_j)) q_last^-1 with
+// z = iNTT(out_{l-1}).  By linearity of the NTT:
+//   z     = iNTT(d_{l-1}) + (iNTT(cx_{l-1}) - delta_{l-1}) P^-1        (mod q_{l-1})
+//   res_j = (d_j + cx_j P^-1 - NTT(delta_j P^-1 + z mod q_j)) q_last^-1  (mod q_j).
+// So the inverse NTT of the P limbs also transforms cx's limb l-1 and the tensor product's
+// limb l-1 (2 more limbs per polynomial), and one forward NTT over 2(l-1) limbs — whose load
+// computes delta_j, delta_{l-1}, z and the sum, and whose store adds d_j + cx_j P^-1 and
+// scales — finishes the whole operation.  Every step is exact modular arithmetic, so the result
+// equals the reference's multiply_and_relin_inplace + rescale_to_next_inplace word for word.
+struct LastLimbMap {  // per polynomial: alpha P limbs of cx, cx limb l-1, tensor limb l-1
+    int alpha, l, nQ;
+    __device__ __forceinline__ bool operator()(int b, int &t, int &k, int &tbl) const {
+        t = b / (alpha + 2);
+        k = b % (alpha + 2);
+        tbl = k < alpha ? nQ + k : l - 1;
+        return true;
+    }
+};
+
+struct LastLimbLoad {
+    const uint64_t *cx;
+    long long cps;
+    TensorBase tb;
+    const Mod *mods;
+    int log_n, l, alpha;
+    __device__ __forceinline__ uint64_t operator()(int t, int k, int tbl, uint32_t idx) const {
+        if (k < alpha) return cx[t * cps + ((size_t)(l + k) << log_n) + idx];
+        if (k == alpha) return cx[t * cps + ((size_t)(l - 1) << log_n) + idx];
+        return tb(t, l - 1, mods[tbl], idx);
+    }
+};
+
+struct LastLimbStore {
+    uint64_t *cx;
+    long long cps;
+    uint64_t *zc, *zd;
+    const uint64_t *phi;
+    const Mod *mods;
+    int log_n, l, alpha;
+    __device__ __forceinline__ void operator()(int t, int k, int tbl, uint32_t idx, uint64_t v) const {
+        if (k < alpha)
+            cx[t * cps + ((size_t)(l + k) << log_n) + idx] = mul_shoup(v, phi[2 * k], phi[2 * k + 1], mods[tbl].q);
+        else
+            (k == alpha ? zc : zd)[((size_t)t << log_n) + idx] = v;
+    }
+};
+
 struct RescaleFusedLoad {
     const uint64_t *cx;
     long long cps;
-    const uint64_t *pmat, *pinv, *z;
+    const uint64_t *pmat, *pinv, *zc, *zd;
     const Mod *mods;
     int log_n, l, nP;
     __device__ __forceinline__ uint64_t operator()(int t, int j, int tbl, uint32_t idx) const {
-        const Mod m = mods[tbl];
+        const Mod m = mods[tbl], ml = mods[l - 1];
         const uint64_t *yp = cx + t * cps + ((size_t)l << log_n) + idx;
-        const uint64_t *pm = pmat + (size_t)j * nP;
-        u128 acc{0, 0};
-        for (int k = 0; k < nP; k++) mac(acc, yp[(size_t)k << log_n], __ldg(pm + k));
-        const uint64_t delta = reduce128(acc, m);
-        const uint64_t dp = mul_shoup(delta, pinv[2 * j], pinv[2 * j + 1], m.q);
-        return add_mod(dp, reduce64(z[((size_t)t << log_n) + idx], m), m.q);
+        const uint64_t *pj = pmat + (size_t)j * nP, *pl = pmat + (size_t)(l - 1) * nP;
+        u128 aj{0, 0}, al{0, 0};
+        for (int k = 0; k < nP; k++) {
+            const uint64_t y = yp[(size_t)k << log_n];
+            mac(aj, y, __ldg(pj + k));
+            mac(al, y, __ldg(pl + k));
+        }
+        const size_t o = ((size_t)t << log_n) + idx;
+        const uint64_t dl = reduce128(al, ml);
+        const uint64_t pl_inv = pinv[2 * (l - 1)], pl_inv_s = pinv[2 * (l - 1) + 1];
+        const uint64_t z = add_mod(zd[o], mul_shoup(sub_mod(zc[o], dl, ml.q), pl_inv, pl_inv_s, ml.q), ml.q);
+        const uint64_t dp = mul_shoup(reduce128(aj, m), pinv[2 * j], pinv[2 * j + 1], m.q);
+        return add_mod(dp, reduce64(z, m), m.q);
     }
 };
 
@@ -348,24 +409,29 @@ void ckks_mul_relin_rescale(const Context &c, const Workspace &w, const uint64_t
                             uint64_t *out, int l, const uint64_t *const *rlk, cudaStream_t s) {
     const KsBuffers b = ks_buffers(c, w);
     const LevelTables &lt = *c.levels[l];
-    const long long lps = (long long)l << c.log_n, zps = 1LL << c.log_n;
+    const Mod *mods = c.d_mods.as<Mod>();
+    const long long lps = (long long)l << c.log_n;
     const uint64_t *a1 = ct1 + lps, *b1 = ct2 + lps;
-    modup_ckks(c, b, TensorD2Load{a1, b1, c.d_mods.as<Mod>(), c.log_n}, l, s);
+    const TensorBase tb{ct1, ct2, lps, c.log_n};
+    modup_ckks(c, b, TensorD2Load{a1, b1, mods, c.log_n}, l, s);
     inner_product(c, b, TensorOwn{a1, b1, c.log_n}, l, rlk, s);
-    moddown_intt_p(c, b, l, s);
-    // last limb of the relinearised product, both polynomials -> z (then coefficient form)
-    uint64_t *z = b.z;
-    moddown_ntt(c, b, b.tm, l, l - 1, 1, z, z + zps, TensorBase{ct1, ct2, lps, c.log_n}, s);
-    PtrStore zs{z, zps, c.log_n};
-    ntt_inv(c, 2, ConstTblMap{l - 1}, PtrLoad{z, zps, c.log_n}, zs, zs, s);
-    // everything else in one forward NTT over 2(l-1) limbs
-    const int qlp = l + c.nP;
+    const int alpha = c.nP, qlp = l + alpha;
     const long long cps = (long long)qlp << c.log_n, ops = (long long)(l - 1) << c.log_n;
+    uint64_t *zc = b.z, *zd = b.z + (2 << c.log_n);
+    PtrStore mid{b.tm, (long long)(alpha + 2) << c.log_n, c.log_n};
+    ntt_inv(c, 2 * (alpha + 2), LastLimbMap{alpha, l, c.nQ}, LastLimbLoad{b.cx, cps, tb, mods, c.log_n, l, alpha},
+            mid, LastLimbStore{b.cx, cps, zc, zd, c.p_hat_inv.as<uint64_t>(), mods, c.log_n, l, alpha}, s);
+    with_digit_bound(alpha, [&]<int A>() {
+        count_launch();
+        rescale_fused_bconv<A><<<dim3(bconv_blocks(c), 2), 256, 0, s>>>(b.tm, ops, b.cx, cps, zc, zd,
+                                                                         c.p_mat.as<uint64_t>(),
+                                                                         c.p_inv.as<uint64_t>(), mods, c.log_n, l,
+                                                                         c.nP);
+    });
     PtrStore ms{b.tm, ops, c.log_n};
-    RescaleFusedLoad ld{b.cx, cps, c.p_mat.as<uint64_t>(), c.p_inv.as<uint64_t>(), z, c.d_mods.as<Mod>(),
-                        c.log_n, l, c.nP};
-    RescaleFusedStore st{out, ops, b.cx, cps, c.p_inv.as<uint64_t>(), lt.inv_qlast.as<uint64_t>(),
-                         c.d_mods.as<Mod>(), c.log_n, TensorBase{ct1, ct2, lps, c.log_n}};
+    PtrLoad ld{b.tm, ops, c.log_n};
+    RescaleFusedStore st{out, ops, b.cx, cps, c.p_inv.as<uint64_t>(), lt.inv_qlast.as<uint64_t>(), mods, c.log_n,
+                         tb};
     ntt_fwd(c, 2 * (l - 1), QlpMap{l - 1, 0, l, c.nQ}, ld, ms, st, s);
 }
 
