@@ -9,71 +9,17 @@
 
 #include "context.cuh"
 #include "host_tables.hpp"
+#include "capi_internal.hpp"
 #include "ops.hpp"
 #include "phantom_gb300.h"
-
-struct fhe_context {
-    std::unique_ptr<pfg::Context> c;
-};
-
-struct fhe_workspace {
-    const fhe_context *ctx = nullptr;
-    uint64_t *base = nullptr;
-    size_t words = 0;
-};
 
 namespace {
 
 thread_local std::string g_last_error;
 
-struct Status {
-    int code;
-    std::string msg;
-};
-
-int fail(int code, const std::string &msg) {
-    g_last_error = msg;
-    return code;
-}
-
-// Runs `body`, translating the reference's exception classes into status codes; with
-// `launches` it also checks that every kernel launch the body made was accepted.
-template <class F>
-int guarded(F &&body, bool launches = true) {
-    try {
-        body();
-        if (launches) {
-            cudaError_t e = cudaGetLastError();
-            if (e != cudaSuccess) return fail(FHE_ERR_CUDA, std::string("CUDA error: ") + cudaGetErrorString(e));
-        }
-        return FHE_OK;
-    } catch (const std::invalid_argument &e) {
-        return fail(FHE_ERR_INVALID_ARGUMENT, e.what());
-    } catch (const std::logic_error &e) {
-        return fail(FHE_ERR_LOGIC, e.what());
-    } catch (const std::bad_alloc &) {
-        return fail(FHE_ERR_OUT_OF_MEMORY, "out of host memory");
-    } catch (const std::runtime_error &e) {
-        return fail(FHE_ERR_CUDA, e.what());
-    } catch (...) {
-        return fail(FHE_ERR_LOGIC, "unknown error");
-    }
-}
-
 struct unsupported : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
-
-const pfg::Context &ctx_of(const fhe_context *ctx) {
-    if (!ctx || !ctx->c) throw std::invalid_argument("context is null");
-    return *ctx->c;
-}
-
-// chain index -> number of data limbs (src/context.cu:141-158)
-int level_of(const pfg::Context &c, size_t chain_index) {
-    if (chain_index < 1 || chain_index > (size_t)c.nQ) throw std::invalid_argument("chain_index out of range");
-    return c.nQ - (int)(chain_index - 1);
-}
 
 pfg::Workspace ws_of(const fhe_context *ctx, fhe_workspace *ws) {
     if (!ws || !ws->base) throw std::invalid_argument("workspace is null");
@@ -92,6 +38,11 @@ void need_keyswitching(const pfg::Context &c) {
 cudaStream_t st(void *s) { return static_cast<cudaStream_t>(s); }
 
 }  // namespace
+
+int pfg_fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
 
 namespace pfg {
 static std::atomic<unsigned long long> g_launches{0};
