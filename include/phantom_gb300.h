@@ -128,6 +128,17 @@ int fhe_multiply_and_relin(const fhe_context *ctx, fhe_workspace *ws, uint64_t *
 int fhe_rescale_to_next(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *in, uint64_t *out, size_t size,
                         size_t chain_index, void *stream);
 
+/* No counterpart in the reference: fhe_rescale_to_next for callers that may not allocate
+ * device memory (for example a plugin whose host process owns all device memory and passes
+ * in only the input and output buffers), so cannot hold an fhe_workspace.  Its scratch is a
+ * fixed 2 MiB array inside the library (kept by every GPU that loads it), which limits
+ * size * N to 2^18 words; larger requests fail with FHE_ERR_INVALID_ARGUMENT.  It calls no
+ * allocator.  The first call on a device looks up the array's device address, so make it
+ * before any stream capture.  All calls on a device share the array: calls that overlap on
+ * the GPU race and must be serialised by the caller. */
+int fhe_rescale_to_next_noalloc(const fhe_context *ctx, const uint64_t *in, uint64_t *out, size_t size,
+                                size_t chain_index, void *stream);
+
 /* mod_switch_to_next for BFV (src/rns.cu:1082-1126): coefficient-domain divide by q_last. */
 int fhe_bfv_mod_switch_to_next(const fhe_context *ctx, const uint64_t *in, uint64_t *out, size_t size,
                                size_t chain_index, void *stream);

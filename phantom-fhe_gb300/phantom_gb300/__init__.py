@@ -63,6 +63,7 @@ def _load():
     L.fhe_relinearize.argtypes = [_vp, _vp, _vp, _sz, _vp, _vp]
     L.fhe_multiply_and_relin.argtypes = [_vp, _vp, _vp, _vp, _sz, _vp, _vp]
     L.fhe_rescale_to_next.argtypes = [_vp, _vp, _vp, _vp, _sz, _sz, _vp]
+    L.fhe_rescale_to_next_noalloc.argtypes = [_vp, _vp, _vp, _sz, _sz, _vp]
     L.fhe_bfv_mod_switch_to_next.argtypes = [_vp, _vp, _vp, _sz, _sz, _vp]
     L.fhe_ckks_multiply_relin_rescale.argtypes = [_vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]
     L.fhe_apply_galois.argtypes = [_vp, _vp, _vp, _sz, ctypes.c_uint32, _vp, _vp]
@@ -189,6 +190,10 @@ class Context:
 
     def rescale_to_next(self, ws, src, dst, size, chain_index, stream=None):
         _check(lib.fhe_rescale_to_next(self._h, ws._h, _ptr(src), _ptr(dst), size, chain_index, _stream(stream)))
+
+    def rescale_to_next_noalloc(self, src, dst, size, chain_index, stream=None):
+        """Rescale without a workspace: for callers that may not allocate device memory."""
+        _check(lib.fhe_rescale_to_next_noalloc(self._h, _ptr(src), _ptr(dst), size, chain_index, _stream(stream)))
 
     def bfv_mod_switch_to_next(self, src, dst, size, chain_index, stream=None):
         _check(lib.fhe_bfv_mod_switch_to_next(self._h, _ptr(src), _ptr(dst), size, chain_index, _stream(stream)))
