@@ -40,8 +40,9 @@ extern "C" {
 #define FHE_ERR_UNSUPPORTED (-5)
 
 /* scheme_type and mul_tech_type values of include/host/encryptionparams.h */
-#define FHE_SCHEME_BFV 1
-#define FHE_SCHEME_CKKS 2
+#define FHE_SCHEME_BGV 1 /* not supported */
+#define FHE_SCHEME_BFV 2
+#define FHE_SCHEME_CKKS 3
 #define FHE_MUL_TECH_HPS 2
 
 typedef struct fhe_context fhe_context;

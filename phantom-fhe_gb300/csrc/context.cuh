@@ -19,7 +19,8 @@
 
 namespace pfg {
 
-enum Scheme { kSchemeNone = 0, kSchemeBFV = 1, kSchemeCKKS = 2, kSchemeBGV = 3 };
+// values of phantom::scheme_type (include/host/encryptionparams.h)
+enum Scheme { kSchemeNone = 0, kSchemeBGV = 1, kSchemeBFV = 2, kSchemeCKKS = 3 };
 enum MulTech { kMulNone = 0, kMulBEHZ = 1, kMulHPS = 2, kMulHPSOverQ = 3, kMulHPSOverQLeveled = 4 };
 
 // Device memory owned by the context (plain cudaMalloc, freed in the destructor).

@@ -14,7 +14,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(HERE, "_build", "libphantom_gb300.so")
 
-SCHEME_BFV, SCHEME_CKKS = 1, 2
+SCHEME_BFV, SCHEME_CKKS = 2, 3  # phantom::scheme_type values
 MUL_TECH_HPS = 2
 
 _vp = ctypes.c_void_p
