@@ -254,6 +254,23 @@ def run_ours(args):
     ntt_gbs = ntt_bytes / t_ntt / 1e9
     del big
 
+    # batch of 64 HMult+relin+rescale at levels drawn uniformly from 5..30 (one call), and the
+    # same 64 operations as a loop of single calls
+    brng = np.random.default_rng(2000 + rank)
+    levels = [int(x) for x in brng.integers(5, 31, size=64)]
+    items = []
+    for lv in levels:
+        ta = torch.randint(0, 1 << 40, (2, lv, N), dtype=torch.int64, device="cuda")
+        tb = torch.randint(0, 1 << 40, (2, lv, N), dtype=torch.int64, device="cuda")
+        items.append((ta, tb, torch.empty((2, lv - 1, N), dtype=torch.int64, device="cuda"), nq - lv + 1))
+    wsb = ctx.workspace(batch_items=64)
+    ctx.multiply_relin_rescale_batch(wsb, items, key, stream)
+    kb = 5
+    t_batch = timed(lambda i: ctx.multiply_relin_rescale_batch(wsb, items, key, stream), kb) / kb
+    t_loop = timed(lambda i: [ctx.multiply_relin_rescale(ws, x[0], x[1], x[2], x[3], key, stream) for x in items],
+                   kb) / kb
+    del items, wsb
+
     # end to end through the C ABI with host buffers: H2D of both inputs, D2H of the result
     pin_a = [torch.empty((2, l, N), dtype=torch.int64).pin_memory() for _ in range(PAIRS)]
     pin_b = [torch.empty((2, l, N), dtype=torch.int64).pin_memory() for _ in range(PAIRS)]
@@ -295,7 +312,9 @@ def run_ours(args):
                          "bound": "hbm", "achieved": ntt_gbs, "peak": peak, "unit": "GB/s",
                          "frac": ntt_gbs / peak, "peak_source": peak_kind,
                          "algorithmic_bytes": ntt_bytes, "traffic": traffic},
-            "extra": {"hrotate_step1_per_s": k2 * world / t_rot, "keyswitch_per_s": k2 * world / t_ks,
+            "extra": {"batch64_uneven_levels_ops_per_s": 64 * world / t_batch,
+                      "batch64_as_single_calls_ops_per_s": 64 * world / t_loop,
+                      "hrotate_step1_per_s": k2 * world / t_rot, "keyswitch_per_s": k2 * world / t_ks,
                       "ntt_forward_ms_64x35": 1000 * t_ntt,
                       "hmult_relin_rescale_algorithmic_bytes": 313524224,
                       "hmult_hbm_frac": 313524224 * value / world / 1e9 / peak,

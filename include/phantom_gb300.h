@@ -91,6 +91,9 @@ int fhe_context_galois_elts(const fhe_context *ctx, uint32_t *out, size_t *count
 size_t fhe_workspace_bytes(const fhe_context *ctx);
 int fhe_workspace_create(const fhe_context *ctx, fhe_workspace **out);
 void fhe_workspace_destroy(fhe_workspace *ws);
+/* Workspace for the batched calls: scratch for min(max_items, 64) ciphertexts at the key level
+ * (the reference has no batched calls; it loops over single calls). */
+int fhe_workspace_create_batch(const fhe_context *ctx, size_t max_items, fhe_workspace **out);
 
 /* nwt_2d_radix8_forward_inplace / nwt_2d_radix8_backward_inplace (include/ntt.cuh:157-226):
  * in-place transform of `num_polys` polynomials of `coeff_modulus_size` limbs each
@@ -150,6 +153,21 @@ int fhe_bfv_mod_switch_to_next(const fhe_context *ctx, const uint64_t *in, uint6
 int fhe_ckks_multiply_relin_rescale(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *ct1,
                                     const uint64_t *ct2, uint64_t *out, size_t chain_index,
                                     const uint64_t *const *rlk, void *stream);
+
+/* A batch of independent HMult + relinearise + rescale operations at their own chain indices
+ * (uneven levels allowed), sharing one relinearisation key.  The reference runs a batch as a host
+ * loop of multiply_and_relin_inplace + rescale_to_next_inplace (src/evaluate.cu:1061-1104,
+ * 1545-1565); here every pipeline step is one launch over up to 64 ciphertexts and the key is
+ * read from HBM once per launch set.  Each output equals the single call's, word for word.
+ * `items` is a host array; ws must come from fhe_workspace_create_batch. */
+typedef struct fhe_ckks_mul_item {
+    const uint64_t *ct1;  /* 2 polys at chain_index, NTT form */
+    const uint64_t *ct2;  /* 2 polys at chain_index */
+    uint64_t *out;        /* 2 polys at chain_index + 1 */
+    size_t chain_index;
+} fhe_ckks_mul_item;
+int fhe_ckks_multiply_relin_rescale_batch(const fhe_context *ctx, fhe_workspace *ws, const fhe_ckks_mul_item *items,
+                                          size_t count, const uint64_t *const *rlk, void *stream);
 
 /* apply_galois_inplace (include/evaluate.cuh:215, src/evaluate.cu:1567-1630), CKKS:
  * ct (2 polys) <- KeySwitch of the automorphism X -> X^galois_elt under gk. */

@@ -142,6 +142,26 @@ int fhe_workspace_create(const fhe_context *ctx, fhe_workspace **out) {
     });
 }
 
+int fhe_workspace_create_batch(const fhe_context *ctx, size_t max_items, fhe_workspace **out) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        need_ptr(out, "out");
+        if (max_items == 0) throw std::invalid_argument("max_items must be positive");
+        const size_t slots = std::min<size_t>(max_items, pfg::kBatchLaunch);
+        auto *w = new fhe_workspace;
+        w->ctx = ctx;
+        w->items = slots;
+        w->words = pfg::workspace_words(c) * slots;
+        cudaError_t e = cudaMalloc(&w->base, w->words * sizeof(uint64_t));
+        if (e != cudaSuccess) {
+            delete w;
+            cudaGetLastError();
+            throw std::bad_alloc();
+        }
+        *out = w;
+    });
+}
+
 void fhe_workspace_destroy(fhe_workspace *ws) {
     if (!ws) return;
     if (ws->base) cudaFree(ws->base);
@@ -276,6 +296,31 @@ int fhe_ckks_multiply_relin_rescale(const fhe_context *ctx, fhe_workspace *ws, c
         const int l = level_of(c, chain_index);
         if (l < 2) throw std::invalid_argument("end of modulus switching chain reached");
         pfg::ckks_mul_relin_rescale(c, w, ct1, ct2, out, l, rlk, st(stream));
+    });
+}
+
+int fhe_ckks_multiply_relin_rescale_batch(const fhe_context *ctx, fhe_workspace *ws, const fhe_ckks_mul_item *items,
+                                          size_t count, const uint64_t *const *rlk, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        pfg::Workspace w = ws_of(ctx, ws);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("batched HMult needs a CKKS context");
+        need_keyswitching(c);
+        need_ptr(items, "items");
+        need_ptr(rlk, "rlk");
+        if (count == 0) return;
+        if (ws->items < std::min<size_t>(count, pfg::kBatchLaunch))
+            throw std::invalid_argument("workspace has too few ciphertext slots for this batch");
+        std::vector<pfg::BatchItem> v;
+        for (size_t i = 0; i < count; i++) {
+            need_ptr(items[i].ct1, "items[i].ct1");
+            need_ptr(items[i].ct2, "items[i].ct2");
+            need_ptr(items[i].out, "items[i].out");
+            const int l = level_of(c, items[i].chain_index);
+            if (l < 2) throw std::invalid_argument("end of modulus switching chain reached");
+            v.push_back(pfg::BatchItem{items[i].ct1, items[i].ct2, items[i].out, l});
+        }
+        pfg::ckks_mul_relin_rescale_batch(c, w.base, ws->words / ws->items, v, rlk, st(stream));
     });
 }
 

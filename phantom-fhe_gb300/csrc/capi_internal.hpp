@@ -18,7 +18,8 @@ struct fhe_context {
 struct fhe_workspace {
     const fhe_context *ctx = nullptr;
     uint64_t *base = nullptr;
-    size_t words = 0;
+    size_t words = 0;      // total
+    size_t items = 1;      // ciphertext slots for the batched calls (words / items each)
 };
 
 // Records `msg` as the calling thread's last error (fhe_last_error) and returns `code`.

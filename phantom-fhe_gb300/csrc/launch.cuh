@@ -126,4 +126,17 @@ void ntt_inv(const Context &c, int blocks, Map m, Load ld, PtrStore mid, Store s
     col_pass<false, true>(c, blocks, m, PtrLoad{mid.base, mid.ps, mid.log_n}, st, s);
 }
 
+// Variants with separate intermediate store / load functors (batched, per-item buffers).
+template <class Map, class Load, class MidStore, class MidLoad, class Store>
+void ntt_fwd2(const Context &c, int blocks, Map m, Load ld, MidStore ms, MidLoad ml, Store st, cudaStream_t s) {
+    col_pass<true, false>(c, blocks, m, ld, ms, s);
+    row_pass<true, true>(c, blocks, m, ml, st, s);
+}
+
+template <class Map, class Load, class MidStore, class MidLoad, class Store>
+void ntt_inv2(const Context &c, int blocks, Map m, Load ld, MidStore ms, MidLoad ml, Store st, cudaStream_t s) {
+    row_pass<false, false>(c, blocks, m, ld, ms, s);
+    col_pass<false, true>(c, blocks, m, ml, st, s);
+}
+
 }  // namespace pfg

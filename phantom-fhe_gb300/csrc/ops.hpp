@@ -22,6 +22,13 @@ struct StepKey {  // one hoisted rotation: permutation table + key digits (devic
     const uint64_t *const *key;
 };
 
+struct BatchItem {  // one HMult+relin+rescale of a batch: inputs at level l, output at l - 1
+    const uint64_t *ct1, *ct2;
+    uint64_t *out;
+    int l;
+};
+constexpr int kBatchLaunch = 64;  // ciphertexts per launch set (larger batches run in chunks)
+
 void ntt_forward(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s);
 void ntt_inverse(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s);
 
@@ -33,6 +40,9 @@ void ckks_mul_relin(const Context &c, const Workspace &w, uint64_t *ct1, const u
                     const uint64_t *const *rlk, cudaStream_t s);
 void ckks_mul_relin_rescale(const Context &c, const Workspace &w, const uint64_t *ct1, const uint64_t *ct2,
                             uint64_t *out, int l, const uint64_t *const *rlk, cudaStream_t s);
+// Batched HMult + relin + rescale; item i uses scratch ws_base + (i % 64) * item_words.
+void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t item_words,
+                                  const std::vector<BatchItem> &items, const uint64_t *const *rlk, cudaStream_t s);
 void ckks_rescale(const Context &c, const Workspace &w, const uint64_t *in, uint64_t *out, int size, int l,
                   cudaStream_t s);
 void ckks_apply_galois(const Context &c, const Workspace &w, uint64_t *ct, int l, const uint32_t *perm,

@@ -1,0 +1,470 @@
+// ops_batch.cu — batched CKKS HMult + relinearise + rescale over ciphertexts at uneven levels.
+//
+// The reference processes a batch as a host loop of single calls
+// (multiply_and_relin_inplace + rescale_to_next_inplace, src/evaluate.cu:1061-1104, 1545-1565),
+// re-reading the whole relinearisation key for every ciphertext.  Here one launch per pipeline
+// step covers every ciphertext of the batch (up to kMaxBatch per launch set): each block looks up
+// its ciphertext from a per-launch prefix table passed by value, so ciphertexts at different
+// levels (different limb counts, digit counts and constant tables) share every launch, and the
+// inner product walks all ciphertexts for one key limb inside a block, so each key word comes
+// from HBM once per batch and from L1/L2 for the other ciphertexts.  The per-ciphertext
+// arithmetic is exactly that of ckks_mul_relin_rescale (ops_ckks.cu), so every output equals the
+// single call's word for word.
+#include "bconv.cuh"
+#include "launch.cuh"
+#include "ops.hpp"
+
+namespace pfg {
+
+constexpr int kMaxBatch = 64;
+constexpr int kSub = 64;  // "poly" argument of batched functors = item * kSub + sub-index
+
+struct BatchItems {
+    int count;
+    int l[kMaxBatch];
+    const uint64_t *a[kMaxBatch], *b[kMaxBatch];
+    uint64_t *out[kMaxBatch];
+    uint64_t *ws[kMaxBatch];
+    const uint64_t *phi[kMaxBatch], *mat[kMaxBatch], *iq[kMaxBatch];
+};
+
+struct Prefix {
+    int count;
+    int p[kMaxBatch + 1];
+    __device__ __forceinline__ int find(int b) const {
+        int c = 0;
+        while (c + 1 < count && p[c + 1] <= b) c++;
+        return c;
+    }
+};
+
+// Offsets of the per-item scratch regions (same layout as the single-call workspace).
+struct ScratchLayout {
+    long long y, tm, cx, g, z;
+};
+
+static ScratchLayout scratch_layout(const Context &c) {
+    const long long n = (long long)c.n, nQ = c.nQ, qlp = nQ + c.nP, beta = c.beta(c.nQ);
+    ScratchLayout s;
+    s.y = 0;
+    s.tm = s.y + nQ * n;
+    s.cx = s.tm + beta * qlp * n;
+    s.g = s.cx + 2 * qlp * n;
+    s.z = s.g + 2 * nQ * n;
+    return s;
+}
+
+// ------------------------------------------------------------------ maps
+
+struct BSeqMap {  // item c: limbs [0, l_c), table k  (mod-up inverse NTT)
+    Prefix pre;
+    __device__ __forceinline__ bool operator()(int b, int &poly, int &k, int &tbl) const {
+        const int c = pre.find(b);
+        k = b - pre.p[c];
+        poly = c * kSub;
+        tbl = k;
+        return true;
+    }
+};
+
+struct BModupMap {  // item c: beta_c digits x (l_c + alpha) limbs, own limbs idle
+    Prefix pre;
+    int l[kMaxBatch];
+    int nQ, alpha;
+    __device__ __forceinline__ bool operator()(int b, int &poly, int &jj, int &tbl) const {
+        const int c = pre.find(b), r = b - pre.p[c], lc = l[c], qlp = lc + alpha;
+        const int d = r / qlp;
+        jj = r % qlp;
+        poly = c * kSub + d;
+        tbl = jj < lc ? jj : nQ + (jj - lc);
+        return !(jj >= d * alpha && jj < d * alpha + alpha && jj < lc);
+    }
+};
+
+struct BLastLimbMap {  // item c, poly t: alpha P limbs, cx limb l-1, tensor limb l-1
+    Prefix pre;
+    int l[kMaxBatch];
+    int nQ, alpha;
+    __device__ __forceinline__ bool operator()(int b, int &poly, int &k, int &tbl) const {
+        const int c = pre.find(b), r = b - pre.p[c];
+        const int t = r / (alpha + 2);
+        k = r % (alpha + 2);
+        poly = c * kSub + t;
+        tbl = k < alpha ? nQ + k : l[c] - 1;
+        return true;
+    }
+};
+
+struct BFinalMap {  // item c, poly t: limbs [0, l_c - 1)
+    Prefix pre;
+    int l[kMaxBatch];
+    __device__ __forceinline__ bool operator()(int b, int &poly, int &j, int &tbl) const {
+        const int c = pre.find(b), r = b - pre.p[c], m = l[c] - 1;
+        const int t = r / m;
+        j = r % m;
+        poly = c * kSub + t;
+        tbl = j;
+        return true;
+    }
+};
+
+// ------------------------------------------------------------------ functors
+
+struct BItemsRef {
+    BatchItems it;
+    ScratchLayout sl;
+    int log_n, alpha;
+    __device__ __forceinline__ long long qlp_n(int c) const { return (long long)(it.l[c] + alpha) << log_n; }
+};
+
+// tensor-product term t of item c at limb j: t = 0: a0*b0, 1: a0*b1 + a1*b0, 2: a1*b1
+__device__ __forceinline__ uint64_t tensor_term(const BatchItems &it, int c, int t, int j, uint32_t idx, int log_n,
+                                                const Mod &m) {
+    const long long lps = (long long)it.l[c] << log_n;
+    const size_t o = ((size_t)j << log_n) + idx;
+    const uint64_t *a = it.a[c], *b = it.b[c];
+    if (t == 2) return mul_mod(a[lps + o], b[lps + o], m);
+    const uint64_t a0 = a[o], b0 = b[o];
+    if (t == 0) return mul_mod(a0, b0, m);
+    u128 acc = mul_wide(a0, b[lps + o]);
+    mac(acc, a[lps + o], b0);
+    return reduce128(acc, m);
+}
+
+struct BD2Load {  // mod-up inverse NTT input: d2 = a1 * b1
+    BItemsRef r;
+    const Mod *mods;
+    __device__ __forceinline__ uint64_t operator()(int poly, int k, int tbl, uint32_t idx) const {
+        return tensor_term(r.it, poly / kSub, 2, k, idx, r.log_n, mods[tbl]);
+    }
+};
+
+// generic scratch access: ws[c] + region + sub * sub_stride(c) + k * N + idx
+template <int REGION>
+struct BScratch {
+    BItemsRef r;
+    __device__ __forceinline__ uint64_t *addr(int poly, int k, uint32_t idx) const {
+        const int c = poly / kSub, sub = poly % kSub;
+        long long off;
+        long long ss;
+        if (REGION == 0) {  // y [l][N]
+            off = r.sl.y;
+            ss = 0;
+        } else if (REGION == 1) {  // tm [beta][qlp][N]
+            off = r.sl.tm;
+            ss = r.qlp_n(c);
+        } else if (REGION == 2) {  // tm reused as [2][alpha+2][N]
+            off = r.sl.tm;
+            ss = (long long)(r.alpha + 2) << r.log_n;
+        } else {  // tm reused as [2][l-1][N]
+            off = r.sl.tm;
+            ss = (long long)(r.it.l[c] - 1) << r.log_n;
+        }
+        return r.it.ws[c] + off + sub * ss + ((long long)k << r.log_n) + idx;
+    }
+    __device__ __forceinline__ uint64_t operator()(int poly, int k, int, uint32_t idx) const { return *addr(poly, k, idx); }
+    __device__ __forceinline__ void operator()(int poly, int k, int, uint32_t idx, uint64_t v) const {
+        *addr(poly, k, idx) = v;
+    }
+};
+
+struct BScaleYStore {  // y[k] = v * partQlHatInv_k
+    BItemsRef r;
+    const Mod *mods;
+    __device__ __forceinline__ void operator()(int poly, int k, int tbl, uint32_t idx, uint64_t v) const {
+        const int c = poly / kSub;
+        const uint64_t *phi = r.it.phi[c];
+        r.it.ws[c][r.sl.y + ((long long)k << r.log_n) + idx] = mul_shoup(v, phi[2 * k], phi[2 * k + 1], mods[tbl].q);
+    }
+};
+
+struct BLastLoad {
+    BItemsRef r;
+    const Mod *mods;
+    __device__ __forceinline__ uint64_t operator()(int poly, int k, int tbl, uint32_t idx) const {
+        const int c = poly / kSub, t = poly % kSub, lc = r.it.l[c];
+        const uint64_t *cx = r.it.ws[c] + r.sl.cx + t * r.qlp_n(c);
+        if (k < r.alpha) return cx[((size_t)(lc + k) << r.log_n) + idx];
+        if (k == r.alpha) return cx[((size_t)(lc - 1) << r.log_n) + idx];
+        return tensor_term(r.it, c, t, lc - 1, idx, r.log_n, mods[tbl]);
+    }
+};
+
+struct BLastStore {
+    BItemsRef r;
+    const uint64_t *phi;  // PHatInv pairs
+    const Mod *mods;
+    __device__ __forceinline__ void operator()(int poly, int k, int tbl, uint32_t idx, uint64_t v) const {
+        const int c = poly / kSub, t = poly % kSub, lc = r.it.l[c];
+        uint64_t *ws = r.it.ws[c];
+        if (k < r.alpha) {
+            ws[r.sl.cx + t * r.qlp_n(c) + ((long long)(lc + k) << r.log_n) + idx] =
+                    mul_shoup(v, phi[2 * k], phi[2 * k + 1], mods[tbl].q);
+        } else {
+            const long long zoff = r.sl.z + ((long long)((k == r.alpha ? 0 : 2) + t) << r.log_n);
+            ws[zoff + idx] = v;
+        }
+    }
+};
+
+struct BFinalStore {  // out = (d_j + cx_j P^-1 - v) q_last^-1
+    BItemsRef r;
+    const uint64_t *pinv;
+    const Mod *mods;
+    __device__ __forceinline__ void operator()(int poly, int j, int tbl, uint32_t idx, uint64_t v) const {
+        const int c = poly / kSub, t = poly % kSub, lc = r.it.l[c];
+        const Mod m = mods[tbl];
+        const size_t o = ((size_t)j << r.log_n) + idx;
+        const uint64_t cxv = r.it.ws[c][r.sl.cx + t * r.qlp_n(c) + o];
+        const uint64_t cp = mul_shoup(cxv, pinv[2 * j], pinv[2 * j + 1], m.q);
+        const uint64_t x = sub_mod(add_mod(tensor_term(r.it, c, t, j, idx, r.log_n, m), cp, m.q), v, m.q);
+        const uint64_t *iq = r.it.iq[c];
+        r.it.out[c][t * ((long long)(lc - 1) << r.log_n) + o] = mul_shoup(x, iq[2 * j], iq[2 * j + 1], m.q);
+    }
+};
+
+// ------------------------------------------------------------------ element-wise batch kernels
+
+// Mod-up base conversion for (item, digit) = block row.
+template <int A>
+__global__ void __launch_bounds__(256) modup_bconv_batch(BItemsRef r, Prefix pre, const Mod *mods, int nQ) {
+    const int c = pre.find(blockIdx.y), d = blockIdx.y - pre.p[c];
+    const int l = r.it.l[c], alpha = r.alpha, qlp = l + alpha, log_n = r.log_n;
+    const int s0 = d * alpha, sz = min(alpha, l - s0);
+    const uint64_t *y = r.it.ws[c] + r.sl.y;
+    uint64_t *tm = r.it.ws[c] + r.sl.tm + (((size_t)d * qlp) << log_n);
+    const uint64_t *mat = r.it.mat[c];
+    const size_t half = (size_t)1 << (log_n - 1);
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < half; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t idx = 2 * e;
+        uint64_t y0[A], y1[A];
+#pragma unroll
+        for (int i = 0; i < A; i++) {
+            if (i >= sz) break;
+            const ulonglong2 v = ld2(y + ((size_t)(s0 + i) << log_n) + idx);
+            y0[i] = v.x;
+            y1[i] = v.y;
+        }
+        for (int jj = 0; jj < qlp; jj++) {
+            if (jj >= s0 && jj < s0 + sz) continue;
+            const Mod m = mods[jj < l ? jj : nQ + (jj - l)];
+            const uint64_t *row = mat + ((size_t)d * qlp + jj) * alpha;
+            u128 a0{0, 0}, a1{0, 0};
+#pragma unroll
+            for (int i = 0; i < A; i++) {
+                if (i >= sz) break;
+                if (i == 8) {
+                    a0 = u128{reduce128(a0, m), 0};
+                    a1 = u128{reduce128(a1, m), 0};
+                }
+                const uint64_t w = __ldg(row + i);
+                mac(a0, y0[i], w);
+                mac(a1, y1[i], w);
+            }
+            st2(tm + ((size_t)jj << log_n) + idx, reduce128(a0, m), reduce128(a1, m));
+        }
+    }
+}
+
+// Inner product for key limb blockIdx.y over every item that has it; the key tile is read from
+// HBM for the first item and from cache for the others.
+__global__ void __launch_bounds__(256) ks_inner_product_batch(BItemsRef r, const uint64_t *const *evk,
+                                                              const Mod *mods, int nQ, int qp) {
+    const int tk = blockIdx.y, alpha = r.alpha, log_n = r.log_n;
+    const Mod m = mods[tk];
+    const size_t half = (size_t)1 << (log_n - 1);
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < half; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t idx = 2 * e;
+        for (int c = 0; c < r.it.count; c++) {
+            const int l = r.it.l[c];
+            if (tk >= l && tk < nQ) continue;  // this level has dropped q_tk
+            const int jj = tk < nQ ? tk : l + (tk - nQ), qlp = l + alpha, beta = (l + alpha - 1) / alpha;
+            const int own_d = jj < l ? jj / alpha : -1;
+            const uint64_t *tm = r.it.ws[c] + r.sl.tm;
+            u128 a0{0, 0}, a1{0, 0}, b0{0, 0}, b1{0, 0};
+            int terms = 0;
+            for (int d = 0; d < beta; d++) {
+                uint64_t x0, x1;
+                if (d == own_d) {
+                    x0 = tensor_term(r.it, c, 2, jj, (uint32_t)idx, log_n, m);
+                    x1 = tensor_term(r.it, c, 2, jj, (uint32_t)idx + 1, log_n, m);
+                } else {
+                    const ulonglong2 v = ld2(tm + (((size_t)d * qlp + jj) << log_n) + idx);
+                    x0 = v.x;
+                    x1 = v.y;
+                }
+                const uint64_t *key = evk[d];
+                const ulonglong2 k0 = ld2(key + ((size_t)tk << log_n) + idx);
+                const ulonglong2 k1 = ld2(key + ((size_t)(qp + tk) << log_n) + idx);
+                if (terms == 7) {
+                    a0 = u128{reduce128(a0, m), 0};
+                    a1 = u128{reduce128(a1, m), 0};
+                    b0 = u128{reduce128(b0, m), 0};
+                    b1 = u128{reduce128(b1, m), 0};
+                    terms = 1;
+                }
+                mac(a0, x0, k0.x);
+                mac(a1, x1, k0.y);
+                mac(b0, x0, k1.x);
+                mac(b1, x1, k1.y);
+                terms++;
+            }
+            uint64_t *cx = r.it.ws[c] + r.sl.cx + ((size_t)jj << log_n) + idx;
+            st2(cx, reduce128(a0, m), reduce128(a1, m));
+            st2(cx + ((size_t)qlp << log_n), reduce128(b0, m), reduce128(b1, m));
+        }
+    }
+}
+
+// Rescale-folded mod-down conversion for (item, poly) = block row (see rescale_fused_bconv).
+template <int A>
+__global__ void __launch_bounds__(256) rescale_bconv_batch(BItemsRef r, Prefix pre, const uint64_t *pmat,
+                                                           const uint64_t *pinv, const Mod *mods) {
+    const int c = pre.find(blockIdx.y), t = blockIdx.y - pre.p[c];
+    const int l = r.it.l[c], nP = r.alpha, log_n = r.log_n;
+    uint64_t *ws = r.it.ws[c];
+    const long long cps = r.qlp_n(c);
+    const uint64_t *yp = ws + r.sl.cx + t * cps + ((size_t)l << log_n);
+    const uint64_t *zc = ws + r.sl.z + ((size_t)t << log_n), *zd = ws + r.sl.z + ((size_t)(2 + t) << log_n);
+    uint64_t *w = ws + r.sl.tm + t * ((long long)(l - 1) << log_n);
+    const Mod ml = mods[l - 1];
+    const uint64_t pli = pinv[2 * (l - 1)], plis = pinv[2 * (l - 1) + 1];
+    const size_t half = (size_t)1 << (log_n - 1);
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < half; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t idx = 2 * e;
+        uint64_t y0[A], y1[A];
+#pragma unroll
+        for (int k = 0; k < A; k++) {
+            if (k >= nP) break;
+            const ulonglong2 v = ld2(yp + ((size_t)k << log_n) + idx);
+            y0[k] = v.x;
+            y1[k] = v.y;
+        }
+        const uint64_t *pl = pmat + (size_t)(l - 1) * nP;
+        u128 a0{0, 0}, a1{0, 0};
+#pragma unroll
+        for (int k = 0; k < A; k++) {
+            if (k >= nP) break;
+            if (k == 8) {
+                a0 = u128{reduce128(a0, ml), 0};
+                a1 = u128{reduce128(a1, ml), 0};
+            }
+            const uint64_t cc = __ldg(pl + k);
+            mac(a0, y0[k], cc);
+            mac(a1, y1[k], cc);
+        }
+        const ulonglong2 vc = ld2(zc + idx), vd = ld2(zd + idx);
+        const uint64_t z0 = add_mod(vd.x, mul_shoup(sub_mod(vc.x, reduce128(a0, ml), ml.q), pli, plis, ml.q), ml.q);
+        const uint64_t z1 = add_mod(vd.y, mul_shoup(sub_mod(vc.y, reduce128(a1, ml), ml.q), pli, plis, ml.q), ml.q);
+        for (int j = 0; j < l - 1; j++) {
+            const Mod m = mods[j];
+            const uint64_t *row = pmat + (size_t)j * nP;
+            u128 b0{0, 0}, b1{0, 0};
+#pragma unroll
+            for (int k = 0; k < A; k++) {
+                if (k >= nP) break;
+                if (k == 8) {
+                    b0 = u128{reduce128(b0, m), 0};
+                    b1 = u128{reduce128(b1, m), 0};
+                }
+                const uint64_t cc = __ldg(row + k);
+                mac(b0, y0[k], cc);
+                mac(b1, y1[k], cc);
+            }
+            const uint64_t pj = pinv[2 * j], pjs = pinv[2 * j + 1];
+            const uint64_t r0 = add_mod(mul_shoup(reduce128(b0, m), pj, pjs, m.q), reduce64(z0, m), m.q);
+            const uint64_t r1 = add_mod(mul_shoup(reduce128(b1, m), pj, pjs, m.q), reduce64(z1, m), m.q);
+            st2(w + ((size_t)j << log_n) + idx, r0, r1);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ driver
+
+template <class F>
+static Prefix make_prefix(int count, F per_item) {
+    Prefix p{};
+    p.count = count;
+    p.p[0] = 0;
+    for (int c = 0; c < count; c++) p.p[c + 1] = p.p[c] + per_item(c);
+    return p;
+}
+
+void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t item_words,
+                                  const std::vector<BatchItem> &items, const uint64_t *const *rlk, cudaStream_t s) {
+    const Mod *mods = c.d_mods.as<Mod>();
+    const int alpha = c.nP, nQ = c.nQ;
+    const unsigned gx = (unsigned)std::max<uint64_t>(1, c.n / 512);
+    for (size_t base = 0; base < items.size(); base += kMaxBatch) {
+        const int count = (int)std::min<size_t>(kMaxBatch, items.size() - base);
+        BItemsRef r{};
+        r.it.count = count;
+        r.sl = scratch_layout(c);
+        r.log_n = c.log_n;
+        r.alpha = alpha;
+        for (int i = 0; i < count; i++) {
+            const BatchItem &b = items[base + i];
+            const LevelTables &lt = *c.levels[b.l];
+            r.it.l[i] = b.l;
+            r.it.a[i] = b.ct1;
+            r.it.b[i] = b.ct2;
+            r.it.out[i] = b.out;
+            r.it.ws[i] = ws_base + (size_t)i * item_words;
+            r.it.phi[i] = lt.part_hat_inv.as<uint64_t>();
+            r.it.mat[i] = lt.modup_mat.as<uint64_t>();
+            r.it.iq[i] = lt.inv_qlast.as<uint64_t>();
+        }
+        auto lvl = [&](int i) { return r.it.l[i]; };
+        auto beta_of = [&](int i) { return c.beta(lvl(i)); };
+        // 1. mod-up inverse NTT of d2 = a1 * b1, scaled by partQlHatInv
+        {
+            Prefix pre = make_prefix(count, lvl);
+            BScratch<0> y{r};
+            ntt_inv2(c, pre.p[count], BSeqMap{pre}, BD2Load{r, mods}, y, y, BScaleYStore{r, mods}, s);
+        }
+        // 2. mod-up base conversion, per (item, digit)
+        {
+            Prefix pre = make_prefix(count, beta_of);
+            with_digit_bound(alpha, [&]<int A>() {
+                count_launch();
+                modup_bconv_batch<A><<<dim3(gx, pre.p[count]), 256, 0, s>>>(r, pre, mods, nQ);
+            });
+        }
+        // 3. mod-up forward NTT of every digit's complement limbs
+        {
+            BModupMap mm{make_prefix(count, [&](int i) { return beta_of(i) * (lvl(i) + alpha); }), {}, nQ, alpha};
+            for (int i = 0; i < count; i++) mm.l[i] = lvl(i);
+            BScratch<1> tm{r};
+            ntt_fwd2(c, mm.pre.p[count], mm, tm, tm, tm, tm, s);
+        }
+        // 4. inner product, one block row per key limb
+        count_launch();
+        ks_inner_product_batch<<<dim3(gx, (unsigned)(nQ + alpha)), 256, 0, s>>>(r, rlk, mods, nQ, nQ + alpha);
+        // 5. inverse NTT of the P limbs (x PHatInv), cx limb l-1 and tensor limb l-1
+        {
+            BLastLimbMap lm{make_prefix(count, [&](int) { return 2 * (alpha + 2); }), {}, nQ, alpha};
+            for (int i = 0; i < count; i++) lm.l[i] = lvl(i);
+            BScratch<2> mid{r};
+            ntt_inv2(c, lm.pre.p[count], lm, BLastLoad{r, mods}, mid, mid,
+                     BLastStore{r, c.p_hat_inv.as<uint64_t>(), mods}, s);
+        }
+        // 6. w_j = delta_j P^-1 + z mod q_j
+        {
+            Prefix pre = make_prefix(count, [&](int) { return 2; });
+            with_digit_bound(alpha, [&]<int A>() {
+                count_launch();
+                rescale_bconv_batch<A><<<dim3(gx, pre.p[count]), 256, 0, s>>>(r, pre, c.p_mat.as<uint64_t>(),
+                                                                               c.p_inv.as<uint64_t>(), mods);
+            });
+        }
+        // 7. forward NTT of w with the final combine
+        {
+            BFinalMap fm{make_prefix(count, [&](int i) { return 2 * (lvl(i) - 1); }), {}};
+            for (int i = 0; i < count; i++) fm.l[i] = lvl(i);
+            BScratch<3> w{r};
+            ntt_fwd2(c, fm.pre.p[count], fm, w, w, w, BFinalStore{r, c.p_inv.as<uint64_t>(), mods}, s);
+        }
+    }
+}
+
+}  // namespace pfg

@@ -39,6 +39,10 @@ class _Params(ctypes.Structure):
                 ("galois_elts", ctypes.POINTER(ctypes.c_uint32)), ("galois_elts_size", _sz)]
 
 
+class _MulItem(ctypes.Structure):
+    _fields_ = [("ct1", _vp), ("ct2", _vp), ("out", _vp), ("chain_index", _sz)]
+
+
 def _load():
     if not os.path.exists(LIB_PATH):
         raise ImportError(f"{LIB_PATH} is not built; run __graft_entry__.build()")
@@ -56,6 +60,8 @@ def _load():
     L.fhe_workspace_bytes.argtypes = [_vp]
     L.fhe_workspace_create.argtypes = [_vp, ctypes.POINTER(_vp)]
     L.fhe_workspace_destroy.argtypes = [_vp]
+    L.fhe_workspace_create_batch.argtypes = [_vp, _sz, ctypes.POINTER(_vp)]
+    L.fhe_ckks_multiply_relin_rescale_batch.argtypes = [_vp, _vp, ctypes.POINTER(_MulItem), _sz, _vp, _vp]
     for f in ("fhe_ntt_forward", "fhe_ntt_inverse"):
         getattr(L, f).argtypes = [_vp, _vp, _sz, _sz, _sz, _vp]
     L.fhe_ckks_multiply.argtypes = [_vp, _vp, _vp, _sz, _vp]
@@ -164,8 +170,8 @@ class Context:
     def workspace_bytes(self):
         return int(lib.fhe_workspace_bytes(self._h))
 
-    def workspace(self):
-        return Workspace(self)
+    def workspace(self, batch_items=None):
+        return Workspace(self, batch_items)
 
     # --- NTT
     def ntt_forward(self, data, num_polys, limbs, start=0, stream=None):
@@ -202,6 +208,12 @@ class Context:
         _check(lib.fhe_ckks_multiply_relin_rescale(self._h, ws._h, _ptr(ct1), _ptr(ct2), _ptr(out), chain_index,
                                                    key.ptr, _stream(stream)))
 
+    def multiply_relin_rescale_batch(self, ws, items, key, stream=None):
+        """items: list of (ct1, ct2, out, chain_index), uneven chain indices allowed."""
+        arr = (_MulItem * len(items))(*[_MulItem(t1.data_ptr(), t2.data_ptr(), o.data_ptr(), c)
+                                        for t1, t2, o, c in items])
+        _check(lib.fhe_ckks_multiply_relin_rescale_batch(self._h, ws._h, arr, len(items), key.ptr, _stream(stream)))
+
     def apply_galois(self, ws, ct, chain_index, elt, key, stream=None):
         _check(lib.fhe_apply_galois(self._h, ws._h, _ptr(ct), chain_index, elt, key.ptr, _stream(stream)))
 
@@ -222,9 +234,12 @@ class Context:
 
 
 class Workspace:
-    def __init__(self, ctx):
+    def __init__(self, ctx, batch_items=None):
         h = _vp()
-        _check(lib.fhe_workspace_create(ctx._h, ctypes.byref(h)))
+        if batch_items:
+            _check(lib.fhe_workspace_create_batch(ctx._h, batch_items, ctypes.byref(h)))
+        else:
+            _check(lib.fhe_workspace_create(ctx._h, ctypes.byref(h)))
         self._h = h
         self.ctx = ctx
 

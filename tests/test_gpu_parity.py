@@ -322,3 +322,55 @@ def test_n15_bfv_hps_multiply_relin_matches_oracle(pg):
     ta = pg.to_device(a)
     ctx.multiply_and_relin(ws, ta, pg.to_device(b), 1, pg.KeySwitchKey(pg.to_device(key)))
     _eq(ta, oc.bfv_mul_relin_hps(a, b, key), "N=2^15 BFV HPS multiply_and_relin")
+
+
+# ---------------------------------------------------------------- batched HMult (uneven levels)
+
+def _batch_case(pg, ctx, mods, chains, seed):
+    rng = np.random.default_rng(seed)
+    key = _key(rng, mods, ctx.dnum, ctx.n)
+    k = pg.KeySwitchKey(pg.to_device(key))
+    items, host = [], []
+    for ch in chains:
+        l = ctx.level(ch)
+        a = O.random_residues(rng, mods[:l], ctx.n, 2)
+        b = O.random_residues(rng, mods[:l], ctx.n, 2)
+        out = torch.empty((2, l - 1, ctx.n), dtype=torch.int64, device="cuda")
+        items.append((pg.to_device(a), pg.to_device(b), out, ch))
+        host.append((a, b, l))
+    return key, k, items, host
+
+
+def test_batch_multiply_relin_rescale_uneven_levels_small(small, pg):
+    ctx, oc, mods, nq, ws = small
+    chains = [1, 5, 3, 2, 4, 1, 3]
+    key, k, items, host = _batch_case(pg, ctx, mods, chains, 90)
+    wsb = ctx.workspace(batch_items=len(chains))
+    ctx.multiply_relin_rescale_batch(wsb, items, k)
+    for (a, b, l), (_, _, out, ch) in zip(host, items):
+        _eq(out, oc.rescale(l, oc.ckks_mul_relin(l, a, b, key)), f"batch item at chain {ch}")
+
+
+def test_batch_more_than_one_launch_set(small, pg):
+    ctx, oc, mods, nq, ws = small
+    chains = [1 + (i * 7) % 5 for i in range(70)]  # 70 > 64: two launch sets
+    key, k, items, host = _batch_case(pg, ctx, mods, chains, 91)
+    wsb = ctx.workspace(batch_items=64)
+    ctx.multiply_relin_rescale_batch(wsb, items, k)
+    for (a, b, l), (_, _, out, ch) in list(zip(host, items))[::9]:
+        _eq(out, oc.rescale(l, oc.ckks_mul_relin(l, a, b, key)), f"batch item at chain {ch}")
+
+
+def test_n16_batch_equals_single_calls(ckks16, pg):
+    ctx, oc, mods, nq, ws = ckks16
+    rng_chains = np.random.default_rng(92)
+    chains = [int(31 - x) for x in rng_chains.integers(5, 31, size=12)]  # levels 5..30
+    key, k, items, host = _batch_case(pg, ctx, mods, chains, 93)
+    wsb = ctx.workspace(batch_items=len(chains))
+    ctx.multiply_relin_rescale_batch(wsb, items, k)
+    for (a, b, l), (ta, tb, out, ch) in zip(host, items):
+        single = torch.empty_like(out)
+        ctx.multiply_relin_rescale(ws, ta, tb, single, ch, k)
+        assert torch.equal(out, single), f"chain {ch}"
+    a, b, l = host[0]
+    _eq(items[0][2], oc.rescale(l, oc.ckks_mul_relin(l, a, b, key)), "batch item 0 vs oracle")
