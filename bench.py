@@ -210,6 +210,19 @@ def run_ours(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    if args.case == "bfv":  # profiling case: BFV HPS multiply + relinearise at N = 2^15
+        nb = 1 << 15
+        bmods = pg.create_coeff_modulus(nb, [50] * 16 + [60, 60])
+        bctx = pg.Context(nb, bmods, 2, scheme=pg.SCHEME_BFV, plain_modulus=65537)
+        bws = bctx.workspace()
+        bkey = pg.KeySwitchKey(pg.to_device(random_residues(rng, bmods, nb, 2 * bctx.dnum)
+                                            .reshape(bctx.dnum, 2, len(bmods), nb)))
+        x = pg.to_device(random_residues(rng, bmods[:16], nb, 2))
+        y = pg.to_device(random_residues(rng, bmods[:16], nb, 2))
+        for _ in range(args.warmup + args.steps):
+            bctx.multiply_and_relin(bws, x, y, 1, bkey, stream)
+        torch.cuda.synchronize()
+        return
     if args.case == "ntt":  # profiling case: forward NTT of 8 polys x 35 limbs (147 MB)
         big = torch.randint(0, 1 << 40, (8, len(mods), N), dtype=torch.int64, device="cuda")
         for _ in range(args.warmup + args.steps):
@@ -254,6 +267,17 @@ def run_ours(args):
     ntt_gbs = ntt_bytes / t_ntt / 1e9
     del big
 
+    # NTT forward + inverse round trip at N = 2^12 over 3 x 60-bit primes, batch 1 (latency)
+    n12 = 1 << 12
+    c12 = pg.Context(n12, pg.create_coeff_modulus(n12, [60, 60, 60]), 1)
+    d12 = torch.randint(0, 1 << 59, (1, 3, n12), dtype=torch.int64, device="cuda")
+    for _ in range(5):
+        c12.ntt_forward(d12, 1, 3, 0, stream)
+        c12.ntt_inverse(d12, 1, 3, 0, stream)
+    k12 = 200
+    t12 = timed(lambda i: (c12.ntt_forward(d12, 1, 3, 0, stream), c12.ntt_inverse(d12, 1, 3, 0, stream)), k12) / k12
+    del c12, d12
+
     # batch of 64 HMult+relin+rescale at levels drawn uniformly from 5..30 (one call), and the
     # same 64 operations as a loop of single calls
     brng = np.random.default_rng(2000 + rank)
@@ -270,6 +294,29 @@ def run_ours(args):
     t_loop = timed(lambda i: [ctx.multiply_relin_rescale(ws, x[0], x[1], x[2], x[3], key, stream) for x in items],
                    kb) / kb
     del items, wsb
+
+    # BFV multiply + relinearise (HPS) at N = 2^15, 16x50-bit + 2x60-bit, t = 65537:
+    # 128 operations captured in one CUDA graph, replayed
+    bfv_bits = [50] * 16 + [60, 60]
+    nb = 1 << 15
+    bmods = pg.create_coeff_modulus(nb, bfv_bits)
+    bctx = pg.Context(nb, bmods, 2, scheme=pg.SCHEME_BFV, plain_modulus=65537)
+    bws = bctx.workspace()
+    bkey = pg.KeySwitchKey(pg.to_device(random_residues(rng, bmods, nb, 2 * bctx.dnum)
+                                        .reshape(bctx.dnum, 2, len(bmods), nb)))
+    bct = [pg.to_device(random_residues(rng, bmods[:16], nb, 2)) for _ in range(2)]
+    bpairs = [(bct[0].clone(), bct[1]) for _ in range(128)]
+    for x, y in bpairs[:3]:
+        bctx.multiply_and_relin(bws, x, y, 1, bkey, stream)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        for x, y in bpairs:
+            bctx.multiply_and_relin(bws, x, y, 1, bkey)
+    g.replay()
+    t_graph = timed(lambda i: g.replay(), 3) / 3
+    t_bloop = timed(lambda i: [bctx.multiply_and_relin(bws, x, y, 1, bkey, stream) for x, y in bpairs], 3) / 3
+    del g, bpairs, bct, bws, bctx
 
     # end to end through the C ABI with host buffers: H2D of both inputs, D2H of the result
     pin_a = [torch.empty((2, l, N), dtype=torch.int64).pin_memory() for _ in range(PAIRS)]
@@ -312,7 +359,10 @@ def run_ours(args):
                          "bound": "hbm", "achieved": ntt_gbs, "peak": peak, "unit": "GB/s",
                          "frac": ntt_gbs / peak, "peak_source": peak_kind,
                          "algorithmic_bytes": ntt_bytes, "traffic": traffic},
-            "extra": {"batch64_uneven_levels_ops_per_s": 64 * world / t_batch,
+            "extra": {"ntt_n12_3x60_roundtrip_us": 1e6 * t12,
+                      "bfv_n15_mult_relin_graph128_ops_per_s": 128 * world / t_graph,
+                      "bfv_n15_mult_relin_loop128_ops_per_s": 128 * world / t_bloop,
+                      "batch64_uneven_levels_ops_per_s": 64 * world / t_batch,
                       "batch64_as_single_calls_ops_per_s": 64 * world / t_loop,
                       "hrotate_step1_per_s": k2 * world / t_rot, "keyswitch_per_s": k2 * world / t_ks,
                       "ntt_forward_ms_64x35": 1000 * t_ntt,
@@ -335,7 +385,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--case", choices=["full", "hmult", "ntt"], default="full",
+    ap.add_argument("--case", choices=["full", "hmult", "ntt", "bfv"], default="full",
                     help="hmult / ntt: run only that part (for profiler captures), print nothing")
     args = ap.parse_args()
     if args.impl == "reference":
