@@ -26,59 +26,88 @@ static int grid_for_bfv(size_t work, int per_block) {
 
 // ------------------------------------------------------------------ HPS base conversion
 
+// Both HPS kernels work on a tile of kHpsTile coefficients per block of 256 threads, with the
+// tile's inputs in shared memory: the per-coefficient FP64 sums run in the reference's loop order
+// (one thread per coefficient), and the integer sums are spread over (output limb, coefficient)
+// pairs so every thread is busy.
+constexpr int kHpsTile = 64;
+
 // out[j] = (sum_i y_i * mat[j][i] mod p_j) - alpha_tab[v][j],  y_i = x_i * hat_inv_i mod q_i,
-// v = llround(sum_i fma(y_i, inv_i)).  One thread per coefficient, y staged in shared memory.
-__global__ void __launch_bounds__(128) hps_bconv(uint64_t *out, long long ops, const uint64_t *in, long long ips,
+// v = llround(sum_i fma(y_i, inv_i)).
+__global__ void __launch_bounds__(256) hps_bconv(uint64_t *out, long long ops, const uint64_t *in, long long ips,
                                                  const Mod *mods, int ib0, int ni, int ob0, int no,
                                                  const uint64_t *hat_inv, const double *inv, const uint64_t *mat,
                                                  const uint64_t *alpha_tab, int log_n) {
-    extern __shared__ uint64_t ys[];  // [ni][128]
+    extern __shared__ uint64_t sh[];
+    uint64_t *ys = sh;                                  // [ni][kHpsTile]
+    long long *vs = reinterpret_cast<long long *>(sh + (size_t)ni * kHpsTile);  // [kHpsTile]
     const uint32_t n = 1u << log_n;
     const int poly = blockIdx.y;
-    const uint32_t idx = blockIdx.x * 128 + threadIdx.x;
-    const uint64_t *x = in + poly * ips;
-    double acc = 0.0;
-    for (int i = 0; i < ni; i++) {
-        const uint64_t q = mods[ib0 + i].q;
-        const uint64_t y = mul_shoup(x[(size_t)i * n + idx], hat_inv[2 * i], hat_inv[2 * i + 1], q);
-        ys[i * 128 + threadIdx.x] = y;
-        acc = __fma_rn(__ull2double_rn(y), inv[i], acc);
+    const uint32_t c0 = blockIdx.x * kHpsTile;
+    const uint64_t *x = in + poly * ips + c0;
+    for (int p = threadIdx.x; p < ni * kHpsTile; p += blockDim.x) {
+        const int i = p / kHpsTile, c = p % kHpsTile;
+        ys[p] = mul_shoup(x[(size_t)i * n + c], hat_inv[2 * i], hat_inv[2 * i + 1], mods[ib0 + i].q);
     }
-    const long long v = llround(acc);
-    uint64_t *o = out + poly * ops;
-    for (int j = 0; j < no; j++) {
+    __syncthreads();
+    if (threadIdx.x < kHpsTile) {
+        double acc = 0.0;
+        for (int i = 0; i < ni; i++) acc = __fma_rn(__ull2double_rn(ys[i * kHpsTile + threadIdx.x]), inv[i], acc);
+        vs[threadIdx.x] = llround(acc);
+    }
+    __syncthreads();
+    uint64_t *o = out + poly * ops + c0;
+    for (int p = threadIdx.x; p < no * kHpsTile; p += blockDim.x) {
+        const int j = p / kHpsTile, c = p % kHpsTile;
         const Mod m = mods[ob0 + j];
-        u128 s{0, 0};
+        const uint64_t *row = mat + (size_t)j * ni;
+        u128 acc{0, 0};
         int terms = 0;
         for (int i = 0; i < ni; i++) {
             if (terms == 7) {
-                s = u128{reduce128(s, m), 0};
+                acc = u128{reduce128(acc, m), 0};
                 terms = 1;
             }
-            mac(s, ys[i * 128 + threadIdx.x], __ldg(mat + (size_t)j * ni + i));
+            mac(acc, ys[i * kHpsTile + c], __ldg(row + i));
             terms++;
         }
-        o[(size_t)j * n + idx] = sub_mod(reduce128(s, m), __ldg(alpha_tab + (size_t)v * no + j), m.q);
+        o[(size_t)j * n + c] = sub_mod(reduce128(acc, m), __ldg(alpha_tab + (size_t)vs[c] * no + j), m.q);
     }
 }
 
-// scaleAndRound_HPS_QR_R followed by bConv_HPS R -> Q for one coefficient per thread.
-__global__ void __launch_bounds__(128) hps_scale_round_to_q(uint64_t *out, long long ops, const uint64_t *in,
+// scaleAndRound_HPS_QR_R followed by bConv_HPS R -> Q.
+__global__ void __launch_bounds__(256) hps_scale_round_to_q(uint64_t *out, long long ops, const uint64_t *in,
                                                             long long ips, const Mod *mods, int nQ, int rbase,
                                                             int nR, const double *frac, const uint64_t *modr,
                                                             const uint64_t *r_hat_inv, const double *r_inv,
                                                             const uint64_t *r2q, const uint64_t *r2q_alpha,
                                                             int log_n) {
-    extern __shared__ uint64_t ys[];  // [nR][128]
+    extern __shared__ uint64_t sh[];
+    const int nqr = nQ + nR;
+    uint64_t *xs = sh;                                   // [nQ + nR][kHpsTile]
+    uint64_t *ys = xs + (size_t)nqr * kHpsTile;          // [nR][kHpsTile]
+    uint64_t *as = ys + (size_t)nR * kHpsTile;           // [nR][kHpsTile] carry alpha, reduced in place
+    long long *vs = reinterpret_cast<long long *>(as + (size_t)nR * kHpsTile);  // [kHpsTile]
     const uint32_t n = 1u << log_n;
     const int poly = blockIdx.y;
-    const uint32_t idx = blockIdx.x * 128 + threadIdx.x;
-    const uint64_t *x = in + poly * ips + idx;
-    double nu = 0.5;
-    for (int i = 0; i < nQ; i++) nu = __fma_rn(__ull2double_rn(__ldg(x + (size_t)i * n)), frac[i], nu);
-    uint64_t alpha = __double2ull_rz(nu);
-    double acc = 0.0;
-    for (int j = 0; j < nR; j++) {
+    const uint32_t c0 = blockIdx.x * kHpsTile;
+    const uint64_t *x = in + poly * ips + c0;
+    for (int p = threadIdx.x; p < nqr * kHpsTile; p += blockDim.x)
+        xs[p] = x[(size_t)(p / kHpsTile) * n + (p % kHpsTile)];
+    __syncthreads();
+    if (threadIdx.x < kHpsTile) {
+        double nu = 0.5;
+        for (int i = 0; i < nQ; i++) nu = __fma_rn(__ull2double_rn(xs[i * kHpsTile + threadIdx.x]), frac[i], nu);
+        // the reference reduces alpha in place across r_0 .. r_j; keep every step of that chain
+        uint64_t alpha = __double2ull_rz(nu);
+        for (int j = 0; j < nR; j++) {
+            alpha = reduce64(alpha, mods[rbase + j]);
+            as[j * kHpsTile + threadIdx.x] = alpha;
+        }
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < nR * kHpsTile; p += blockDim.x) {
+        const int j = p / kHpsTile, c = p % kHpsTile;
         const Mod m = mods[rbase + j];
         const uint64_t *row = modr + (size_t)j * (nQ + 1);
         u128 cur{0, 0};
@@ -88,20 +117,24 @@ __global__ void __launch_bounds__(128) hps_scale_round_to_q(uint64_t *out, long 
                 cur = u128{reduce128(cur, m), 0};
                 terms = 1;
             }
-            mac(cur, __ldg(x + (size_t)i * n), __ldg(row + i));
+            mac(cur, xs[i * kHpsTile + c], __ldg(row + i));
             terms++;
         }
         if (terms == 7) cur = u128{reduce128(cur, m), 0};
-        mac(cur, __ldg(x + (size_t)(nQ + j) * n), __ldg(row + nQ));
-        alpha = reduce64(alpha, m);  // in place, as the reference does
-        const uint64_t rt = add_mod(reduce128(cur, m), alpha, m.q);
-        const uint64_t y = mul_shoup(rt, r_hat_inv[2 * j], r_hat_inv[2 * j + 1], m.q);
-        ys[j * 128 + threadIdx.x] = y;
-        acc = __fma_rn(__ull2double_rn(y), r_inv[j], acc);
+        mac(cur, xs[(nQ + j) * kHpsTile + c], __ldg(row + nQ));
+        const uint64_t rt = add_mod(reduce128(cur, m), as[p], m.q);
+        ys[p] = mul_shoup(rt, r_hat_inv[2 * j], r_hat_inv[2 * j + 1], m.q);
     }
-    const long long v = llround(acc);
-    uint64_t *o = out + poly * ops;
-    for (int i = 0; i < nQ; i++) {
+    __syncthreads();
+    if (threadIdx.x < kHpsTile) {
+        double acc = 0.0;
+        for (int j = 0; j < nR; j++) acc = __fma_rn(__ull2double_rn(ys[j * kHpsTile + threadIdx.x]), r_inv[j], acc);
+        vs[threadIdx.x] = llround(acc);
+    }
+    __syncthreads();
+    uint64_t *o = out + poly * ops + c0;
+    for (int p = threadIdx.x; p < nQ * kHpsTile; p += blockDim.x) {
+        const int i = p / kHpsTile, c = p % kHpsTile;
         const Mod m = mods[i];
         u128 s{0, 0};
         int terms = 0;
@@ -110,10 +143,10 @@ __global__ void __launch_bounds__(128) hps_scale_round_to_q(uint64_t *out, long 
                 s = u128{reduce128(s, m), 0};
                 terms = 1;
             }
-            mac(s, ys[j * 128 + threadIdx.x], __ldg(r2q + (size_t)i * nR + j));
+            mac(s, ys[j * kHpsTile + c], __ldg(r2q + (size_t)i * nR + j));
             terms++;
         }
-        o[(size_t)i * n + idx] = sub_mod(reduce128(s, m), __ldg(r2q_alpha + (size_t)v * nQ + i), m.q);
+        o[(size_t)i * n + c] = sub_mod(reduce128(s, m), __ldg(r2q_alpha + (size_t)vs[c] * nQ + i), m.q);
     }
 }
 
@@ -249,20 +282,20 @@ void bfv_mul_relin_hps(const Context &c, const Workspace &w, uint64_t *ct1, cons
     const bool square = ct1 == ct2;
     // 1. extend both operands to QR
     cudaMemcpy2DAsync(ea, qrps * 8, ct1, qps * 8, qps * 8, 2, cudaMemcpyDeviceToDevice, s);
-    dim3 g((unsigned)(n / 128), 2);
-    const size_t sm_q = (size_t)nQ * 128 * 8, sm_r = (size_t)nR * 128 * 8;
+    dim3 g((unsigned)(n / kHpsTile), 2);
+    const size_t sm_q = ((size_t)nQ + 1) * kHpsTile * 8, sm_r = ((size_t)3 * nR + nQ + 1) * kHpsTile * 8;
     if (sm_q > 48 * 1024) cudaFuncSetAttribute(hps_bconv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_q);
     if (sm_r > 48 * 1024)
         cudaFuncSetAttribute(hps_scale_round_to_q, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_r);
     count_launch();
-    hps_bconv<<<g, 128, sm_q, s>>>(ea + qps, qrps, ct1, qps, mods, 0, nQ, rbase, nR, c.hps_q_hat_inv.as<uint64_t>(),
+    hps_bconv<<<g, 256, sm_q, s>>>(ea + qps, qrps, ct1, qps, mods, 0, nQ, rbase, nR, c.hps_q_hat_inv.as<uint64_t>(),
                                    c.hps_q_inv.as<double>(), c.hps_q2r_mat.as<uint64_t>(),
                                    c.hps_q2r_alpha.as<uint64_t>(), c.log_n);
     const uint64_t *ebp = ea;
     if (!square) {
         cudaMemcpy2DAsync(eb, qrps * 8, ct2, qps * 8, qps * 8, 2, cudaMemcpyDeviceToDevice, s);
         count_launch();
-        hps_bconv<<<g, 128, sm_q, s>>>(eb + qps, qrps, ct2, qps, mods, 0, nQ, rbase, nR,
+        hps_bconv<<<g, 256, sm_q, s>>>(eb + qps, qrps, ct2, qps, mods, 0, nQ, rbase, nR,
                                        c.hps_q_hat_inv.as<uint64_t>(), c.hps_q_inv.as<double>(),
                                        c.hps_q2r_mat.as<uint64_t>(), c.hps_q2r_alpha.as<uint64_t>(), c.log_n);
         ebp = eb;
@@ -274,9 +307,9 @@ void bfv_mul_relin_hps(const Context &c, const Workspace &w, uint64_t *ct1, cons
     PtrStore t3s{t3, qrps, c.log_n};
     ntt_inv(c, 3 * qr, qm, TensorQrLoad{ea, ebp, qrps, mods, c.log_n}, t3s, t3s, s);
     // 3. scale and round to R, then back to Q
-    dim3 g3((unsigned)(n / 128), 3);
+    dim3 g3((unsigned)(n / kHpsTile), 3);
     count_launch();
-    hps_scale_round_to_q<<<g3, 128, sm_r, s>>>(o3, qps, t3, qrps, mods, nQ, rbase, nR, c.hps_frac.as<double>(),
+    hps_scale_round_to_q<<<g3, 256, sm_r, s>>>(o3, qps, t3, qrps, mods, nQ, rbase, nR, c.hps_frac.as<double>(),
                                                 c.hps_modr.as<uint64_t>(), c.hps_r_hat_inv.as<uint64_t>(),
                                                 c.hps_r_inv.as<double>(), c.hps_r2q_mat.as<uint64_t>(),
                                                 c.hps_r2q_alpha.as<uint64_t>(), c.log_n);
