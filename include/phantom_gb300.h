@@ -185,6 +185,58 @@ int fhe_rotate(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t c
 int fhe_hoisting(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t chain_index, const int *steps,
                  size_t num_steps, const uint64_t *const *const *galois_keys, void *stream);
 
+/* Rotations of one ciphertext by several steps that share one mod-up of c1, each result kept
+ * (the baby steps of a matrix-vector product).  The reference computes them as separate
+ * rotate calls (python/src/binding.cu:529-533 calling src/evaluate.cu:1665).  outs[i] equals
+ * hoisting(ct, {steps[i]}) (src/evaluate.cu:1670-1865) word for word: the same plaintext as
+ * rotate(ct, steps[i]), with the noise of a mod-up taken before the permutation.  Each step
+ * needs its own Galois key. */
+int fhe_ckks_rotations_hoisted(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *ct, size_t chain_index,
+                               const int *steps, size_t num_steps, const uint64_t *const *const *galois_keys,
+                               uint64_t *const *outs, void *stream);
+
+/* multiply_plain (include/evaluate.cuh:94-100, src/evaluate.cu:1224-1250, CKKS NTT form):
+ * out (2 polys) = ct * pt, pt one polynomial over the same chain_index.  out may alias ct. */
+int fhe_ckks_multiply_plain(const fhe_context *ctx, const uint64_t *ct, const uint64_t *pt, uint64_t *out,
+                            size_t chain_index, void *stream);
+
+/* add_inplace (include/evaluate.cuh:46, src/evaluate.cu:116-198): out = a + b, `size` polys. */
+int fhe_ckks_add(const fhe_context *ctx, const uint64_t *a, const uint64_t *b, uint64_t *out, size_t size,
+                 size_t chain_index, void *stream);
+
+/* Baby-step/giant-step plaintext-matrix x ciphertext-vector product, the
+ * bsgs_complete_from_cpu binding (python/src/binding.cu:507-595): D diagonals (device array
+ * [D][limbs][N], already encoded at chain_index), G baby steps, B giant steps (G * B >= D);
+ * out (2 polys at chain_index + 1) = Rescale(sum_g rot_{gG}(sum_b ct_b * diag_{gG+b})).
+ * hoisted = 0 runs the reference's loop (one rotation per baby step, giant rotations by g*G,
+ * keys for 1..G-1 and every g*G or their NAF parts) and gives its words exactly; hoisted = 1
+ * computes the baby steps with one shared mod-up and the giant steps by Horner's rule with
+ * rotations by G only (keys for 1..G-1 and G): the same plaintext, different noise.
+ * scratch: fhe_bsgs_scratch_bytes(ctx, G) bytes of device memory. */
+size_t fhe_bsgs_scratch_bytes(const fhe_context *ctx, size_t G);
+int fhe_ckks_bsgs_matvec(const fhe_context *ctx, fhe_workspace *ws, uint64_t *scratch, const uint64_t *ct,
+                         size_t chain_index, const uint64_t *diags, size_t D, size_t G, size_t B,
+                         const uint64_t *const *const *galois_keys, uint64_t *out, int hoisted, void *stream);
+
+/* PhantomSecretKey::encrypt_symmetric, CKKS (src/secretkey.cu:463-500 with
+ * encrypt_zero_symmetric, 232-295) with the randomness supplied by the caller instead of the
+ * reference's device PRNG: out = (pt - (a*s + NTT(e)), a).  s and a in NTT form over the
+ * ciphertext's limbs, e an int64 polynomial of N coefficients; pt may be NULL (zero). */
+int fhe_ckks_encrypt_symmetric(const fhe_context *ctx, const uint64_t *pt, const uint64_t *s_ntt, const uint64_t *a,
+                               const int64_t *e, uint64_t *out, size_t chain_index, void *stream);
+
+/* PhantomSecretKey::decrypt, CKKS (src/secretkey.cu:693-720): pt = c0 + c1 * s (NTT form). */
+int fhe_ckks_decrypt(const fhe_context *ctx, const uint64_t *ct, const uint64_t *s_ntt, uint64_t *pt,
+                     size_t chain_index, void *stream);
+
+/* PhantomSecretKey::generate_one_kswitch_key (src/secretkey.cu:297-341) for create_relin_keys
+ * (galois_elt = 0, source key s^2) and create_galois_keys (source key sigma_elt(s)), with the
+ * randomness supplied by the caller: a = dnum uniform polynomials [dnum][QP][N] in NTT form,
+ * e = dnum int64 error polynomials [dnum][N].  key receives [dnum][2][QP][N] with
+ * key[d] = (-(a_d s + e_d) + (P mod q_j) s_src on digit d's limbs, a_d).  s_ntt covers QP. */
+int fhe_kswitch_keygen(const fhe_context *ctx, fhe_workspace *ws, uint32_t galois_elt, const uint64_t *s_ntt,
+                       const uint64_t *a, const int64_t *e, uint64_t *key, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -324,7 +324,7 @@ int fhe_ckks_multiply_relin_rescale_batch(const fhe_context *ctx, fhe_workspace 
     });
 }
 
-static int galois_index(const pfg::Context &c, uint32_t elt) {
+int galois_index(const pfg::Context &c, uint32_t elt) {
     auto it = std::find(c.galois_elts.begin(), c.galois_elts.end(), elt);
     return it == c.galois_elts.end() ? -1 : (int)(it - c.galois_elts.begin());
 }
@@ -343,28 +343,133 @@ int fhe_apply_galois(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, si
     });
 }
 
-static void rotate_rec(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t chain_index, int step,
-                       const uint64_t *const *const *gks, void *stream) {
-    const pfg::Context &c = ctx_of(ctx);
-    const uint32_t elt = pfg::host::elt_from_step(step, c.n);
-    const int idx = galois_index(c, elt);
-    if (idx >= 0) {
-        int rc = fhe_apply_galois(ctx, ws, ct, chain_index, elt, gks[idx], stream);
-        if (rc != FHE_OK) throw std::invalid_argument(g_last_error);
-        return;
-    }
-    // NAF decomposition (src/evaluate.cu:1647-1661)
-    auto naf = pfg::host::naf(step);
-    if (naf.size() == 1) throw std::invalid_argument("Galois key not present");
-    for (int s : naf)
-        if ((uint64_t)std::abs(s) != (c.n >> 1)) rotate_rec(ctx, ws, ct, chain_index, s, gks, stream);
-}
-
 int fhe_rotate(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t chain_index, int step,
                const uint64_t *const *const *galois_keys, void *stream) {
     return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        pfg::Workspace w = ws_of(ctx, ws);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("Galois automorphisms are implemented for CKKS");
+        need_keyswitching(c);
+        need_ptr(ct, "ct");
         need_ptr(galois_keys, "galois_keys");
-        rotate_rec(ctx, ws, ct, chain_index, step, galois_keys, stream);
+        pfg::ckks_rotate(c, w, ct, level_of(c, chain_index), step, galois_keys, st(stream));
+    });
+}
+
+int fhe_ckks_rotations_hoisted(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *ct, size_t chain_index,
+                               const int *steps, size_t num_steps, const uint64_t *const *const *galois_keys,
+                               uint64_t *const *outs, void *stream) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        pfg::Workspace w = ws_of(ctx, ws);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("rotations are implemented for CKKS");
+        need_keyswitching(c);
+        need_ptr(ct, "ct");
+        need_ptr(steps, "steps");
+        need_ptr(galois_keys, "galois_keys");
+        need_ptr(outs, "outs");
+        std::vector<pfg::StepKey> sk;
+        std::vector<uint64_t *> o;
+        for (size_t i = 0; i < num_steps; i++) {
+            const uint32_t elt = pfg::host::elt_from_step(steps[i], c.n);
+            const int idx = galois_index(c, elt);
+            if (idx < 0 || !galois_keys[idx]) throw std::logic_error("Galois key not present in hoisting");
+            need_ptr(outs[i], "outs[i]");
+            sk.push_back(pfg::StepKey{c.perm_table(elt), galois_keys[idx]});
+            o.push_back(outs[i]);
+        }
+        if (!sk.empty()) pfg::ckks_rotations_hoisted(c, w, ct, level_of(c, chain_index), sk, o, st(stream));
+    });
+}
+
+int fhe_ckks_multiply_plain(const fhe_context *ctx, const uint64_t *ct, const uint64_t *pt, uint64_t *out,
+                            size_t chain_index, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("multiply_plain: CKKS only");
+        need_ptr(ct, "ct");
+        need_ptr(pt, "pt");
+        need_ptr(out, "out");
+        pfg::ckks_multiply_plain(c, ct, pt, out, level_of(c, chain_index), st(stream));
+    });
+}
+
+int fhe_ckks_add(const fhe_context *ctx, const uint64_t *a, const uint64_t *b, uint64_t *out, size_t size,
+                 size_t chain_index, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        need_ptr(a, "a");
+        need_ptr(b, "b");
+        need_ptr(out, "out");
+        if (size == 0 || size > 3) throw std::invalid_argument("bad ciphertext size");
+        pfg::ckks_add(c, a, b, out, level_of(c, chain_index), (int)size, st(stream));
+    });
+}
+
+size_t fhe_bsgs_scratch_bytes(const fhe_context *ctx, size_t G) {
+    if (!ctx || !ctx->c || G == 0) return 0;
+    return pfg::bsgs_scratch_words(*ctx->c, (int)G) * sizeof(uint64_t);
+}
+
+int fhe_ckks_bsgs_matvec(const fhe_context *ctx, fhe_workspace *ws, uint64_t *scratch, const uint64_t *ct,
+                         size_t chain_index, const uint64_t *diags, size_t D, size_t G, size_t B,
+                         const uint64_t *const *const *galois_keys, uint64_t *out, int hoisted, void *stream) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        pfg::Workspace w = ws_of(ctx, ws);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("matrix-vector product: CKKS only");
+        need_keyswitching(c);
+        need_ptr(scratch, "scratch");
+        need_ptr(ct, "ct");
+        need_ptr(diags, "diags");
+        need_ptr(galois_keys, "galois_keys");
+        need_ptr(out, "out");
+        if (D == 0 || G == 0 || B == 0 || G * B < D) throw std::invalid_argument("need D > 0 and G * B >= D");
+        if (G > 256) throw std::invalid_argument("too many baby steps");
+        const int l = level_of(c, chain_index);
+        if (l < 2) throw std::invalid_argument("end of modulus switching chain reached");
+        pfg::ckks_bsgs_matvec(c, w, scratch, ct, l, diags, (int)D, (int)G, (int)B, galois_keys, out, hoisted != 0,
+                              st(stream));
+    });
+}
+
+int fhe_ckks_encrypt_symmetric(const fhe_context *ctx, const uint64_t *pt, const uint64_t *s_ntt, const uint64_t *a,
+                               const int64_t *e, uint64_t *out, size_t chain_index, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        need_ptr(s_ntt, "s");
+        need_ptr(a, "a");
+        need_ptr(e, "e");
+        need_ptr(out, "out");
+        pfg::ckks_encrypt_sk(c, pt, s_ntt, a, e, out, level_of(c, chain_index), st(stream));
+    });
+}
+
+int fhe_ckks_decrypt(const fhe_context *ctx, const uint64_t *ct, const uint64_t *s_ntt, uint64_t *pt,
+                     size_t chain_index, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        need_ptr(ct, "ct");
+        need_ptr(s_ntt, "s");
+        need_ptr(pt, "pt");
+        pfg::ckks_decrypt(c, ct, s_ntt, pt, level_of(c, chain_index), st(stream));
+    });
+}
+
+int fhe_kswitch_keygen(const fhe_context *ctx, fhe_workspace *ws, uint32_t galois_elt, const uint64_t *s_ntt,
+                       const uint64_t *a, const int64_t *e, uint64_t *key, void *stream) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        pfg::Workspace w = ws_of(ctx, ws);
+        need_keyswitching(c);
+        need_ptr(s_ntt, "s");
+        need_ptr(a, "a");
+        need_ptr(e, "e");
+        need_ptr(key, "key");
+        if (galois_elt && galois_index(c, galois_elt) < 0) throw std::invalid_argument("Galois elt not present");
+        const size_t need = (size_t)(c.beta(c.nQ) + 1) * (c.nQ + c.nP) * c.n + 64;
+        if (w.words < need) throw std::logic_error("workspace too small for key generation");
+        pfg::kswitch_keygen(c, galois_elt, s_ntt, a, e, key, w.base, st(stream));
     });
 }
 

@@ -50,6 +50,24 @@ void ckks_apply_galois(const Context &c, const Workspace &w, uint64_t *ct, int l
 void ckks_hoisting(const Context &c, const Workspace &w, uint64_t *ct, int l, const std::vector<StepKey> &steps,
                    cudaStream_t s);
 
+void ckks_rotations_hoisted(const Context &c, const Workspace &w, const uint64_t *ct, int l,
+                            const std::vector<StepKey> &steps, const std::vector<uint64_t *> &outs, cudaStream_t s);
+void ckks_multiply_plain(const Context &c, const uint64_t *ct, const uint64_t *pt, uint64_t *out, int l,
+                         cudaStream_t s);
+void ckks_add(const Context &c, const uint64_t *a, const uint64_t *b, uint64_t *out, int l, int polys,
+              cudaStream_t s);
+void ckks_rotate(Context &c, const Workspace &w, uint64_t *ct, int l, int step,
+                 const uint64_t *const *const *galois_keys, cudaStream_t s);
+size_t bsgs_scratch_words(const Context &c, int G);
+void ckks_bsgs_matvec(Context &c, const Workspace &w, uint64_t *scratch, const uint64_t *ct, int l,
+                      const uint64_t *diags, int D, int G, int B, const uint64_t *const *const *galois_keys,
+                      uint64_t *out, bool hoisted, cudaStream_t s);
+void ckks_encrypt_sk(const Context &c, const uint64_t *m, const uint64_t *s_ntt, const uint64_t *a, const int64_t *e,
+                     uint64_t *out, int l, cudaStream_t st);
+void ckks_decrypt(const Context &c, const uint64_t *ct, const uint64_t *s_ntt, uint64_t *m, int l, cudaStream_t st);
+void kswitch_keygen(Context &c, uint32_t elt, const uint64_t *s_ntt, const uint64_t *a, const int64_t *e,
+                    uint64_t *key, uint64_t *scratch, cudaStream_t st);
+
 // BFV (coefficient form).
 void bfv_keyswitch(const Context &c, const Workspace &w, uint64_t *ct, const uint64_t *c2, int l,
                    const uint64_t *const *evk, cudaStream_t s);

@@ -35,8 +35,8 @@ size_t workspace_words(const Context &c) {
     size_t w = 0;
     if (a) {
         const size_t beta = c.beta((int)nQ), qlp = nQ + a;
-        // y | tm | cx | g0,g1 (or acc0) | z (4 limbs)
-        w = n * (nQ + beta * qlp + 2 * qlp + 2 * nQ + 4);
+        // y | tm | cx | g0,g1 (or acc0) | z (4 limbs) | h [2][nQ] (hoisted rotations' mod-down)
+        w = n * (nQ + beta * qlp + 2 * qlp + 2 * nQ + 4 + 2 * nQ);
     }
     if (c.scheme == kSchemeBFV) {
         const size_t qr = nQ + c.nR;
@@ -167,7 +167,7 @@ static int grid_for(size_t work, int per_block) {
 // ------------------------------------------------------------------ pipeline pieces
 
 struct KsBuffers {
-    uint64_t *y, *tm, *cx, *g, *z;
+    uint64_t *y, *tm, *cx, *g, *z, *h;
 };
 
 static KsBuffers ks_buffers(const Context &c, const Workspace &w) {
@@ -178,6 +178,7 @@ static KsBuffers ks_buffers(const Context &c, const Workspace &w) {
     b.cx = b.tm + beta * qlp * n;
     b.g = b.cx + 2 * qlp * n;
     b.z = b.g + 2 * nQ * n;
+    b.h = b.z + 4 * n;
     return b;
 }
 
@@ -550,6 +551,34 @@ void ckks_hoisting(const Context &c, const Workspace &w, uint64_t *ct, int l, co
     }
     moddown_intt_p(c, b, l, s);
     moddown_ntt(c, b, b.tm, l, 0, l, ct, ct + lps, FirstPolyBase{acc0, c.log_n}, s);
+}
+
+// Individual rotations sharing one mod-up of c1 (GB300 addition; the reference's
+// hoisting_inplace returns only their sum).  outs[i] (2 polys at level l) = rotation by steps[i]:
+// (sigma(c0) + ModDown(<sigma(ModUp(c1)), gk>)_0, ModDown(...)_1).  The automorphism is applied
+// to the mod-up digits, exactly as hoisting_inplace does, so outs[i] decrypts like rotate() but
+// is not word-identical to it.
+void ckks_rotations_hoisted(const Context &c, const Workspace &w, const uint64_t *ct, int l,
+                            const std::vector<StepKey> &steps, const std::vector<uint64_t *> &outs, cudaStream_t s) {
+    const KsBuffers b = ks_buffers(c, w);
+    const long long lps = (long long)l << c.log_n;
+    const uint64_t *c1 = ct + lps;
+    modup_ckks(c, b, PtrLoad{c1, lps, c.log_n}, l, s);
+    const int qlp = l + c.nP;
+    for (size_t i = 0; i < steps.size(); i++) {
+        count_launch();
+        galois_permute<<<grid_for((size_t)lps, 256), 256, 0, s>>>(b.g, ct, steps[i].perm, c.log_n, (size_t)lps);
+        HoistSteps hs{};
+        hs.count = 1;
+        hs.perm[0] = steps[i].perm;
+        hs.key[0] = steps[i].key;
+        count_launch();
+        ks_inner_product_hoisted<<<grid_for((size_t)qlp << c.log_n, 256), 256, 0, s>>>(
+                b.cx, b.tm, c1, hs, c.d_mods.as<Mod>(), c.log_n, l, c.nQ, c.nP, c.beta(l), c.nQ + c.nP, false);
+        moddown_intt_p(c, b, l, s);
+        // the mod-down's scratch must not be tm (it still holds the shared mod-up)
+        moddown_ntt(c, b, b.h, l, 0, l, outs[i], outs[i] + lps, FirstPolyBase{b.g, c.log_n}, s);
+    }
 }
 
 // ------------------------------------------------------------------ tensor (standalone)

@@ -75,6 +75,17 @@ def _load():
     L.fhe_apply_galois.argtypes = [_vp, _vp, _vp, _sz, ctypes.c_uint32, _vp, _vp]
     L.fhe_rotate.argtypes = [_vp, _vp, _vp, _sz, ctypes.c_int, ctypes.POINTER(_vp), _vp]
     L.fhe_hoisting.argtypes = [_vp, _vp, _vp, _sz, ctypes.POINTER(ctypes.c_int), _sz, ctypes.POINTER(_vp), _vp]
+    L.fhe_ckks_rotations_hoisted.argtypes = [_vp, _vp, _vp, _sz, ctypes.POINTER(ctypes.c_int), _sz,
+                                             ctypes.POINTER(_vp), ctypes.POINTER(_vp), _vp]
+    L.fhe_ckks_multiply_plain.argtypes = [_vp, _vp, _vp, _vp, _sz, _vp]
+    L.fhe_ckks_add.argtypes = [_vp, _vp, _vp, _vp, _sz, _sz, _vp]
+    L.fhe_bsgs_scratch_bytes.restype = _sz
+    L.fhe_bsgs_scratch_bytes.argtypes = [_vp, _sz]
+    L.fhe_ckks_bsgs_matvec.argtypes = [_vp, _vp, _vp, _vp, _sz, _vp, _sz, _sz, _sz, ctypes.POINTER(_vp), _vp,
+                                       ctypes.c_int, _vp]
+    L.fhe_ckks_encrypt_symmetric.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]
+    L.fhe_ckks_decrypt.argtypes = [_vp, _vp, _vp, _vp, _sz, _vp]
+    L.fhe_kswitch_keygen.argtypes = [_vp, _vp, ctypes.c_uint32, _vp, _vp, _vp, _vp, _vp]
     return L
 
 
@@ -231,6 +242,42 @@ class Context:
         st = (ctypes.c_int * len(steps))(*steps)
         _check(lib.fhe_hoisting(self._h, ws._h, _ptr(ct), chain_index, st, len(steps), self._gk_array(galois_keys),
                                 _stream(stream)))
+
+
+    def rotations_hoisted(self, ws, ct, chain_index, steps, galois_keys, outs, stream=None):
+        """outs[i] <- ct rotated by steps[i]; one mod-up of c1 shared by all steps."""
+        st = (ctypes.c_int * len(steps))(*steps)
+        o = (_vp * len(outs))(*[t.data_ptr() for t in outs])
+        _check(lib.fhe_ckks_rotations_hoisted(self._h, ws._h, _ptr(ct), chain_index, st, len(steps),
+                                              self._gk_array(galois_keys), o, _stream(stream)))
+
+    def multiply_plain(self, ct, pt, out, chain_index, stream=None):
+        _check(lib.fhe_ckks_multiply_plain(self._h, _ptr(ct), _ptr(pt), _ptr(out), chain_index, _stream(stream)))
+
+    def add(self, a, b, out, size, chain_index, stream=None):
+        _check(lib.fhe_ckks_add(self._h, _ptr(a), _ptr(b), _ptr(out), size, chain_index, _stream(stream)))
+
+    def bsgs_scratch_bytes(self, G):
+        return int(lib.fhe_bsgs_scratch_bytes(self._h, G))
+
+    def bsgs_matvec(self, ws, scratch, ct, chain_index, diags, D, G, B, galois_keys, out, hoisted=True,
+                    stream=None):
+        """out <- Rescale(sum_g rot_{gG}(sum_b rot_b(ct) * diags[gG + b]))."""
+        _check(lib.fhe_ckks_bsgs_matvec(self._h, ws._h, _ptr(scratch), _ptr(ct), chain_index, _ptr(diags), D, G, B,
+                                        self._gk_array(galois_keys), _ptr(out), int(bool(hoisted)),
+                                        _stream(stream)))
+
+    def encrypt_symmetric(self, pt, s_ntt, a, e, out, chain_index, stream=None):
+        _check(lib.fhe_ckks_encrypt_symmetric(self._h, _ptr(pt), _ptr(s_ntt), _ptr(a), _ptr(e), _ptr(out),
+                                              chain_index, _stream(stream)))
+
+    def decrypt(self, ct, s_ntt, pt, chain_index, stream=None):
+        _check(lib.fhe_ckks_decrypt(self._h, _ptr(ct), _ptr(s_ntt), _ptr(pt), chain_index, _stream(stream)))
+
+    def kswitch_keygen(self, ws, galois_elt, s_ntt, a, e, key, stream=None):
+        """galois_elt 0: relinearisation key (s^2); else the Galois key of that element."""
+        _check(lib.fhe_kswitch_keygen(self._h, ws._h, galois_elt, _ptr(s_ntt), _ptr(a), _ptr(e), _ptr(key),
+                                      _stream(stream)))
 
 
 class Workspace:
