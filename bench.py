@@ -122,7 +122,7 @@ def cpu_baseline_sample(mods, nq, threads):
     while True:
         oc.rescale(l, oc.ckks_mul_relin(l, a, b, key))
         reps += 1
-        if time.perf_counter() - t0 > 10.0 or reps >= 8:
+        if time.perf_counter() - t0 > 10.0 or reps >= 200:
             break
     dt = time.perf_counter() - t0
     return reps / dt, reps, dt
@@ -164,6 +164,83 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": "ops/s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "ops/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+MV_BITS = [60] + [40] * 19 + [60] * 4  # Q = 1x60 + 19x40, P = 4x60 (dnum = 5)
+MV_DIM, MV_G, MV_B, MV_BATCH = 128, 11, 12, 32
+
+
+def matvec_bench(pg, torch, timed, stream, rank, profile_only=False):
+    """128x128 plaintext matrix times encrypted vector by the diagonal method with baby-step /
+    giant-step rotations at N = 2^16 (Q = 1x60 + 19x40, P = 4x60, dnum = 5): 32 vectors at
+    levels drawn uniformly from 3..20, real keys from seeded randomness, matrix entries uniform
+    in [-1, 1].  Hoisted form: baby steps 1..10 share one mod-up, giant steps by Horner's rule
+    with rotations by 11 only (11 Galois keys); the reference's loop (giant rotations by g*11,
+    21 keys) runs beside it.  Slot error of the decrypted results against an FP64 matmul."""
+    from phantom_gb300.ckks import CkksEncoder, SecretKey
+    n, d, G, B = N, MV_DIM, MV_G, MV_B
+    mods = pg.create_coeff_modulus(n, MV_BITS)
+    nq = 20
+    hsteps = list(range(1, G + 1))
+    xsteps = list(range(1, G)) + [g * G for g in range(1, B)]
+    ctx = pg.Context(n, mods, 4, galois_elts=sorted({pg.elt_from_step(s, n) for s in hsteps + xsteps}))
+    ws = ctx.workspace()
+    rng = np.random.default_rng(5000 + rank)
+    sk = SecretKey(ctx, rng)
+    gks = sk.galois_keys(ws, sorted(set(hsteps + xsteps)))
+    enc = CkksEncoder(n)
+    S = n // 2
+    scale = 2.0 ** 40
+    M = rng.uniform(-1, 1, size=(d, d))
+    idx = np.arange(S)
+    diag_full = torch.stack([enc.encode(ctx, np.roll(M[idx % d, (idx + k) % d], (k // G) * G), scale, 1)
+                             for k in range(d)])
+    levels = [int(x) for x in rng.integers(3, 21, size=MV_BATCH)]
+    diags_at = {}
+    for lv in sorted(set(levels)):
+        diags_at[lv] = diag_full[:, :lv].contiguous()
+    del diag_full
+    xs, cts, outs = [], [], []
+    for lv in levels:
+        x = rng.uniform(-1, 1, size=d) + 1j * rng.uniform(-1, 1, size=d)
+        x /= np.maximum(1, np.abs(x))
+        chain = nq - lv + 1
+        xs.append(x)
+        cts.append((sk.encrypt(enc.encode(ctx, np.tile(x, S // d), scale, chain), chain), chain, lv))
+        outs.append(torch.empty((2, lv - 1, n), dtype=torch.int64, device="cuda"))
+    scratch = torch.empty(ctx.bsgs_scratch_bytes(G) // 8, dtype=torch.int64, device="cuda")
+
+    def batch(hoisted):
+        for (ct, chain, lv), o in zip(cts, outs):
+            ctx.bsgs_matvec(ws, scratch, ct, chain, diags_at[lv], d, G, B, gks, o, hoisted=hoisted, stream=stream)
+
+    batch(True)
+    if profile_only:
+        batch(True)
+        torch.cuda.synchronize()
+        return {}
+    torch.cuda.synchronize()
+    l0 = pg.lib.fhe_kernel_launches()
+    k = 3
+    t_h = timed(lambda i: batch(True), k) / k
+    launches = (pg.lib.fhe_kernel_launches() - l0) / k
+    errs = []
+    for (ct, chain, lv), o, x in zip(cts, outs, xs):
+        y = enc.decode(ctx, sk.decrypt(o, chain + 1), scale * scale / mods[lv - 1], chain + 1)
+        errs.append(float(np.max(np.abs(y - np.tile(M @ x, S // d)))))
+    err_h = max(errs)
+    batch(False)
+    t_x = timed(lambda i: batch(False), k) / k
+    errs = []
+    for (ct, chain, lv), o, x in zip(cts, outs, xs):
+        y = enc.decode(ctx, sk.decrypt(o, chain + 1), scale * scale / mods[lv - 1], chain + 1)
+        errs.append(float(np.max(np.abs(y - np.tile(M @ x, S // d)))))
+    return {"matvec128_batch32_uneven_hoisted_per_s": MV_BATCH / t_h,
+            "matvec128_batch32_uneven_reference_loop_per_s": MV_BATCH / t_x,
+            "matvec128_hoisted_max_slot_error": err_h,
+            "matvec128_reference_loop_max_slot_error": max(errs),
+            "matvec128_hoisted_launches_per_batch": launches,
+            "matvec128_levels": levels}
 
 
 def run_ours(args):
@@ -228,6 +305,9 @@ def run_ours(args):
         for _ in range(args.warmup + args.steps):
             ctx.ntt_forward(big, 8, len(mods), 0, stream)
         torch.cuda.synchronize()
+        return
+    if args.case == "matvec":  # profiling case: one batch of 32 hoisted matrix-vector products
+        matvec_bench(pg, torch, timed, stream, rank, profile_only=True)
         return
     for i in range(max(args.warmup, 3)):
         step(i)
@@ -318,6 +398,8 @@ def run_ours(args):
     t_bloop = timed(lambda i: [bctx.multiply_and_relin(bws, x, y, 1, bkey, stream) for x, y in bpairs], 3) / 3
     del g, bpairs, bct, bws, bctx
 
+    mv = matvec_bench(pg, torch, timed, stream, rank)
+
     # end to end through the C ABI with host buffers: H2D of both inputs, D2H of the result
     pin_a = [torch.empty((2, l, N), dtype=torch.int64).pin_memory() for _ in range(PAIRS)]
     pin_b = [torch.empty((2, l, N), dtype=torch.int64).pin_memory() for _ in range(PAIRS)]
@@ -368,7 +450,7 @@ def run_ours(args):
                       "ntt_forward_ms_64x35": 1000 * t_ntt,
                       "hmult_relin_rescale_algorithmic_bytes": 313524224,
                       "hmult_hbm_frac": 313524224 * value / world / 1e9 / peak,
-                      "launches_per_step": launches / args.steps}}
+                      "launches_per_step": launches / args.steps, **mv}}
     if rank == 0 and world == 1:
         v, reps, dt = cpu_baseline_sample(mods, nq, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": v, "unit": "ops/s", "cores": os.cpu_count() or 1, "kind": "port",
@@ -385,7 +467,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--case", choices=["full", "hmult", "ntt", "bfv"], default="full",
+    ap.add_argument("--case", choices=["full", "hmult", "ntt", "bfv", "matvec"], default="full",
                     help="hmult / ntt: run only that part (for profiler captures), print nothing")
     args = ap.parse_args()
     if args.impl == "reference":
