@@ -337,6 +337,13 @@ def run_ours(args):
     c2 = pg.to_device(random_residues(rng, mods[:l], N, 1)[0])
     t_rot = timed(lambda i: ctx.rotate(ws, ct, CHAIN, 1, gks, stream), k2)
     t_ks = timed(lambda i: ctx.keyswitch(ws, ct, c2, CHAIN, key, stream), k2)
+    # the same operations with the base conversions on the CUDA cores instead of the tensor cores
+    tc_default = ctx.tensor_cores
+    ctx.tensor_cores = False
+    t_hm_cc = timed(step, k2)
+    t_ks_cc = timed(lambda i: ctx.keyswitch(ws, ct, c2, CHAIN, key, stream), k2)
+    ctx.tensor_cores = tc_default
+    tc_status = ctx.device_status()
     # NTT throughput: 64 polynomials x 35 limbs (1.17 GB > 4x L2), forward transform
     polys, limbs = 64, len(mods)
     big = torch.randint(0, 1 << 40, (polys, limbs, N), dtype=torch.int64, device="cuda")
@@ -447,6 +454,9 @@ def run_ours(args):
                       "batch64_uneven_levels_ops_per_s": 64 * world / t_batch,
                       "batch64_as_single_calls_ops_per_s": 64 * world / t_loop,
                       "hrotate_step1_per_s": k2 * world / t_rot, "keyswitch_per_s": k2 * world / t_ks,
+                      "tensor_core_bconv": tc_default, "tensor_core_status": tc_status,
+                      "hmult_relin_rescale_cuda_core_bconv_ops_per_s": k2 * world / t_hm_cc,
+                      "keyswitch_cuda_core_bconv_per_s": k2 * world / t_ks_cc,
                       "ntt_forward_ms_64x35": 1000 * t_ntt,
                       "hmult_relin_rescale_algorithmic_bytes": 313524224,
                       "hmult_hbm_frac": 313524224 * value / world / 1e9 / peak,

@@ -78,6 +78,19 @@ uint32_t fhe_galois_elt_from_step(int step, uint64_t poly_modulus_degree);
 int fhe_context_create(const fhe_params *params, fhe_context **out);
 void fhe_context_destroy(fhe_context *ctx);
 
+/* Base conversions of the key switch on the tensor cores (exact bf16 byte-plane GEMMs,
+ * tcgen05) or on the CUDA cores (64-bit multiply-accumulate).  Both give the same words; the
+ * tensor-core form is the default wherever it applies (1 <= special_modulus_size <= 6 and at
+ * most 32 output limbs per digit).  No counterpart in the reference, whose conversions are
+ * CUDA-core kernels (src/rns_bconv.cu:455-485). */
+int fhe_context_set_tensor_cores(fhe_context *ctx, int enable);
+int fhe_context_tensor_cores(const fhe_context *ctx);
+
+/* Reads and clears the context's device status word (synchronises the device).  Non-zero
+ * means a bounded wait inside a tensor-core kernel gave up and that call's output is invalid.
+ * No counterpart in the reference. */
+int fhe_context_status(const fhe_context *ctx, unsigned *out);
+
 /* Sizes of a context: N, |Q|, |P|, |R| (BFV HPS base, else 0), dnum = ceil(|Q|/|P|). */
 int fhe_context_sizes(const fhe_context *ctx, uint64_t *n, size_t *size_q, size_t *size_p, size_t *size_r,
                       size_t *dnum);

@@ -103,6 +103,34 @@ int fhe_context_sizes(const fhe_context *ctx, uint64_t *n, size_t *size_q, size_
     }, false);
 }
 
+int fhe_context_set_tensor_cores(fhe_context *ctx, int enable) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        if (enable && !c.tc_avail)
+            throw std::invalid_argument("tensor-core base conversion needs 1 <= special_modulus_size <= 6");
+        c.tc_on = enable != 0;
+    }, false);
+}
+
+int fhe_context_tensor_cores(const fhe_context *ctx) {
+    if (!ctx || !ctx->c) return 0;
+    return ctx->c->tc_on ? 1 : 0;
+}
+
+int fhe_context_status(const fhe_context *ctx, unsigned *out) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        need_ptr(out, "out");
+        unsigned v = 0;
+        if (cudaMemcpy(&v, c.d_status.p, sizeof(v), cudaMemcpyDeviceToHost) != cudaSuccess)
+            throw std::runtime_error("reading the device status word failed");
+        const unsigned zero = 0;
+        if (cudaMemcpy(c.d_status.p, &zero, sizeof(zero), cudaMemcpyHostToDevice) != cudaSuccess)
+            throw std::runtime_error("clearing the device status word failed");
+        *out = v;
+    }, false);
+}
+
 int fhe_context_moduli(const fhe_context *ctx, uint64_t *out) {
     return guarded([&] {
         const pfg::Context &c = ctx_of(ctx);

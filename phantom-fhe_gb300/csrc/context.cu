@@ -1,4 +1,6 @@
 // context.cu — builds and uploads the device tables (see context.cuh).
+#include <cmath>
+#include <cstring>
 #include <stdexcept>
 #include <string>
 
@@ -27,6 +29,22 @@ void DevBuf::upload(const void *src, size_t n) {
 template <class T>
 static void up(DevBuf &b, const std::vector<T> &v) {
     b.upload(v.data(), v.size() * sizeof(T));
+}
+
+// bf16 bit pattern of an integer below 256 (exact: at most 8 significant bits)
+static uint16_t bf16_of_byte(unsigned v) {
+    const float f = (float)v;
+    uint32_t bits;
+    std::memcpy(&bits, &f, 4);
+    return (uint16_t)(bits >> 16);
+}
+
+// element (row, k) of a K-major, no-swizzle tensor-core operand with kpad columns:
+// 8-row x 16-byte core matrices, K neighbours 128 B apart, 8-row blocks kpad / 8 x 128 B apart
+static size_t canon_index(int row, int k, int kpad) {
+    const size_t byte = (size_t)(row & 7) * 16 + (size_t)(row >> 3) * (kpad / 8) * 128 + (size_t)(k & 7) * 2 +
+                        (size_t)(k >> 3) * 128;
+    return byte / 2;
 }
 
 const uint32_t *Context::perm_table(uint32_t elt) {
@@ -67,6 +85,17 @@ std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, cons
     c->t = plain_modulus;
     c->mods = coeff_modulus;
     const int nQ = c->nQ, nP = c->nP;
+    int dev = 0;
+    check(cudaGetDevice(&dev), "cudaGetDevice");
+    check(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev), "multiprocessor count");
+    {
+        const unsigned zero = 0;
+        c->d_status.upload(&zero, sizeof(zero));
+    }
+    // the byte-plane GEMM is exact for K = 8 alpha <= 48 (every plane sum stays below 2^22)
+    c->tc_avail = nP >= 1 && nP <= 6;
+    c->tc_on = c->tc_avail;
+    c->tc_kpad = (8 * nP + 15) / 16 * 16;
     std::vector<uint64_t> Q(coeff_modulus.begin(), coeff_modulus.begin() + nQ);
     std::vector<uint64_t> P(coeff_modulus.begin() + nQ, coeff_modulus.end());
 
@@ -140,6 +169,43 @@ std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, cons
             }
             up(lt->part_hat_inv, phi);
             up(lt->modup_mat, mat);
+            if (c->tc_avail && l + alpha - (l - (beta - 1) * alpha) <= 32) {
+                // byte planes of M'_(i,a) = 2^(8a) M_d[jj][i] mod p_jj, rows (output o, plane b)
+                const int kp = c->tc_kpad;
+                std::vector<uint16_t> bm((size_t)beta * 256 * kp, 0);
+                std::vector<TcOutMeta> meta((size_t)beta * 32);
+                std::vector<int> nn(beta, 0);
+                for (int d = 0; d < beta; d++) {
+                    const int s = d * alpha, sz = std::min(alpha, l - s);
+                    // output positions: limbs below 2^40 first (5 byte planes), then the others (8)
+                    std::vector<int> pos;
+                    for (int pass = 0; pass < 2; pass++)
+                        for (int jj = 0; jj < l + alpha; jj++) {
+                            if (jj >= s && jj < s + sz) continue;
+                            const bool narrow = c->mods[c->qlp_table(l, jj)] < (1ull << 40);
+                            if (narrow == (pass == 0)) pos.push_back(jj);
+                            if (narrow && pass == 0) nn[d]++;
+                        }
+                    for (int o = 0; o < (int)pos.size(); o++) {
+                        const int jj = pos[o];
+                        const uint64_t p = c->mods[c->qlp_table(l, jj)];
+                        meta[(size_t)d * 32 + o] = TcOutMeta{(uint32_t)jj, (float)(1.0 / (double)p)};
+                        for (int i = 0; i < sz; i++) {
+                            uint64_t mp = mat[((size_t)d * (l + alpha) + jj) * alpha + i];
+                            for (int a = 0; a < 8; a++) {
+                                for (int b = 0; b < 8; b++)
+                                    bm[(size_t)d * 256 * kp + canon_index(o * 8 + b, i * 8 + a, kp)] =
+                                            bf16_of_byte((unsigned)(mp >> (8 * b)) & 0xFF);
+                                mp = mulmod(mp, 256 % p, p);
+                            }
+                        }
+                    }
+                }
+                up(lt->tc_modup, bm);
+                up(lt->tc_modup_meta, meta);
+                up(lt->tc_modup_nn, nn);
+                lt->tc_ok = true;
+            }
         }
         if (l > 1) {
             std::vector<uint64_t> iq(2 * (l - 1));

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "ntt.cuh"
+#include "tc.cuh"
 
 namespace pfg {
 
@@ -48,6 +49,13 @@ struct LevelTables {
     DevBuf modup_mat;
     // q_last^-1 mod q_j (value, Shoup), j < l - 1
     DevBuf inv_qlast;  // [l-1][2]
+    // tensor-core mod-up: per digit, the byte planes of 2^(8a) M_d[jj][i] mod p_jj as a bf16
+    // operand [256 rows = (output, plane)][kpad = (input limb, byte)] in the canonical K-major
+    // layout (see tc.cuh); tc_ok when every digit has at most 32 outputs
+    DevBuf tc_modup;
+    DevBuf tc_modup_meta;  // [beta][32 positions]: output limb jj and 1/p_jj (f32), limbs below 2^40 first
+    DevBuf tc_modup_nn;    // [beta]: number of positions below 2^40
+    bool tc_ok = false;
 };
 
 struct Context {
@@ -73,6 +81,11 @@ struct Context {
     std::vector<uint32_t> galois_elts;
     std::map<uint32_t, std::unique_ptr<DevBuf>> perms;
     std::mutex perm_mu;
+    // tensor-core base conversions: available (alpha <= 6) and switched on
+    bool tc_avail = false, tc_on = false;
+    int tc_kpad = 0;  // K of the byte-plane GEMM: 8 alpha rounded up to 16
+    int num_sms = 0;
+    DevBuf d_status;  // device error word (bounded waits that gave up), read by fhe_context_status
 
     int l1() const { return log_n / 2; }
     int l2() const { return log_n - log_n / 2; }

@@ -24,6 +24,7 @@
 #include <stdexcept>
 
 #include "bconv.cuh"
+#include "bconv_tc.cuh"
 #include "keyswitch.cuh"
 #include "launch.cuh"
 #include "ops.hpp"
@@ -185,6 +186,27 @@ static KsBuffers ks_buffers(const Context &c, const Workspace &w) {
 // Steps 1-2: y = iNTT(c2) * partQlHatInv; tm = NTT(bconv(y)) for every digit.
 static unsigned bconv_blocks(const Context &c) { return (unsigned)std::max<uint64_t>(1, c.n / 2 / 256); }
 
+// tensor-core mod-up conversion of every digit: two persistent CTAs per SM
+void modup_bconv_tc_launch(const Context &c, const LevelTables &lt, uint64_t *tm, const uint64_t *y, int l,
+                           cudaStream_t s) {
+    const int beta = lt.beta;
+    const int per_digit = std::max(1, c.num_sms / beta);  // one wave: one resident CTA per SM
+    const dim3 g((unsigned)std::min(per_digit, 1 << (c.log_n - 7)), beta);
+    with_tc_ksteps(c.tc_kpad, [&]<int KS>() {
+        static bool attr = [] {
+            cudaFuncSetAttribute(modup_bconv_tc<KS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc::kPipeSmemBytes);
+            return true;
+        }();
+        (void)attr;
+        count_launch();
+        modup_bconv_tc<KS><<<g, tc::kPipeThreads, tc::kPipeSmemBytes, s>>>(
+                tm, y, lt.tc_modup.as<uint16_t>(), lt.tc_modup_meta.as<TcOutMeta>(), lt.tc_modup_nn.as<int>(),
+                c.d_mods.as<Mod>(),
+                c.d_status.as<unsigned>(), c.log_n, l, c.nQ, c.nP);
+    });
+}
+
 template <class C2Load>
 static void modup_ckks(const Context &c, const KsBuffers &b, C2Load c2ld, int l, cudaStream_t s) {
     const LevelTables &lt = *c.levels[l];
@@ -194,12 +216,16 @@ static void modup_ckks(const Context &c, const KsBuffers &b, C2Load c2ld, int l,
     ntt_inv(c, l, SeqMap{l, 0}, c2ld, ys,
             ScaleStore{b.y, yps, c.log_n, 0, lt.part_hat_inv.as<uint64_t>(), c.d_mods.as<Mod>()}, s);
     const long long tps = (long long)qlp << c.log_n;
-    dim3 g(bconv_blocks(c), beta);
-    with_digit_bound(alpha, [&]<int A>() {
-        count_launch();
-        modup_bconv<A, false><<<g, 256, 0, s>>>(b.tm, b.y, nullptr, lt.modup_mat.as<uint64_t>(), c.d_mods.as<Mod>(),
-                                                 c.log_n, l, c.nQ, alpha);
-    });
+    if (c.tc_on && lt.tc_ok) {
+        modup_bconv_tc_launch(c, lt, b.tm, b.y, l, s);
+    } else {
+        dim3 g(bconv_blocks(c), beta);
+        with_digit_bound(alpha, [&]<int A>() {
+            count_launch();
+            modup_bconv<A, false><<<g, 256, 0, s>>>(b.tm, b.y, nullptr, lt.modup_mat.as<uint64_t>(),
+                                                     c.d_mods.as<Mod>(), c.log_n, l, c.nQ, alpha);
+        });
+    }
     PtrStore ts{b.tm, tps, c.log_n};
     ntt_fwd(c, beta * qlp, ModupMap{qlp, l, c.nQ, alpha, true}, PtrLoad{b.tm, tps, c.log_n}, ts, ts, s);
 }

@@ -53,6 +53,9 @@ def _load():
     L.fhe_create_coeff_modulus.argtypes = [_u64, ctypes.POINTER(ctypes.c_int), _sz, ctypes.POINTER(_u64)]
     L.fhe_context_create.argtypes = [ctypes.POINTER(_Params), ctypes.POINTER(_vp)]
     L.fhe_context_destroy.argtypes = [_vp]
+    L.fhe_context_set_tensor_cores.argtypes = [_vp, ctypes.c_int]
+    L.fhe_context_tensor_cores.argtypes = [_vp]
+    L.fhe_context_status.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint)]
     L.fhe_context_sizes.argtypes = [_vp] + [ctypes.POINTER(_u64)] + [ctypes.POINTER(_sz)] * 4
     L.fhe_context_moduli.argtypes = [_vp, ctypes.POINTER(_u64)]
     L.fhe_context_galois_elts.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(_sz)]
@@ -174,6 +177,21 @@ class Context:
         if getattr(self, "_h", None):
             lib.fhe_context_destroy(self._h)
             self._h = None
+
+    @property
+    def tensor_cores(self):
+        """Whether the key switch's base conversions run on the tensor cores."""
+        return bool(lib.fhe_context_tensor_cores(self._h))
+
+    @tensor_cores.setter
+    def tensor_cores(self, on):
+        _check(lib.fhe_context_set_tensor_cores(self._h, int(bool(on))))
+
+    def device_status(self):
+        """Reads and clears the device status word (0 = every bounded wait completed)."""
+        v = ctypes.c_uint()
+        _check(lib.fhe_context_status(self._h, ctypes.byref(v)))
+        return int(v.value)
 
     def level(self, chain_index):
         return self.size_q - (chain_index - 1)

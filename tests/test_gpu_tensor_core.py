@@ -1,0 +1,89 @@
+"""Tensor-core (tcgen05, exact bf16 byte-plane GEMM) base conversions against the oracle and
+against the CUDA-core form, word for word, over digit sizes 1..6, 40- and 60-bit primes (both
+epilogue paths), partial last digits and every level of a chain."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+from oracle import oracle as O  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import phantom_gb300
+    return phantom_gb300
+
+
+def _eq(got_t, want, what):
+    got = got_t.cpu().numpy().view(np.uint64)
+    want = np.asarray(want, dtype=np.uint64).reshape(got.shape)
+    bad = int((got != want).sum())
+    assert bad == 0, f"{what}: {bad} of {got.size} words differ"
+
+
+PARAMS = {
+    # name: (N, bit sizes, special primes, chain indices to test)
+    "a1": (4096, [60, 40, 40, 40, 60], 1, [1, 3]),
+    "a2_partial": (4096, [60, 40, 40, 40, 40, 60, 60], 2, [1, 2, 4]),
+    "a3_all60": (8192, [60] * 7 + [60] * 3, 3, [1, 2, 5]),
+    "a5_n16_l30": (65536, [60] + [40] * 29 + [60] * 5, 5, [1, 2, 13]),
+    "a4_n16_l20": (65536, [60] + [40] * 19 + [60] * 4, 4, [1, 6, 17]),
+    "a6": (4096, [60] + [50] * 11 + [60] * 6, 6, [1, 4]),
+}
+
+
+@pytest.mark.parametrize("name", list(PARAMS))
+def test_keyswitch_tensor_core_matches_oracle_and_cuda_core(pg, name):
+    n, bits, special, chains = PARAMS[name]
+    mods = pg.create_coeff_modulus(n, bits)
+    nq = len(bits) - special
+    ctx = pg.Context(n, mods, special)
+    assert ctx.tensor_cores, "tensor-core conversions are the default for special_modulus_size <= 6"
+    oc = O.Context(n.bit_length() - 1, mods, nq, special)
+    ws = ctx.workspace()
+    rng = np.random.default_rng(len(bits) * 7 + special)
+    key = O.random_residues(rng, mods, n, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), n)
+    k = pg.KeySwitchKey(pg.to_device(key))
+    for chain in chains:
+        l = ctx.level(chain)
+        ct = O.random_residues(rng, mods[:l], n, 2)
+        c2 = O.random_residues(rng, mods[:l], n, 1)[0]
+        want = oc.keyswitch(l, ct, c2, key)
+        for tc in (True, False):
+            ctx.tensor_cores = tc
+            t = pg.to_device(ct)
+            ctx.keyswitch(ws, t, pg.to_device(c2), chain, k)
+            _eq(t, want, f"{name} chain {chain} tensor_cores={tc}")
+        assert ctx.device_status() == 0
+        ctx.tensor_cores = True
+
+
+def test_fused_hmult_rescale_tensor_core(pg):
+    n = 65536
+    bits = [60] + [40] * 29 + [60] * 5
+    mods = pg.create_coeff_modulus(n, bits)
+    ctx = pg.Context(n, mods, 5)
+    oc = O.Context(16, mods, 30, 5)
+    ws = ctx.workspace()
+    rng = np.random.default_rng(99)
+    key = O.random_residues(rng, mods, n, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), n)
+    k = pg.KeySwitchKey(pg.to_device(key))
+    l = 30
+    a = O.random_residues(rng, mods[:l], n, 2)
+    b = O.random_residues(rng, mods[:l], n, 2)
+    out = torch.empty((2, l - 1, n), dtype=torch.int64, device="cuda")
+    ctx.multiply_relin_rescale(ws, pg.to_device(a), pg.to_device(b), out, 1, k)
+    _eq(out, oc.rescale(l, oc.ckks_mul_relin(l, a, b, key)), "HMult+relin+rescale (tensor cores)")
+    assert ctx.device_status() == 0
+
+
+def test_tensor_cores_unavailable_for_wide_digits(pg):
+    n = 4096
+    mods = pg.create_coeff_modulus(n, [60, 40, 40, 40] + [60] * 7)
+    ctx = pg.Context(n, mods, 7)
+    assert not ctx.tensor_cores
+    with pytest.raises(pg.InvalidArgument):
+        ctx.tensor_cores = True
