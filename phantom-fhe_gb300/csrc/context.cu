@@ -127,9 +127,10 @@ std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, cons
     up(c->d_itw, all_itw);
     up(c->d_ninv, ninv);
 
+    std::vector<uint64_t> pmat((size_t)nQ * nP), pinv(2 * nQ);
     if (nP > 0) {
         // mod-down constants (rns.cu:107-124, BaseConverter(P -> Ql), host/rns.cu:438-498)
-        std::vector<uint64_t> phi(2 * nP), pmat((size_t)nQ * nP), pinv(2 * nQ);
+        std::vector<uint64_t> phi(2 * nP);
         for (int k = 0; k < nP; k++) {
             phi[2 * k] = invmod(prod_mod(P, k, P[k]), P[k]);
             phi[2 * k + 1] = shoup(phi[2 * k], P[k]);
@@ -205,6 +206,51 @@ std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, cons
                 up(lt->tc_modup_meta, meta);
                 up(lt->tc_modup_nn, nn);
                 lt->tc_ok = true;
+            }
+        }
+        if (nP > 0 && c->tc_avail && l <= 32) {
+            // tensor-core P -> Ql conversions: positions = j < l, limbs below 2^40 first; for the
+            // fused rescale the constants carry P^-1 mod q_j and j = l - 1 takes the last position
+            const int kp = c->tc_kpad;
+            auto build = [&](bool rescale, DevBuf &bbuf, DevBuf &mbuf, int &nn) {
+                std::vector<int> pos;
+                const int nlim = rescale ? l - 1 : l;
+                nn = 0;
+                for (int pass = 0; pass < 2; pass++)
+                    for (int j = 0; j < nlim; j++) {
+                        const bool narrow = Q[j] < (1ull << 40);
+                        if (narrow == (pass == 0)) pos.push_back(j);
+                        if (narrow && pass == 0) nn++;
+                    }
+                if (rescale) pos.push_back(l - 1);
+                std::vector<uint16_t> bm((size_t)256 * kp, 0);
+                std::vector<TcOutMeta> meta(32);
+                for (int o = 0; o < (int)pos.size(); o++) {
+                    const int j = pos[o];
+                    const uint64_t q = Q[j];
+                    meta[o] = TcOutMeta{(uint32_t)j, (float)(1.0 / (double)q)};
+                    for (int k = 0; k < nP; k++) {
+                        uint64_t mp = pmat[(size_t)j * nP + k];
+                        if (rescale) mp = mulmod(mp, pinv[2 * j], q);
+                        for (int a = 0; a < 8; a++) {
+                            for (int b = 0; b < 8; b++)
+                                bm[canon_index(o * 8 + b, k * 8 + a, kp)] = bf16_of_byte((unsigned)(mp >> (8 * b)) & 0xFF);
+                            mp = mulmod(mp, 256 % q, q);
+                        }
+                    }
+                }
+                up(bbuf, bm);
+                up(mbuf, meta);
+            };
+            build(false, lt->tc_moddown, lt->tc_moddown_meta, lt->tc_moddown_nn);
+            lt->tc_moddown_ok = true;
+            if (l > 1) {
+                bool fits = true;  // z < q_(l-1) <= 2 q_j keeps delta_j P^-1 + z below 4 q_j
+                for (int j = 0; j < l - 1; j++) fits = fits && Q[l - 1] <= 2 * Q[j];
+                if (fits) {
+                    build(true, lt->tc_rescale, lt->tc_rescale_meta, lt->tc_rescale_nn);
+                    lt->tc_rescale_ok = true;
+                }
             }
         }
         if (l > 1) {

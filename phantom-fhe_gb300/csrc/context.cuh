@@ -56,6 +56,11 @@ struct LevelTables {
     DevBuf tc_modup_meta;  // [beta][32 positions]: output limb jj and 1/p_jj (f32), limbs below 2^40 first
     DevBuf tc_modup_nn;    // [beta]: number of positions below 2^40
     bool tc_ok = false;
+    // tensor-core P -> Ql conversions (mod-down; mod-down fused with the rescale), one operand
+    // [256][kpad] each, positions j < l (limbs below 2^40 first; rescale: j = l - 1 last)
+    DevBuf tc_moddown, tc_moddown_meta, tc_rescale, tc_rescale_meta;
+    int tc_moddown_nn = 0, tc_rescale_nn = 0;
+    bool tc_moddown_ok = false, tc_rescale_ok = false;
 };
 
 struct Context {

@@ -186,7 +186,30 @@ static KsBuffers ks_buffers(const Context &c, const Workspace &w) {
 // Steps 1-2: y = iNTT(c2) * partQlHatInv; tm = NTT(bconv(y)) for every digit.
 static unsigned bconv_blocks(const Context &c) { return (unsigned)std::max<uint64_t>(1, c.n / 2 / 256); }
 
-// tensor-core mod-up conversion of every digit: two persistent CTAs per SM
+// tensor-core P -> Ql conversion of both polynomials (one persistent CTA per SM)
+template <bool RESCALE>
+static void pq_bconv_tc_launch(const Context &c, const LevelTables &lt, uint64_t *out, long long ops,
+                               const uint64_t *cx, long long cps, int l, const uint64_t *zc, const uint64_t *zd,
+                               cudaStream_t s) {
+    const dim3 g((unsigned)std::max(1, std::min(c.num_sms / 2, 1 << (c.log_n - 7))), 2);
+    const DevBuf &bm = RESCALE ? lt.tc_rescale : lt.tc_moddown;
+    const DevBuf &meta = RESCALE ? lt.tc_rescale_meta : lt.tc_moddown_meta;
+    const int nn = RESCALE ? lt.tc_rescale_nn : lt.tc_moddown_nn;
+    with_tc_ksteps(c.tc_kpad, [&]<int KS>() {
+        static bool attr = [] {
+            cudaFuncSetAttribute(pq_bconv_tc<KS, RESCALE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc::kPipeSmemBytes);
+            return true;
+        }();
+        (void)attr;
+        count_launch();
+        pq_bconv_tc<KS, RESCALE><<<g, tc::kPipeThreads, tc::kPipeSmemBytes, s>>>(
+                out, ops, cx, cps, bm.as<uint16_t>(), meta.as<TcOutMeta>(), nn, c.d_mods.as<Mod>(),
+                c.d_status.as<unsigned>(), c.log_n, l, c.nP, zc, zd, c.p_inv.as<uint64_t>());
+    });
+}
+
+// tensor-core mod-up conversion of every digit: one persistent CTA per SM
 void modup_bconv_tc_launch(const Context &c, const LevelTables &lt, uint64_t *tm, const uint64_t *y, int l,
                            cudaStream_t s) {
     const int beta = lt.beta;
@@ -259,11 +282,16 @@ static void moddown_ntt(const Context &c, const KsBuffers &b, uint64_t *mid, int
     const int qlp = l + c.nP;
     const long long cps = (long long)qlp << c.log_n;
     const long long mps = (long long)l << c.log_n;
-    with_digit_bound(c.nP, [&]<int A>() {
-        count_launch();
-        moddown_bconv<A><<<dim3(bconv_blocks(c), 2), 256, 0, s>>>(mid, mps, b.cx, cps, c.p_mat.as<uint64_t>(),
-                                                                   c.d_mods.as<Mod>(), c.log_n, l, c.nP);
-    });
+    const LevelTables &lt = *c.levels[l];
+    if (c.tc_on && lt.tc_moddown_ok) {
+        pq_bconv_tc_launch<false>(c, lt, mid, mps, b.cx, cps, l, nullptr, nullptr, s);
+    } else {
+        with_digit_bound(c.nP, [&]<int A>() {
+            count_launch();
+            moddown_bconv<A><<<dim3(bconv_blocks(c), 2), 256, 0, s>>>(mid, mps, b.cx, cps, c.p_mat.as<uint64_t>(),
+                                                                       c.d_mods.as<Mod>(), c.log_n, l, c.nP);
+        });
+    }
     PtrStore ms{mid, mps, c.log_n};
     ModdownStore<Base> st{out0, out1, k0, b.cx, cps, c.p_inv.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, base};
     ntt_fwd(c, 2 * nl, QlpMap{nl, k0, l, c.nQ}, PtrLoad{mid, mps, c.log_n}, ms, st, s);
@@ -448,13 +476,17 @@ void ckks_mul_relin_rescale(const Context &c, const Workspace &w, const uint64_t
     PtrStore mid{b.tm, (long long)(alpha + 2) << c.log_n, c.log_n};
     ntt_inv(c, 2 * (alpha + 2), LastLimbMap{alpha, l, c.nQ}, LastLimbLoad{b.cx, cps, tb, mods, c.log_n, l, alpha},
             mid, LastLimbStore{b.cx, cps, zc, zd, c.p_hat_inv.as<uint64_t>(), mods, c.log_n, l, alpha}, s);
-    with_digit_bound(alpha, [&]<int A>() {
-        count_launch();
-        rescale_fused_bconv<A><<<dim3(bconv_blocks(c), 2), 256, 0, s>>>(b.tm, ops, b.cx, cps, zc, zd,
-                                                                         c.p_mat.as<uint64_t>(),
-                                                                         c.p_inv.as<uint64_t>(), mods, c.log_n, l,
-                                                                         c.nP);
-    });
+    if (c.tc_on && lt.tc_rescale_ok) {
+        pq_bconv_tc_launch<true>(c, lt, b.tm, ops, b.cx, cps, l, zc, zd, s);
+    } else {
+        with_digit_bound(alpha, [&]<int A>() {
+            count_launch();
+            rescale_fused_bconv<A><<<dim3(bconv_blocks(c), 2), 256, 0, s>>>(b.tm, ops, b.cx, cps, zc, zd,
+                                                                             c.p_mat.as<uint64_t>(),
+                                                                             c.p_inv.as<uint64_t>(), mods, c.log_n,
+                                                                             l, c.nP);
+        });
+    }
     PtrStore ms{b.tm, ops, c.log_n};
     PtrLoad ld{b.tm, ops, c.log_n};
     RescaleFusedStore st{out, ops, b.cx, cps, c.p_inv.as<uint64_t>(), lt.inv_qlast.as<uint64_t>(), mods, c.log_n,
