@@ -306,6 +306,19 @@ def run_ours(args):
             ctx.ntt_forward(big, 8, len(mods), 0, stream)
         torch.cuda.synchronize()
         return
+    if args.case == "batch":  # profiling case: batched HMult+relin+rescale, 64 at levels 5..30
+        brng = np.random.default_rng(2000 + rank)
+        levels = [int(x) for x in brng.integers(5, 31, size=64)]
+        items = []
+        for lv in levels:
+            ta = torch.randint(0, 1 << 40, (2, lv, N), dtype=torch.int64, device="cuda")
+            tb = torch.randint(0, 1 << 40, (2, lv, N), dtype=torch.int64, device="cuda")
+            items.append((ta, tb, torch.empty((2, lv - 1, N), dtype=torch.int64, device="cuda"), nq - lv + 1))
+        wsb = ctx.workspace(batch_items=64)
+        for _ in range(args.warmup + args.steps):
+            ctx.multiply_relin_rescale_batch(wsb, items, key, stream)
+        torch.cuda.synchronize()
+        return
     if args.case == "matvec":  # profiling case: one batch of 32 hoisted matrix-vector products
         matvec_bench(pg, torch, timed, stream, rank, profile_only=True)
         return
@@ -477,7 +490,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--case", choices=["full", "hmult", "ntt", "bfv", "matvec"], default="full",
+    ap.add_argument("--case", choices=["full", "hmult", "ntt", "bfv", "matvec", "batch"], default="full",
                     help="hmult / ntt: run only that part (for profiler captures), print nothing")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -1,24 +1,42 @@
-// bconv_tc.cuh — mod-up base conversion on the tensor cores (tcgen05), word-for-word equal to
-// modup_bconv (bconv.cuh) and to the reference's bconv_matmul_padded_unroll2_kernel
-// (src/rns_bconv.cu:455-485) fed by DRNSTool::modup (:530-628).
+// bconv_tc.cuh — RNS base conversions of the key switch on the tensor cores (tcgen05), word for
+// word equal to the CUDA-core kernels of bconv.cuh and to the reference's
+//   mod-up    bconv_matmul_padded_unroll2_kernel (src/rns_bconv.cu:455-485, DRNSTool::modup :530-628)
+//   mod-down  bConv_BEHZ (:212-229) in DRNSTool::moddown_from_NTT (:776-828)
+// through the byte-plane GEMM of tc.cuh.
 //
-// Per digit d (blockIdx.y) the conversion of its sz input limbs to the l + alpha - sz other QlP
-// limbs is the byte-plane GEMM of tc.cuh: A = [128 coefficients][8 alpha bytes] (filled from y,
-// one 16-byte core-matrix row per input residue), B = the digit's constant byte planes (built at
-// context creation, copied to shared memory once per CTA), D = [128][8 x outputs] f32 in tensor
-// memory.  CTAs are persistent over 128-coefficient tiles; 256 threads: all fill A, one issues
-// the MMAs, and each of the 8 warps reads its lane quarter of D for half of the outputs and
-// writes canonical residues to tm[d][jj][n] (coalesced 8-byte stores).
+// One kernel serves every form.  A "group" is one conversion with a fixed constant operand: a
+// digit of a mod-up, a polynomial of a mod-down, or either of one ciphertext of a batch.  A group
+// has sz input limbs (rows = coefficients) and npos output positions; the work is (group,
+// 128-row tile) units and each persistent CTA (one per SM, 512 threads) takes a contiguous range
+// of them, so it reloads a group's constant operand (double-buffered in shared memory) only at
+// group boundaries.  Iteration i of the tile pipeline fills tile i's A (loaded into registers
+// during the previous iteration), issues its MMAs into one of two 256-column accumulators, starts
+// the loads of tile i + 1 and runs tile i - 1's epilogue while the MMAs execute: one barrier per
+// tile.  Outputs are lazy residues in [0, 2p) ([0, 4p) with the rescale term), the input range
+// of the forward NTT that consumes every one of them.
 #pragma once
+#include <algorithm>
+
+#include "launch.cuh"
 #include "tc.cuh"
 
 namespace pfg {
 
-// The pipeline shared by the tensor-core conversions: one CTA per SM, 512 threads, two
-// accumulators (2 x 256 tensor-memory columns) and two A buffers.  Iteration i writes tile i's A
-// (loaded into registers during the previous iteration), issues tile i's MMAs, starts the loads
-// of tile i + 1 and runs tile i - 1's epilogue while the MMAs execute: one barrier per tile.
-// Only thread 0 waits on the MMA barrier (bounded); the others sleep in __syncthreads.
+// One conversion: inputs in + (i << log_n) (i < sz), outputs out + (jj << log_n) for the
+// positions of meta, constant operand bmat ([256][kpad], canonical layout), positions [0, nn)
+// with 5 byte planes and [nn, nlim) with 8.  Rescale groups (see pq forms below) carry zc, zd
+// (this polynomial's rows) and the level l.
+struct TcGroup {
+    const uint64_t *in;
+    uint64_t *out;
+    const uint16_t *bmat;
+    const TcOutMeta *meta;
+    const uint64_t *zc, *zd;
+    int sz, npos, nn, l;
+};
+
+// The tile pipeline; only thread 0 waits on the MMA barrier (bounded), the others sleep in
+// __syncthreads.  On a timeout every thread returns after the same barrier.
 template <class Load, class Fill, class Issue, class Epi>
 __device__ __forceinline__ void tc_pipeline(int cnt, uint64_t *bar, uint32_t *ok_flag, unsigned *status, Load &&load,
                                             Fill &&fill, Issue &&issue, Epi &&epilogue) {
@@ -48,24 +66,24 @@ __device__ __forceinline__ void tc_pipeline(int cnt, uint64_t *bar, uint32_t *ok
     }
 }
 
-// TMEM columns [col0, col0 + 8) of output positions [o, o1) -> dst[s_off[pos]] (lazy residues);
-// extra(pos) is added (rescale: z).
+// Output positions [o, o1) of one row: accumulator columns [8 pos, 8 pos + 8) -> dst[off[pos]],
+// plus extra(pos) (the rescale's z).
 template <int NPL, class Extra>
-__device__ __forceinline__ void tc_emit(uint32_t trow, uint64_t *dst, int o, int o1, const uint64_t *s_p,
-                                        const uint64_t *s_off, const float *s_inv, Extra extra) {
+__device__ __forceinline__ void tc_emit(uint32_t trow, uint64_t *dst, int o, int o1, const uint64_t *p,
+                                        const uint64_t *off, const float *inv, Extra extra) {
     for (; o + 1 < o1; o += 2) {
         uint32_t x0[8], x1[8];
         tc::ld8(trow + o * 8, x0);
         tc::ld8(trow + o * 8 + 8, x1);
         tc::wait_ld();
-        dst[s_off[o]] = tc::reduce_planes_lazy<NPL>(x0, s_p[o], s_inv[o]) + extra(o);
-        dst[s_off[o + 1]] = tc::reduce_planes_lazy<NPL>(x1, s_p[o + 1], s_inv[o + 1]) + extra(o + 1);
+        dst[off[o]] = tc::reduce_planes_lazy<NPL>(x0, p[o], inv[o]) + extra(o);
+        dst[off[o + 1]] = tc::reduce_planes_lazy<NPL>(x1, p[o + 1], inv[o + 1]) + extra(o + 1);
     }
     if (o < o1) {
         uint32_t x0[8];
         tc::ld8(trow + o * 8, x0);
         tc::wait_ld();
-        dst[s_off[o]] = tc::reduce_planes_lazy<NPL>(x0, s_p[o], s_inv[o]) + extra(o);
+        dst[off[o]] = tc::reduce_planes_lazy<NPL>(x0, p[o], inv[o]) + extra(o);
     }
 }
 
@@ -73,141 +91,33 @@ struct NoExtra {
     __device__ __forceinline__ uint64_t operator()(int) const { return 0; }
 };
 
-// Mod-up conversion of digit d = blockIdx.y (lazy outputs, consumed by the forward NTT).
-template <int KSTEPS>
+// RESCALE (HMult + relinearise + rescale, P -> Ql form): the constants carry P^-1 mod q_j, the
+// last position is j = l - 1 with e = delta_(l-1) P^-1, z = zd + zc P^-1 - e mod q_(l-1)
+// (canonical; one warp group computes it per row and shares it through shared memory), and the
+// other outputs are delta_j P^-1 + z (below 4 q_j because q_(l-1) <= 2 q_j, checked on the host).
+template <int KSTEPS, bool RESCALE, class Src>
 __global__ void __launch_bounds__(tc::kPipeThreads, 1)
-        modup_bconv_tc(uint64_t *tm, const uint64_t *y, const uint16_t *bmat, const TcOutMeta *meta,
-                       const int *nnarrow, const Mod *mods, unsigned *status, int log_n, int l, int nQ, int alpha) {
-    constexpr int KP = KSTEPS * 16;
-    constexpr uint32_t SBO = KP / 8 * 128;
-    constexpr int ABYTES = tc::kRows * KP * 2;
+        tc_bconv_kernel(Src src, int ngroups, const Mod *mods, const uint64_t *pinv, unsigned *status, int log_n) {
+    constexpr int KP = KSTEPS * 16, KC = KP / 8;
+    constexpr uint32_t SBO = KC * 128;
+    constexpr int ABYTES = tc::kRows * KP * 2, BBYTES = tc::kTmemCols * KP * 2;
+    constexpr int NSLOT = 3;  // per-tile metadata: slot i % 3 was last read two barriers before fill(i)
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *sA = smem;                   // 2 x 128 x KP bf16
-    uint8_t *sB = smem + 2 * ABYTES;      // 256 x KP bf16
+    uint8_t *sA = smem;               // 2 x 128 x KP bf16
+    uint8_t *sB = smem + 2 * ABYTES;  // 2 x 256 x KP bf16
     __shared__ uint32_t tmem_slot, ok_flag;
     __shared__ __align__(8) uint64_t bar[2];
-    __shared__ uint64_t s_p[tc::kMaxOut];       // output modulus, by output position
-    __shared__ uint64_t s_off[tc::kMaxOut];     // output limb offset in tm
-    __shared__ float s_inv[tc::kMaxOut];        // 1 / p as f32
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int d = blockIdx.y, qlp = l + alpha, s0 = d * alpha, sz = min(alpha, l - s0), nout = qlp - sz;
-    const int ncols = (nout * 8 + 15) & ~15;
-
-    const uint4 *src = reinterpret_cast<const uint4 *>(bmat + (size_t)d * tc::kTmemCols * KP);
-    for (int i = tid; i < ncols * KP * 2 / 16; i += tc::kPipeThreads) reinterpret_cast<uint4 *>(sB)[i] = src[i];
-    for (int i = tid; i < 2 * tc::kRows * (KP / 8); i += tc::kPipeThreads) {  // K columns past the digit stay zero
-        const int buf = i / (tc::kRows * (KP / 8)), rem = i % (tc::kRows * (KP / 8));
-        const int r = rem / (KP / 8), kc = rem % (KP / 8);
-        if (kc >= sz)
-            *reinterpret_cast<uint4 *>(sA + buf * ABYTES + (r & 7) * 16 + (r >> 3) * SBO + kc * 128) =
-                    make_uint4(0, 0, 0, 0);
-    }
-    if (tid < nout) {
-        const TcOutMeta m = meta[d * tc::kMaxOut + tid];
-        const int jj = (int)m.jj;
-        s_p[tid] = mods[jj < l ? jj : nQ + (jj - l)].q;
-        s_off[tid] = ((size_t)d * qlp + jj) << log_n;
-        s_inv[tid] = m.invp;
-    }
-    const int nn = nnarrow[d], nw = nout - nn;
-    if (warp == 0) tc::tmem_alloc(&tmem_slot, 2 * tc::kTmemCols);
-    if (tid == 0) {
-        tc::mbar_init(&bar[0], 1);
-        tc::mbar_init(&bar[1], 1);
-    }
-    tc::fence_before();
-    __syncthreads();
-    tc::fence_after();
-    const uint32_t tmem = tmem_slot;
-    const uint32_t idesc = tc::idesc_bf16(tc::kRows, ncols);
-    const int ntiles = 1 << (log_n - 7);
-    const int cnt = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-    const int r = tid & (tc::kRows - 1), lq = warp & 3, grp = warp >> 2;
-    // positions [0, nn) have 5 byte planes, [nn, nout) have 8; each warp group takes a quarter of each
-    const int a0 = grp * nn / 4, a1 = (grp + 1) * nn / 4;
-    const int b0 = nn + grp * nw / 4, b1 = nn + (grp + 1) * nw / 4;
-    // fill: thread -> (row r, limbs i0 and i0 + 4)
-    const int i0 = tid >> 7;
-    uint64_t ya = 0, yb = 0;
-    auto load = [&](int i) {
-        const size_t n0 = (size_t)((int)blockIdx.x + i * (int)gridDim.x) * tc::kRows;
-        if (i0 < sz) ya = y[((size_t)(s0 + i0) << log_n) + n0 + r];
-        if (i0 + 4 < sz) yb = y[((size_t)(s0 + i0 + 4) << log_n) + n0 + r];
-    };
-    auto fill = [&](int i) {
-        uint8_t *a = sA + (i & 1) * ABYTES + (r & 7) * 16 + (r >> 3) * SBO;
-        if (i0 < sz) *reinterpret_cast<uint4 *>(a + i0 * 128) = tc::bytes_bf16(ya);
-        if (i0 + 4 < sz) *reinterpret_cast<uint4 *>(a + (i0 + 4) * 128) = tc::bytes_bf16(yb);
-    };
-    auto issue = [&](int i) {
-        const uint32_t base = tc::saddr(sA + (i & 1) * ABYTES), bb = tc::saddr(sB);
-        tc::fence_after();
-#pragma unroll
-        for (int k = 0; k < KSTEPS; k++)
-            tc::mma_bf16(tmem + (i & 1) * tc::kTmemCols, tc::sdesc(base + k * 256, 128, SBO),
-                         tc::sdesc(bb + k * 256, 128, SBO), idesc, k > 0);
-        tc::commit(&bar[i & 1]);
-    };
-    auto epilogue = [&](int i) {
-        const uint32_t trow = tmem + (i & 1) * tc::kTmemCols + ((uint32_t)(lq * 32) << 16);
-        uint64_t *dst = tm + (size_t)((int)blockIdx.x + i * (int)gridDim.x) * tc::kRows + lq * 32 + lane;
-        tc_emit<5>(trow, dst, a0, a1, s_p, s_off, s_inv, NoExtra{});
-        tc_emit<8>(trow, dst, b0, b1, s_p, s_off, s_inv, NoExtra{});
-    };
-    tc_pipeline(cnt, bar, &ok_flag, status, load, fill, issue, epilogue);
-    __syncthreads();
-    if (warp == 0) {
-        tc::fence_after();
-        tc::tmem_free(tmem, 2 * tc::kTmemCols);
-    }
-}
-
-// P -> Ql conversion of polynomial t = blockIdx.y on the tensor cores.  Input: the nP P limbs
-// of cx[t] ([x_k PHatInv_k]_{p_k}, coefficient form).  Output positions (meta) cover j < l.
-//   !RESCALE (DRNSTool::moddown_from_NTT, src/rns_bconv.cu:776-828, bConv_BEHZ :212-229):
-//     out[t][j] = sum_k y_k (P/p_k) mod q_j (lazy), for the forward NTT of the mod-down.
-//   RESCALE (HMult + relinearise + rescale, see ckks_mul_relin_rescale): the constants carry
-//     P^-1 mod q_j, position l - 1 holds e = delta_(l-1) P^-1 and
-//     z = zd + zc P^-1 - e mod q_(l-1) (canonical; one warp group computes it per row and
-//     shares it through shared memory), then out[t][j] = delta_j P^-1 + z (j < l - 1, lazy:
-//     below 4 q_j because q_(l-1) <= 2 q_j, checked on the host).
-template <int KSTEPS, bool RESCALE>
-__global__ void __launch_bounds__(tc::kPipeThreads, 1)
-        pq_bconv_tc(uint64_t *out, long long ops, const uint64_t *cx, long long cps, const uint16_t *bmat,
-                    const TcOutMeta *meta, int nn, const Mod *mods, unsigned *status, int log_n, int l, int nP,
-                    const uint64_t *zc, const uint64_t *zd, const uint64_t *pinv) {
-    constexpr int KP = KSTEPS * 16;
-    constexpr uint32_t SBO = KP / 8 * 128;
-    constexpr int ABYTES = tc::kRows * KP * 2;
-    extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *sA = smem;
-    uint8_t *sB = smem + 2 * ABYTES;
-    __shared__ uint32_t tmem_slot, ok_flag;
-    __shared__ __align__(8) uint64_t bar[2];
-    __shared__ uint64_t s_p[tc::kMaxOut], s_off[tc::kMaxOut];
-    __shared__ float s_inv[tc::kMaxOut];
+    __shared__ uint64_t s_p[NSLOT][tc::kMaxOut], s_off[NSLOT][tc::kMaxOut];
+    __shared__ float s_inv[NSLOT][tc::kMaxOut];
+    __shared__ TcGroup s_grp[NSLOT];
+    __shared__ int s_bslot[NSLOT];
     __shared__ uint64_t s_z[tc::kRows];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int t = blockIdx.y, sz = nP, npos = l;
-    const int ncols = (npos * 8 + 15) & ~15;
-    const uint64_t *in = cx + t * cps + ((size_t)l << log_n);
-    uint64_t *dst_t = out + t * ops;
+    const int tiles = 1 << (log_n - 7);
+    const long long units = (long long)ngroups * tiles;
+    const long long u0 = units * blockIdx.x / gridDim.x, u1 = units * (blockIdx.x + 1) / gridDim.x;
+    const int cnt = (int)(u1 - u0);
 
-    const uint4 *src = reinterpret_cast<const uint4 *>(bmat);
-    for (int i = tid; i < ncols * KP * 2 / 16; i += tc::kPipeThreads) reinterpret_cast<uint4 *>(sB)[i] = src[i];
-    for (int i = tid; i < 2 * tc::kRows * (KP / 8); i += tc::kPipeThreads) {
-        const int buf = i / (tc::kRows * (KP / 8)), rem = i % (tc::kRows * (KP / 8));
-        const int r = rem / (KP / 8), kc = rem % (KP / 8);
-        if (kc >= sz)
-            *reinterpret_cast<uint4 *>(sA + buf * ABYTES + (r & 7) * 16 + (r >> 3) * SBO + kc * 128) =
-                    make_uint4(0, 0, 0, 0);
-    }
-    if (tid < npos) {
-        const TcOutMeta m = meta[tid];
-        s_p[tid] = mods[m.jj].q;
-        s_off[tid] = (size_t)m.jj << log_n;
-        s_inv[tid] = m.invp;
-    }
     if (warp == 0) tc::tmem_alloc(&tmem_slot, 2 * tc::kTmemCols);
     if (tid == 0) {
         tc::mbar_init(&bar[0], 1);
@@ -217,27 +127,63 @@ __global__ void __launch_bounds__(tc::kPipeThreads, 1)
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = tmem_slot;
-    const uint32_t idesc = tc::idesc_bf16(tc::kRows, ncols);
-    const int ntiles = 1 << (log_n - 7);
-    const int cnt = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-    const int r = tid & (tc::kRows - 1), lq = warp & 3, grp = warp >> 2;
-    const int nlim = RESCALE ? npos - 1 : npos, nw = nlim - nn;
-    const int a0 = grp * nn / 4, a1 = (grp + 1) * nn / 4;
-    const int b0 = nn + grp * nw / 4, b1 = nn + (grp + 1) * nw / 4;
-    const int i0 = tid >> 7;
+    const int r = tid & (tc::kRows - 1), lq = warp & 3, grp = warp >> 2, i0 = tid >> 7;
+
+    // every thread tracks the same group sequence
+    int cur_group = -1, bslot = 1, lg = -1;
+    int sg0 = -1, sg1 = -1, sg2 = -1;  // group whose metadata each slot holds (registers)
+    TcGroup g{}, lgrp{};
     uint64_t ya = 0, yb = 0;
+    const int tshift = log_n - 7;  // tiles per group is a power of two
+    auto group_of = [&](int i) { return (int)((u0 + i) >> tshift); };
+    auto tile_of = [&](int i) { return (int)((u0 + i) & (tiles - 1)); };
     auto load = [&](int i) {
-        const size_t n0 = (size_t)((int)blockIdx.x + i * (int)gridDim.x) * tc::kRows;
-        if (i0 < sz) ya = in[((size_t)i0 << log_n) + n0 + r];
-        if (i0 + 4 < sz) yb = in[((size_t)(i0 + 4) << log_n) + n0 + r];
+        const int gi = group_of(i);
+        if (gi != lg) {
+            lg = gi;
+            lgrp = src(gi);
+        }
+        const size_t n = (size_t)tile_of(i) * tc::kRows + r;
+        if (i0 < lgrp.sz) ya = lgrp.in[((size_t)i0 << log_n) + n];
+        if (i0 + 4 < lgrp.sz) yb = lgrp.in[((size_t)(i0 + 4) << log_n) + n];
     };
     auto fill = [&](int i) {
+        const int gi = group_of(i), sl = i % NSLOT;
+        if (gi != cur_group) {  // the group's constant operand goes to the other B slot
+            cur_group = gi;
+            g = src(gi);
+            bslot ^= 1;
+            const int ncols = (g.npos * 8 + 15) & ~15;
+            const uint4 *bs = reinterpret_cast<const uint4 *>(g.bmat);
+            uint4 *bd = reinterpret_cast<uint4 *>(sB + bslot * BBYTES);
+            for (int k = tid; k < ncols * KP * 2 / 16; k += tc::kPipeThreads) bd[k] = bs[k];
+        }
+        const int have = sl == 0 ? sg0 : (sl == 1 ? sg1 : sg2);
+        if (have != gi) {  // a slot keeps its metadata while its group does not change
+            if (sl == 0) sg0 = gi;
+            else if (sl == 1) sg1 = gi;
+            else sg2 = gi;
+            if (tid < g.npos) {
+                const TcOutMeta m = g.meta[tid];
+                s_p[sl][tid] = mods[m.tbl].q;
+                s_off[sl][tid] = (size_t)m.jj << log_n;
+                s_inv[sl][tid] = m.invp;
+            }
+            if (tid == 0) {
+                s_grp[sl] = g;
+                s_bslot[sl] = bslot;
+            }
+        }
         uint8_t *a = sA + (i & 1) * ABYTES + (r & 7) * 16 + (r >> 3) * SBO;
-        if (i0 < sz) *reinterpret_cast<uint4 *>(a + i0 * 128) = tc::bytes_bf16(ya);
-        if (i0 + 4 < sz) *reinterpret_cast<uint4 *>(a + (i0 + 4) * 128) = tc::bytes_bf16(yb);
+        if (i0 < KC) *reinterpret_cast<uint4 *>(a + i0 * 128) = i0 < g.sz ? tc::bytes_bf16(ya) : make_uint4(0, 0, 0, 0);
+        if (i0 + 4 < KC)
+            *reinterpret_cast<uint4 *>(a + (i0 + 4) * 128) =
+                    i0 + 4 < g.sz ? tc::bytes_bf16(yb) : make_uint4(0, 0, 0, 0);
     };
     auto issue = [&](int i) {
-        const uint32_t base = tc::saddr(sA + (i & 1) * ABYTES), bb = tc::saddr(sB);
+        const int sl = i % NSLOT;
+        const uint32_t idesc = tc::idesc_bf16(tc::kRows, (s_grp[sl].npos * 8 + 15) & ~15);
+        const uint32_t base = tc::saddr(sA + (i & 1) * ABYTES), bb = tc::saddr(sB + s_bslot[sl] * BBYTES);
         tc::fence_after();
 #pragma unroll
         for (int k = 0; k < KSTEPS; k++)
@@ -246,32 +192,36 @@ __global__ void __launch_bounds__(tc::kPipeThreads, 1)
         tc::commit(&bar[i & 1]);
     };
     auto epilogue = [&](int i) {
+        const int sl = i % NSLOT;
+        const TcGroup gg = s_grp[sl];
         const uint32_t trow = tmem + (i & 1) * tc::kTmemCols + ((uint32_t)(lq * 32) << 16);
-        const size_t n = (size_t)((int)blockIdx.x + i * (int)gridDim.x) * tc::kRows + lq * 32 + lane;
-        uint64_t *dst = dst_t + n;
+        const int row = lq * 32 + lane;
+        const size_t n = (size_t)tile_of(i) * tc::kRows + row;
+        uint64_t *dst = gg.out + n;
+        const int nlim = RESCALE ? gg.npos - 1 : gg.npos, nw = nlim - gg.nn;
+        const int a0 = grp * gg.nn / 4, a1 = (grp + 1) * gg.nn / 4;
+        const int b0 = gg.nn + grp * nw / 4, b1 = gg.nn + (grp + 1) * nw / 4;
         if constexpr (RESCALE) {
-            const int row = lq * 32 + lane;
             if (grp == 0) {
-                const int pl = npos - 1;
-                const uint64_t ql = s_p[pl];
+                const int pl = gg.npos - 1;
+                const uint64_t ql = s_p[sl][pl];
                 uint32_t x[8];
                 tc::ld8(trow + pl * 8, x);
                 tc::wait_ld();
-                uint64_t e = ql < (1ull << 40) ? tc::reduce_planes_lazy<5>(x, ql, s_inv[pl])
-                                               : tc::reduce_planes_lazy<8>(x, ql, s_inv[pl]);
+                uint64_t e = ql < (1ull << 40) ? tc::reduce_planes_lazy<5>(x, ql, s_inv[sl][pl])
+                                               : tc::reduce_planes_lazy<8>(x, ql, s_inv[sl][pl]);
                 e = csub(e, ql);
-                const size_t o = ((size_t)t << log_n) + n;
-                const uint64_t zcp = mul_shoup(zc[o], pinv[2 * (l - 1)], pinv[2 * (l - 1) + 1], ql);
-                s_z[row] = sub_mod(add_mod(zd[o], zcp, ql), e, ql);
+                const uint64_t zcp = mul_shoup(gg.zc[n], pinv[2 * (gg.l - 1)], pinv[2 * (gg.l - 1) + 1], ql);
+                s_z[row] = sub_mod(add_mod(gg.zd[n], zcp, ql), e, ql);
             }
             asm volatile("bar.sync %0, 128;" ::"r"(1 + lq) : "memory");  // the four warps of this lane quarter
             const uint64_t z = s_z[row];
             auto addz = [z](int) { return z; };
-            tc_emit<5>(trow, dst, a0, a1, s_p, s_off, s_inv, addz);
-            tc_emit<8>(trow, dst, b0, b1, s_p, s_off, s_inv, addz);
+            tc_emit<5>(trow, dst, a0, a1, s_p[sl], s_off[sl], s_inv[sl], addz);
+            tc_emit<8>(trow, dst, b0, b1, s_p[sl], s_off[sl], s_inv[sl], addz);
         } else {
-            tc_emit<5>(trow, dst, a0, a1, s_p, s_off, s_inv, NoExtra{});
-            tc_emit<8>(trow, dst, b0, b1, s_p, s_off, s_inv, NoExtra{});
+            tc_emit<5>(trow, dst, a0, a1, s_p[sl], s_off[sl], s_inv[sl], NoExtra{});
+            tc_emit<8>(trow, dst, b0, b1, s_p[sl], s_off[sl], s_inv[sl], NoExtra{});
         }
     };
     tc_pipeline(cnt, bar, &ok_flag, status, load, fill, issue, epilogue);
@@ -282,6 +232,38 @@ __global__ void __launch_bounds__(tc::kPipeThreads, 1)
     }
 }
 
+// Mod-up of one ciphertext: group = digit d.  y [l][N] -> tm [beta][l + alpha][N].
+struct ModupSrc {
+    const uint64_t *y;
+    uint64_t *tm;
+    const uint16_t *bmat;
+    const TcOutMeta *meta;
+    const int *nn;
+    int l, alpha, log_n, kpad;
+    __device__ __forceinline__ TcGroup operator()(int d) const {
+        const int s0 = d * alpha, sz = min(alpha, l - s0), qlp = l + alpha;
+        return TcGroup{y + ((size_t)s0 << log_n), tm + (((size_t)d * qlp) << log_n), bmat + (size_t)d * 256 * kpad,
+                       meta + d * tc::kMaxOut, nullptr, nullptr, sz, qlp - sz, nn[d], l};
+    }
+};
+
+// P -> Ql of one ciphertext: group = polynomial t.  Inputs: the P limbs of cx[t]; outputs out[t].
+struct PqSrc {
+    const uint64_t *cx;
+    long long cps;
+    uint64_t *out;
+    long long ops;
+    const uint16_t *bmat;
+    const TcOutMeta *meta;
+    const uint64_t *zc, *zd;  // rescale: [2][N] each
+    int nn, l, nP, log_n;
+    __device__ __forceinline__ TcGroup operator()(int t) const {
+        return TcGroup{cx + t * cps + ((size_t)l << log_n), out + t * ops, bmat, meta,
+                       zc ? zc + ((size_t)t << log_n) : nullptr, zd ? zd + ((size_t)t << log_n) : nullptr, nP, l, nn,
+                       l};
+    }
+};
+
 // KSTEPS = kpad / 16 in {1, 2, 3}
 template <class F>
 void with_tc_ksteps(int kpad, F &&f) {
@@ -290,6 +272,25 @@ void with_tc_ksteps(int kpad, F &&f) {
         case 2: f.template operator()<2>(); break;
         default: f.template operator()<3>(); break;
     }
+}
+
+// Launch over ngroups groups: one persistent CTA per SM (it owns all 512 tensor-memory columns).
+template <bool RESCALE, class Src>
+void tc_bconv_launch(int kpad, int num_sms, int log_n, const Src &src, int ngroups, const Mod *mods,
+                     const uint64_t *pinv, unsigned *status, cudaStream_t s) {
+    const long long units = (long long)ngroups << (log_n - 7);
+    const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>(num_sms, units));
+    with_tc_ksteps(kpad, [&]<int KS>() {
+        static bool attr = [] {
+            cudaFuncSetAttribute(tc_bconv_kernel<KS, RESCALE, Src>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc::kPipeSmemBytes);
+            return true;
+        }();
+        (void)attr;
+        count_launch();
+        tc_bconv_kernel<KS, RESCALE, Src><<<grid, tc::kPipeThreads, tc::kPipeSmemBytes, s>>>(src, ngroups, mods, pinv,
+                                                                                         status, log_n);
+    });
 }
 
 }  // namespace pfg

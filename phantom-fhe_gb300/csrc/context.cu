@@ -190,7 +190,7 @@ std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, cons
                     for (int o = 0; o < (int)pos.size(); o++) {
                         const int jj = pos[o];
                         const uint64_t p = c->mods[c->qlp_table(l, jj)];
-                        meta[(size_t)d * 32 + o] = TcOutMeta{(uint32_t)jj, (float)(1.0 / (double)p)};
+                        meta[(size_t)d * 32 + o] = TcOutMeta{(uint32_t)jj, (uint32_t)c->qlp_table(l, jj), (float)(1.0 / (double)p)};
                         for (int i = 0; i < sz; i++) {
                             uint64_t mp = mat[((size_t)d * (l + alpha) + jj) * alpha + i];
                             for (int a = 0; a < 8; a++) {
@@ -228,7 +228,7 @@ std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, cons
                 for (int o = 0; o < (int)pos.size(); o++) {
                     const int j = pos[o];
                     const uint64_t q = Q[j];
-                    meta[o] = TcOutMeta{(uint32_t)j, (float)(1.0 / (double)q)};
+                    meta[o] = TcOutMeta{(uint32_t)j, (uint32_t)j, (float)(1.0 / (double)q)};
                     for (int k = 0; k < nP; k++) {
                         uint64_t mp = pmat[(size_t)j * nP + k];
                         if (rescale) mp = mulmod(mp, pinv[2 * j], q);

@@ -11,6 +11,7 @@
 // arithmetic is exactly that of ckks_mul_relin_rescale (ops_ckks.cu), so every output equals the
 // single call's word for word.
 #include "bconv.cuh"
+#include "bconv_tc.cuh"
 #include "launch.cuh"
 #include "ops.hpp"
 
@@ -379,6 +380,46 @@ __global__ void __launch_bounds__(256) rescale_bconv_batch(BItemsRef r, Prefix p
     }
 }
 
+// ------------------------------------------------------------------ tensor-core group sources
+
+// Mod-up of a batch: group = (item, digit) through a prefix over digit counts.
+struct BatchModupSrc {
+    Prefix pre;
+    uint64_t *ws[kMaxBatch];
+    const uint16_t *bmat[kMaxBatch];
+    const TcOutMeta *meta[kMaxBatch];
+    const int *nn[kMaxBatch];
+    int l[kMaxBatch];
+    long long y_off, tm_off;
+    int alpha, log_n, kpad;
+    __device__ __forceinline__ TcGroup operator()(int gidx) const {
+        const int c = pre.find(gidx), d = gidx - pre.p[c], lc = l[c], qlp = lc + alpha;
+        const int s0 = d * alpha, sz = min(alpha, lc - s0);
+        return TcGroup{ws[c] + y_off + ((size_t)s0 << log_n), ws[c] + tm_off + (((size_t)d * qlp) << log_n),
+                       bmat[c] + (size_t)d * 256 * kpad, meta[c] + d * tc::kMaxOut, nullptr, nullptr, sz, qlp - sz,
+                       nn[c][d], lc};
+    }
+};
+
+// Step 6 of a batch (P -> Ql fused with the rescale): group = (item, polynomial).
+struct BatchRescaleSrc {
+    uint64_t *ws[kMaxBatch];
+    const uint16_t *bmat[kMaxBatch];
+    const TcOutMeta *meta[kMaxBatch];
+    int nn[kMaxBatch];
+    int l[kMaxBatch];
+    long long cx_off, tm_off, z_off;
+    int alpha, log_n;
+    __device__ __forceinline__ TcGroup operator()(int gidx) const {
+        const int c = gidx >> 1, t = gidx & 1, lc = l[c];
+        uint64_t *w = ws[c];
+        const long long qlp_n = (long long)(lc + alpha) << log_n;
+        return TcGroup{w + cx_off + t * qlp_n + ((size_t)lc << log_n), w + tm_off + t * ((long long)(lc - 1) << log_n),
+                       bmat[c], meta[c], w + z_off + ((size_t)t << log_n), w + z_off + ((size_t)(2 + t) << log_n),
+                       alpha, lc, nn[c], lc};
+    }
+};
+
 // ------------------------------------------------------------------ driver
 
 template <class F>
@@ -422,13 +463,38 @@ void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t it
             BScratch<0> y{r};
             ntt_inv2(c, pre.p[count], BSeqMap{pre}, BD2Load{r, mods}, y, y, BScaleYStore{r, mods}, s);
         }
+        bool tc_up = c.tc_on, tc_rs = c.tc_on;
+        for (int i = 0; i < count; i++) {
+            tc_up = tc_up && c.levels[lvl(i)]->tc_ok;
+            tc_rs = tc_rs && c.levels[lvl(i)]->tc_rescale_ok;
+        }
         // 2. mod-up base conversion, per (item, digit)
         {
             Prefix pre = make_prefix(count, beta_of);
-            with_digit_bound(alpha, [&]<int A>() {
-                count_launch();
-                modup_bconv_batch<A><<<dim3(gx, pre.p[count]), 256, 0, s>>>(r, pre, mods, nQ);
-            });
+            if (tc_up) {
+                BatchModupSrc src{};
+                src.pre = pre;
+                for (int i = 0; i < count; i++) {
+                    const LevelTables &lt = *c.levels[lvl(i)];
+                    src.ws[i] = r.it.ws[i];
+                    src.bmat[i] = lt.tc_modup.as<uint16_t>();
+                    src.meta[i] = lt.tc_modup_meta.as<TcOutMeta>();
+                    src.nn[i] = lt.tc_modup_nn.as<int>();
+                    src.l[i] = lvl(i);
+                }
+                src.y_off = r.sl.y;
+                src.tm_off = r.sl.tm;
+                src.alpha = alpha;
+                src.log_n = c.log_n;
+                src.kpad = c.tc_kpad;
+                tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, pre.p[count], mods,
+                                       c.p_inv.as<uint64_t>(), c.d_status.as<unsigned>(), s);
+            } else {
+                with_digit_bound(alpha, [&]<int A>() {
+                    count_launch();
+                    modup_bconv_batch<A><<<dim3(gx, pre.p[count]), 256, 0, s>>>(r, pre, mods, nQ);
+                });
+            }
         }
         // 3. mod-up forward NTT of every digit's complement limbs
         {
@@ -449,7 +515,24 @@ void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t it
                      BLastStore{r, c.p_hat_inv.as<uint64_t>(), mods}, s);
         }
         // 6. w_j = delta_j P^-1 + z mod q_j
-        {
+        if (tc_rs) {
+            BatchRescaleSrc src{};
+            for (int i = 0; i < count; i++) {
+                const LevelTables &lt = *c.levels[lvl(i)];
+                src.ws[i] = r.it.ws[i];
+                src.bmat[i] = lt.tc_rescale.as<uint16_t>();
+                src.meta[i] = lt.tc_rescale_meta.as<TcOutMeta>();
+                src.nn[i] = lt.tc_rescale_nn;
+                src.l[i] = lvl(i);
+            }
+            src.cx_off = r.sl.cx;
+            src.tm_off = r.sl.tm;
+            src.z_off = r.sl.z;
+            src.alpha = alpha;
+            src.log_n = c.log_n;
+            tc_bconv_launch<true>(c.tc_kpad, c.num_sms, c.log_n, src, 2 * count, mods, c.p_inv.as<uint64_t>(),
+                                  c.d_status.as<unsigned>(), s);
+        } else {
             Prefix pre = make_prefix(count, [&](int) { return 2; });
             with_digit_bound(alpha, [&]<int A>() {
                 count_launch();

@@ -186,48 +186,26 @@ static KsBuffers ks_buffers(const Context &c, const Workspace &w) {
 // Steps 1-2: y = iNTT(c2) * partQlHatInv; tm = NTT(bconv(y)) for every digit.
 static unsigned bconv_blocks(const Context &c) { return (unsigned)std::max<uint64_t>(1, c.n / 2 / 256); }
 
-// tensor-core P -> Ql conversion of both polynomials (one persistent CTA per SM)
+// tensor-core P -> Ql conversion of both polynomials (rescale: fused with the rescale's z)
 template <bool RESCALE>
 static void pq_bconv_tc_launch(const Context &c, const LevelTables &lt, uint64_t *out, long long ops,
                                const uint64_t *cx, long long cps, int l, const uint64_t *zc, const uint64_t *zd,
                                cudaStream_t s) {
-    const dim3 g((unsigned)std::max(1, std::min(c.num_sms / 2, 1 << (c.log_n - 7))), 2);
-    const DevBuf &bm = RESCALE ? lt.tc_rescale : lt.tc_moddown;
-    const DevBuf &meta = RESCALE ? lt.tc_rescale_meta : lt.tc_moddown_meta;
-    const int nn = RESCALE ? lt.tc_rescale_nn : lt.tc_moddown_nn;
-    with_tc_ksteps(c.tc_kpad, [&]<int KS>() {
-        static bool attr = [] {
-            cudaFuncSetAttribute(pq_bconv_tc<KS, RESCALE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 tc::kPipeSmemBytes);
-            return true;
-        }();
-        (void)attr;
-        count_launch();
-        pq_bconv_tc<KS, RESCALE><<<g, tc::kPipeThreads, tc::kPipeSmemBytes, s>>>(
-                out, ops, cx, cps, bm.as<uint16_t>(), meta.as<TcOutMeta>(), nn, c.d_mods.as<Mod>(),
-                c.d_status.as<unsigned>(), c.log_n, l, c.nP, zc, zd, c.p_inv.as<uint64_t>());
-    });
+    const PqSrc src{cx, cps, out, ops,
+                    (RESCALE ? lt.tc_rescale : lt.tc_moddown).as<uint16_t>(),
+                    (RESCALE ? lt.tc_rescale_meta : lt.tc_moddown_meta).as<TcOutMeta>(), zc, zd,
+                    RESCALE ? lt.tc_rescale_nn : lt.tc_moddown_nn, l, c.nP, c.log_n};
+    tc_bconv_launch<RESCALE>(c.tc_kpad, c.num_sms, c.log_n, src, 2, c.d_mods.as<Mod>(), c.p_inv.as<uint64_t>(),
+                             c.d_status.as<unsigned>(), s);
 }
 
-// tensor-core mod-up conversion of every digit: one persistent CTA per SM
+// tensor-core mod-up conversion of every digit
 void modup_bconv_tc_launch(const Context &c, const LevelTables &lt, uint64_t *tm, const uint64_t *y, int l,
                            cudaStream_t s) {
-    const int beta = lt.beta;
-    const int per_digit = std::max(1, c.num_sms / beta);  // one wave: one resident CTA per SM
-    const dim3 g((unsigned)std::min(per_digit, 1 << (c.log_n - 7)), beta);
-    with_tc_ksteps(c.tc_kpad, [&]<int KS>() {
-        static bool attr = [] {
-            cudaFuncSetAttribute(modup_bconv_tc<KS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 tc::kPipeSmemBytes);
-            return true;
-        }();
-        (void)attr;
-        count_launch();
-        modup_bconv_tc<KS><<<g, tc::kPipeThreads, tc::kPipeSmemBytes, s>>>(
-                tm, y, lt.tc_modup.as<uint16_t>(), lt.tc_modup_meta.as<TcOutMeta>(), lt.tc_modup_nn.as<int>(),
-                c.d_mods.as<Mod>(),
-                c.d_status.as<unsigned>(), c.log_n, l, c.nQ, c.nP);
-    });
+    const ModupSrc src{y, tm, lt.tc_modup.as<uint16_t>(), lt.tc_modup_meta.as<TcOutMeta>(), lt.tc_modup_nn.as<int>(),
+                       l, c.nP, c.log_n, c.tc_kpad};
+    tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, lt.beta, c.d_mods.as<Mod>(), c.p_inv.as<uint64_t>(),
+                           c.d_status.as<unsigned>(), s);
 }
 
 template <class C2Load>

@@ -22,9 +22,10 @@
 
 namespace pfg {
 
-// One output of a tensor-core base conversion: its QlP limb index and 1/p as f32.
+// One output of a tensor-core base conversion: its limb index in the output buffer, the index of
+// its modulus in the context's table, and 1/p as f32.
 struct TcOutMeta {
-    uint32_t jj;
+    uint32_t jj, tbl;
     float invp;
 };
 
