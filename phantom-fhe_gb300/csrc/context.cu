@@ -88,6 +88,7 @@ std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, cons
     int dev = 0;
     check(cudaGetDevice(&dev), "cudaGetDevice");
     check(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev), "multiprocessor count");
+    check(cudaDeviceGetAttribute(&c->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "shared memory limit");
     {
         const unsigned zero = 0;
         c->d_status.upload(&zero, sizeof(zero));
@@ -319,6 +320,61 @@ std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, cons
         up(c->hps_r2q_alpha, r2qa);
         up(c->hps_frac, frac);
         up(c->hps_modr, modr);
+
+        // tensor-core forms of the three HPS contractions (byte-plane operands, see tc.cuh); the
+        // extra slot of a conversion carries its FP64 correction v with constant -Q (or -R)
+        auto bytes_below = [](uint64_t m) {
+            int b = 0;
+            for (uint64_t v = m - 1; v; v >>= 8) b++;
+            return b;
+        };
+        int qbytes = 0, rbytes = 0;
+        for (uint64_t q : Q) qbytes += bytes_below(q);
+        for (uint64_t r : R) rbytes += bytes_below(r);
+        // every plane sum below 2^24: at most 258 nonzero byte products of at most 255 * 255
+        const bool exact = qbytes + 1 <= 258 && rbytes + 1 <= 258 && qbytes + rbytes <= 258;
+        if (exact && nQ <= 32 && nR <= 32 && nQ + nR <= 34) {
+            auto operand = [&](int npos, int nslots, int kp, auto p_of, auto const_of) {
+                std::vector<uint16_t> bm((size_t)256 * kp, 0);
+                for (int o = 0; o < npos; o++) {
+                    const uint64_t p = p_of(o);
+                    for (int sl = 0; sl < nslots; sl++) {
+                        uint64_t mp = const_of(o, sl);
+                        if (!mp) continue;
+                        for (int a = 0; a < 8; a++) {
+                            for (int b = 0; b < 8; b++)
+                                bm[canon_index(o * 8 + b, sl * 8 + a, kp)] = bf16_of_byte((unsigned)(mp >> (8 * b)) & 0xFF);
+                            mp = mulmod(mp, 256 % p, p);
+                        }
+                    }
+                }
+                return bm;
+            };
+            auto kpad = [](int slots) { return (slots * 8 + 15) / 16 * 16; };
+            c->tc_hps_kp_q2r = kpad(nQ + 1);
+            c->tc_hps_kp_r2q = kpad(nR + 1);
+            c->tc_hps_kp_scale = kpad(nQ + nR);
+            up(c->tc_hps_q2r, operand(nR, nQ + 1, c->tc_hps_kp_q2r, [&](int o) { return R[o]; }, [&](int o, int sl) {
+                   if (sl < nQ) return q2r[(size_t)o * nQ + sl];
+                   const uint64_t qm = prod_mod(Q, -1, R[o]);
+                   return qm ? R[o] - qm : 0;
+               }));
+            up(c->tc_hps_r2q, operand(nQ, nR + 1, c->tc_hps_kp_r2q, [&](int o) { return Q[o]; }, [&](int o, int sl) {
+                   if (sl < nR) return r2q[(size_t)o * nR + sl];
+                   const uint64_t rm = prod_mod(R, -1, Q[o]);
+                   return rm ? Q[o] - rm : 0;
+               }));
+            up(c->tc_hps_scale, operand(nR, nQ + nR, c->tc_hps_kp_scale, [&](int o) { return R[o]; },
+                                        [&](int o, int sl) -> uint64_t {
+                                            if (sl < nQ) return modr[(size_t)o * (nQ + 1) + sl];
+                                            return sl - nQ == o ? modr[(size_t)o * (nQ + 1) + nQ] : 0;
+                                        }));
+            // the scale-and-round tile (A, B, staged inputs, carries) must fit one CTA
+            const size_t ncols = (size_t)(nR * 8 + 15) / 16 * 16;
+            const size_t scale_smem = (size_t)128 * c->tc_hps_kp_scale * 2 + ncols * c->tc_hps_kp_scale * 2 +
+                                      (size_t)(nQ + nR) * 128 * 8 + (size_t)nR * 128 * 8;
+            c->tc_hps_ok = scale_smem + 4096 <= (size_t)c->smem_optin;
+        }
     }
 
     c->galois_elts = galois_elts;

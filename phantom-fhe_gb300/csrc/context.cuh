@@ -82,6 +82,11 @@ struct Context {
     DevBuf hps_q2r_alpha, hps_r2q_alpha;   // [nQ+1][nR], [nR+1][nQ]
     DevBuf hps_frac;                        // [nQ] doubles
     DevBuf hps_modr;                        // [nR][nQ+1]
+    // tensor-core operands of the HPS contractions ([256][kp] bf16 byte planes): Q -> R and
+    // R -> Q conversions (input limbs + the FP64 correction slot) and the scale-and-round QR -> R
+    DevBuf tc_hps_q2r, tc_hps_r2q, tc_hps_scale;
+    int tc_hps_kp_q2r = 0, tc_hps_kp_r2q = 0, tc_hps_kp_scale = 0;
+    bool tc_hps_ok = false;
     // Galois
     std::vector<uint32_t> galois_elts;
     std::map<uint32_t, std::unique_ptr<DevBuf>> perms;
@@ -90,6 +95,7 @@ struct Context {
     bool tc_avail = false, tc_on = false;
     int tc_kpad = 0;  // K of the byte-plane GEMM: 8 alpha rounded up to 16
     int num_sms = 0;
+    int smem_optin = 0;  // largest dynamic shared memory a block may opt in to (bytes)
     DevBuf d_status;  // device error word (bounded waits that gave up), read by fhe_context_status
 
     int l1() const { return log_n / 2; }

@@ -12,7 +12,11 @@
 //      (...(alpha mod r_0)... ) mod r_j; this is reproduced;
 //   4. relinearisation of c2 in the coefficient domain (DRNSTool::modup / moddown_from_NTT BFV
 //      branches, src/rns_bconv.cu:530-628, 776-828).
+#include <stdexcept>
+#include <string>
+
 #include "bconv.cuh"
+#include "hps_tc.cuh"
 #include "keyswitch.cuh"
 #include "launch.cuh"
 #include "ops.hpp"
@@ -272,6 +276,47 @@ void bfv_keyswitch(const Context &c, const Workspace &w, uint64_t *ct, const uin
     bfv_keyswitch_to(c, w.base, ct, ct, c2, l, evk, s);
 }
 
+template <int MODE>
+static void hps_tc_launch(const Context &c, const HpsTcArgs &a, cudaStream_t s) {
+    const size_t smem = hps_tc_smem(a, MODE);
+    if (smem + 4096 > (size_t)c.smem_optin) throw std::logic_error("HPS tensor-core tile exceeds shared memory");
+    static int attr_set = 0;  // raised once to the device's opt-in limit (less the static part)
+    if (!attr_set) {
+        const cudaError_t e = cudaFuncSetAttribute(hps_tc_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   c.smem_optin - 4096);
+        if (e != cudaSuccess) throw std::runtime_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+        attr_set = 1;
+    }
+    const int per_sm = smem <= 100 * 1024 ? 2 : 1;  // 2 x 256 tensor-memory columns at most
+    const int units = a.polys << (a.log_n - 7);
+    count_launch();
+    hps_tc_kernel<MODE><<<std::min(units, per_sm * c.num_sms), 256, smem, s>>>(a);
+}
+
+// Q -> R (or R -> Q) HPS conversion of `polys` polynomials on the tensor cores.
+static void hps_conv_tc(const Context &c, bool q2r, uint64_t *out, long long ops, const uint64_t *in, long long ips,
+                        int polys, cudaStream_t s) {
+    const int nQ = c.nQ, nR = c.nR, rbase = c.nQ + c.nP;
+    HpsTcArgs a{};
+    a.out = out;
+    a.ops = ops;
+    a.in = in;
+    a.ips = ips;
+    a.mods = c.d_mods.as<Mod>();
+    a.in_tbl0 = q2r ? 0 : rbase;
+    a.ni = q2r ? nQ : nR;
+    a.out_tbl0 = q2r ? rbase : 0;
+    a.no = q2r ? nR : nQ;
+    a.hat_inv = (q2r ? c.hps_q_hat_inv : c.hps_r_hat_inv).as<uint64_t>();
+    a.dinv = (q2r ? c.hps_q_inv : c.hps_r_inv).as<double>();
+    a.bmat = (q2r ? c.tc_hps_q2r : c.tc_hps_r2q).as<uint16_t>();
+    a.kp = q2r ? c.tc_hps_kp_q2r : c.tc_hps_kp_r2q;
+    a.polys = polys;
+    a.log_n = c.log_n;
+    a.status = c.d_status.as<unsigned>();
+    hps_tc_launch<kHpsConv>(c, a, s);
+}
+
 void bfv_mul_relin_hps(const Context &c, const Workspace &w, uint64_t *ct1, const uint64_t *ct2,
                        const uint64_t *const *rlk, cudaStream_t s) {
     const int nQ = c.nQ, nR = c.nR, qr = nQ + nR, rbase = c.nQ + c.nP;
@@ -287,17 +332,26 @@ void bfv_mul_relin_hps(const Context &c, const Workspace &w, uint64_t *ct1, cons
     if (sm_q > 48 * 1024) cudaFuncSetAttribute(hps_bconv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_q);
     if (sm_r > 48 * 1024)
         cudaFuncSetAttribute(hps_scale_round_to_q, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_r);
-    count_launch();
-    hps_bconv<<<g, 256, sm_q, s>>>(ea + qps, qrps, ct1, qps, mods, 0, nQ, rbase, nR, c.hps_q_hat_inv.as<uint64_t>(),
-                                   c.hps_q_inv.as<double>(), c.hps_q2r_mat.as<uint64_t>(),
-                                   c.hps_q2r_alpha.as<uint64_t>(), c.log_n);
+    const bool tc = c.tc_on && c.tc_hps_ok;
+    if (tc) {
+        hps_conv_tc(c, true, ea + qps, qrps, ct1, qps, 2, s);
+    } else {
+        count_launch();
+        hps_bconv<<<g, 256, sm_q, s>>>(ea + qps, qrps, ct1, qps, mods, 0, nQ, rbase, nR,
+                                       c.hps_q_hat_inv.as<uint64_t>(), c.hps_q_inv.as<double>(),
+                                       c.hps_q2r_mat.as<uint64_t>(), c.hps_q2r_alpha.as<uint64_t>(), c.log_n);
+    }
     const uint64_t *ebp = ea;
     if (!square) {
         cudaMemcpy2DAsync(eb, qrps * 8, ct2, qps * 8, qps * 8, 2, cudaMemcpyDeviceToDevice, s);
-        count_launch();
-        hps_bconv<<<g, 256, sm_q, s>>>(eb + qps, qrps, ct2, qps, mods, 0, nQ, rbase, nR,
-                                       c.hps_q_hat_inv.as<uint64_t>(), c.hps_q_inv.as<double>(),
-                                       c.hps_q2r_mat.as<uint64_t>(), c.hps_q2r_alpha.as<uint64_t>(), c.log_n);
+        if (tc) {
+            hps_conv_tc(c, true, eb + qps, qrps, ct2, qps, 2, s);
+        } else {
+            count_launch();
+            hps_bconv<<<g, 256, sm_q, s>>>(eb + qps, qrps, ct2, qps, mods, 0, nQ, rbase, nR,
+                                           c.hps_q_hat_inv.as<uint64_t>(), c.hps_q_inv.as<double>(),
+                                           c.hps_q2r_mat.as<uint64_t>(), c.hps_q2r_alpha.as<uint64_t>(), c.log_n);
+        }
         ebp = eb;
     }
     // 2. NTT over QR, tensor (inside the inverse NTT's load), inverse NTT
@@ -307,12 +361,37 @@ void bfv_mul_relin_hps(const Context &c, const Workspace &w, uint64_t *ct1, cons
     PtrStore t3s{t3, qrps, c.log_n};
     ntt_inv(c, 3 * qr, qm, TensorQrLoad{ea, ebp, qrps, mods, c.log_n}, t3s, t3s, s);
     // 3. scale and round to R, then back to Q
-    dim3 g3((unsigned)(n / kHpsTile), 3);
-    count_launch();
-    hps_scale_round_to_q<<<g3, 256, sm_r, s>>>(o3, qps, t3, qrps, mods, nQ, rbase, nR, c.hps_frac.as<double>(),
-                                                c.hps_modr.as<uint64_t>(), c.hps_r_hat_inv.as<uint64_t>(),
-                                                c.hps_r_inv.as<double>(), c.hps_r2q_mat.as<uint64_t>(),
-                                                c.hps_r2q_alpha.as<uint64_t>(), c.log_n);
+    if (tc) {
+        // rt [3][nR][N] goes to ea (free once the tensor has been transformed)
+        const long long rps = (long long)nR * n;
+        HpsTcArgs a{};
+        a.out = ea;
+        a.ops = rps;
+        a.in = t3;
+        a.ips = qrps;
+        a.mods = mods;
+        a.in_tbl0 = 0;
+        a.in_tbl_r = rbase;
+        a.ni = nQ;
+        a.nr = nR;
+        a.out_tbl0 = rbase;
+        a.no = nR;
+        a.dinv = c.hps_frac.as<double>();
+        a.bmat = c.tc_hps_scale.as<uint16_t>();
+        a.kp = c.tc_hps_kp_scale;
+        a.polys = 3;
+        a.log_n = c.log_n;
+        a.status = c.d_status.as<unsigned>();
+        hps_tc_launch<kHpsScale>(c, a, s);
+        hps_conv_tc(c, false, o3, qps, ea, rps, 3, s);
+    } else {
+        dim3 g3((unsigned)(n / kHpsTile), 3);
+        count_launch();
+        hps_scale_round_to_q<<<g3, 256, sm_r, s>>>(o3, qps, t3, qrps, mods, nQ, rbase, nR, c.hps_frac.as<double>(),
+                                                    c.hps_modr.as<uint64_t>(), c.hps_r_hat_inv.as<uint64_t>(),
+                                                    c.hps_r_inv.as<double>(), c.hps_r2q_mat.as<uint64_t>(),
+                                                    c.hps_r2q_alpha.as<uint64_t>(), c.log_n);
+    }
     // 4. relinearise c2 into (c0, c1), written to ct1
     bfv_keyswitch_to(c, ks, ct1, o3, o3 + 2 * qps, nQ, rlk, s);
 }

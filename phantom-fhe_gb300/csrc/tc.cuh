@@ -118,16 +118,16 @@ __device__ __forceinline__ uint4 bytes_bf16(uint64_t v) {
 
 // x = V mod p up to one multiple of p (x in [0, 2p)), V = sum_b C_b 2^(8b), from the f32 bit
 // patterns r[b] of the NPL plane sums.  Every constant M'_(i,a) is below p, so V < 255 K p and
-// the quotient is below 2^14.  The f32 value of V times 1/p (relative error < 2^-20, absolute
-// < 0.01) minus 0.52 rounds to floor(V / p) or floor(V / p) - 1, clamped at 0; V and q p are only
-// needed modulo 2^64 because the remainder is small.  [0, 2p) is a valid input of the lazy
-// forward NTT that consumes these values.
+// the quotient is below 255 K <= 2^16 (K <= 258 nonzero byte terms).  The f32 value of V times
+// 1/p has relative error below 2^-20.5, so absolute error below 0.05; minus 0.625 it rounds to
+// floor(V / p) or floor(V / p) - 1, clamped at 0.  V and q p are only needed modulo 2^64 because
+// the remainder is small.  [0, 2p) is a valid input of the lazy forward NTT.
 template <int NPL>
 __device__ __forceinline__ uint64_t reduce_planes_lazy(const uint32_t *r, uint64_t p, float invp) {
     float vf = __uint_as_float(r[0]);
 #pragma unroll
     for (int b = 1; b < NPL; b++) vf = fmaf(__uint_as_float(r[b]), __uint_as_float((uint32_t)(127 + 8 * b) << 23), vf);
-    const float qf = fmaf(vf, invp, -0.52f);
+    const float qf = fmaf(vf, invp, -0.625f);
     const int32_t qs = (int32_t)(__float_as_uint(qf + 12582912.0f) - 0x4B400000u);  // round to nearest
     const uint32_t q = (uint32_t)max(qs, 0);
     uint32_t u[NPL];

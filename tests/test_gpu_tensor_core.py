@@ -87,3 +87,38 @@ def test_tensor_cores_unavailable_for_wide_digits(pg):
     assert not ctx.tensor_cores
     with pytest.raises(pg.InvalidArgument):
         ctx.tensor_cores = True
+
+
+BFV_PARAMS = {
+    "bfv_n12_4x50": (4096, [50, 50, 50, 50, 60, 60], 2, 65537),
+    "bfv_n15_16x50": (32768, [50] * 16 + [60, 60], 2, 65537),
+    "bfv_n13_6x40": (8192, [40] * 6 + [60], 1, 786433),
+}
+
+
+@pytest.mark.parametrize("name", list(BFV_PARAMS))
+def test_bfv_hps_tensor_core_matches_oracle_and_cuda_core(pg, name):
+    """HPS conversions and scale-and-round on the tensor cores (with the FP64 corrections in the
+    reference's order) give the oracle's words, as the CUDA-core kernels do."""
+    n, bits, special, t = BFV_PARAMS[name]
+    mods = pg.create_coeff_modulus(n, bits)
+    nq = len(bits) - special
+    ctx = pg.Context(n, mods, special, scheme=pg.SCHEME_BFV, plain_modulus=t)
+    oc = O.Context(n.bit_length() - 1, mods, nq, special, t)
+    ws = ctx.workspace()
+    rng = np.random.default_rng(nq * 31 + special)
+    key = O.random_residues(rng, mods, n, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), n)
+    k = pg.KeySwitchKey(pg.to_device(key))
+    a = O.random_residues(rng, mods[:nq], n, 2)
+    b = O.random_residues(rng, mods[:nq], n, 2)
+    want = oc.bfv_mul_relin_hps(a, b, key)
+    for tc in (True, False):
+        ctx.tensor_cores = tc
+        ta = pg.to_device(a)
+        ctx.multiply_and_relin(ws, ta, pg.to_device(b), 1, k)
+        _eq(ta, want, f"{name} BFV multiply_and_relin tensor_cores={tc}")
+    ctx.tensor_cores = True
+    ts = pg.to_device(a)
+    ctx.multiply_and_relin(ws, ts, ts, 1, k)
+    _eq(ts, oc.bfv_mul_relin_hps(a, a, key), f"{name} BFV square_and_relin (tensor cores)")
+    assert ctx.device_status() == 0
