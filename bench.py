@@ -416,6 +416,9 @@ def run_ours(args):
     g.replay()
     t_graph = timed(lambda i: g.replay(), 3) / 3
     t_bloop = timed(lambda i: [bctx.multiply_and_relin(bws, x, y, 1, bkey, stream) for x, y in bpairs], 3) / 3
+    bctx.tensor_cores = False
+    t_bloop_cc = timed(lambda i: [bctx.multiply_and_relin(bws, x, y, 1, bkey, stream) for x, y in bpairs], 3) / 3
+    bctx.tensor_cores = True
     del g, bpairs, bct, bws, bctx
 
     mv = matvec_bench(pg, torch, timed, stream, rank)
@@ -464,6 +467,7 @@ def run_ours(args):
             "extra": {"ntt_n12_3x60_roundtrip_us": 1e6 * t12,
                       "bfv_n15_mult_relin_graph128_ops_per_s": 128 * world / t_graph,
                       "bfv_n15_mult_relin_loop128_ops_per_s": 128 * world / t_bloop,
+                      "bfv_n15_mult_relin_loop128_cuda_core_ops_per_s": 128 * world / t_bloop_cc,
                       "batch64_uneven_levels_ops_per_s": 64 * world / t_batch,
                       "batch64_as_single_calls_ops_per_s": 64 * world / t_loop,
                       "hrotate_step1_per_s": k2 * world / t_rot, "keyswitch_per_s": k2 * world / t_ks,

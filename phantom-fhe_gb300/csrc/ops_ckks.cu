@@ -52,13 +52,29 @@ size_t workspace_words(const Context &c) {
 
 // ------------------------------------------------------------------ NTT entry points
 
+// N = 2^12: one CTA holds a whole limb (16 coefficients per thread), so the transform is a
+// single pass — the row-pass kernel with the full length as its vector and no column stages.
+template <bool FWD>
+static void ntt_single_pass_n12(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s) {
+    const long long ps = (long long)limbs << c.log_n;
+    NttTables T = c.ntt();
+    T.l1 = 0;
+    T.l2 = 12;
+    count_launch();
+    PtrStore st{data, ps, c.log_n};
+    ntt_row_pass<12, FWD, true><<<dim3(1, (unsigned)(polys * limbs)), kNttThreads, 0, s>>>(
+            T, SeqMap{limbs, start}, PtrLoad{data, ps, c.log_n}, st);
+}
+
 void ntt_forward(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s) {
+    if (c.log_n == 12) return ntt_single_pass_n12<true>(c, data, polys, limbs, start, s);
     const long long ps = (long long)limbs << c.log_n;
     PtrStore st{data, ps, c.log_n};
     ntt_fwd(c, polys * limbs, SeqMap{limbs, start}, PtrLoad{data, ps, c.log_n}, st, st, s);
 }
 
 void ntt_inverse(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s) {
+    if (c.log_n == 12) return ntt_single_pass_n12<false>(c, data, polys, limbs, start, s);
     const long long ps = (long long)limbs << c.log_n;
     PtrStore st{data, ps, c.log_n};
     ntt_inv(c, polys * limbs, SeqMap{limbs, start}, PtrLoad{data, ps, c.log_n}, st, st, s);
