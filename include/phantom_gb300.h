@@ -86,6 +86,16 @@ void fhe_context_destroy(fhe_context *ctx);
 int fhe_context_set_tensor_cores(fhe_context *ctx, int enable);
 int fhe_context_tensor_cores(const fhe_context *ctx);
 
+/* NTT stage split (autotuner).  The forward transform runs its first l1 stages as a column
+ * pass and the remaining log2(N) - l1 as a row pass; every supported split gives the same
+ * words.  fhe_context_autotune times each supported split on scratch limbs (forward + inverse,
+ * CUDA events, one-time setup call that allocates and synchronises) and keeps the fastest;
+ * fhe_context_set_ntt_split applies a stored choice.  No counterpart in the reference, whose
+ * radix-8 two-phase split is fixed per degree (src/ntt/fntt_2d.cu:620-653). */
+int fhe_context_ntt_split(const fhe_context *ctx);
+int fhe_context_set_ntt_split(fhe_context *ctx, int l1);
+int fhe_context_autotune(fhe_context *ctx, int *chosen_l1, float *best_us);
+
 /* Reads and clears the context's device status word (synchronises the device).  Non-zero
  * means a bounded wait inside a tensor-core kernel gave up and that call's output is invalid.
  * No counterpart in the reference. */

@@ -131,6 +131,75 @@ int fhe_context_status(const fhe_context *ctx, unsigned *out) {
     }, false);
 }
 
+int fhe_context_ntt_split(const fhe_context *ctx) {
+    if (!ctx || !ctx->c) return 0;
+    return ctx->c->l1();
+}
+
+int fhe_context_set_ntt_split(fhe_context *ctx, int l1) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        if (!c.split_ok(l1)) throw std::invalid_argument("unsupported NTT stage split for this degree");
+        c.l1_sel = l1;
+    }, false);
+}
+
+int fhe_context_autotune(fhe_context *ctx, int *chosen_l1, float *best_us) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        // the operations' regime: every QP limb, enough polynomials for >= 256 MB (beyond L2)
+        const int limbs = c.nQ + c.nP;
+        const size_t poly_bytes = (size_t)limbs * c.n * 8;
+        const int polys = (int)std::min<size_t>(64, std::max<size_t>(1, ((size_t)256 << 20) / poly_bytes + 1));
+        const size_t words = (size_t)polys * limbs * c.n;
+        uint64_t *buf = nullptr;
+        if (cudaMalloc(&buf, words * 8) != cudaSuccess) throw std::runtime_error("autotune scratch allocation failed");
+        cudaMemset(buf, 0, words * 8);
+        cudaStream_t s;
+        cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        const int keep = c.l1_sel;
+        int best = 0;
+        float best_t = 0.f;
+        for (int l1 = 6; l1 <= 8; l1++) {
+            if (!c.split_ok(l1)) continue;
+            c.l1_sel = l1;
+            for (int i = 0; i < 2; i++) {
+                pfg::ntt_forward(c, buf, polys, limbs, 0, s);
+                pfg::ntt_inverse(c, buf, polys, limbs, 0, s);
+            }
+            const int reps = 3;
+            float us = 0.f;
+            for (int trial = 0; trial < 3; trial++) {  // best of three
+                cudaEventRecord(e0, s);
+                for (int i = 0; i < reps; i++) {
+                    pfg::ntt_forward(c, buf, polys, limbs, 0, s);
+                    pfg::ntt_inverse(c, buf, polys, limbs, 0, s);
+                }
+                cudaEventRecord(e1, s);
+                cudaEventSynchronize(e1);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                const float t = 1000.f * ms / reps;
+                if (trial == 0 || t < us) us = t;
+            }
+            if (!best || us < best_t) {
+                best = l1;
+                best_t = us;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaStreamDestroy(s);
+        cudaFree(buf);
+        c.l1_sel = best ? best : keep;
+        if (chosen_l1) *chosen_l1 = c.l1();
+        if (best_us) *best_us = best_t;
+    });
+}
+
 int fhe_context_moduli(const fhe_context *ctx, uint64_t *out) {
     return guarded([&] {
         const pfg::Context &c = ctx_of(ctx);

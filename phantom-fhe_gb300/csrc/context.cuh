@@ -98,8 +98,12 @@ struct Context {
     int smem_optin = 0;  // largest dynamic shared memory a block may opt in to (bytes)
     DevBuf d_status;  // device error word (bounded waits that gave up), read by fhe_context_status
 
-    int l1() const { return log_n / 2; }
-    int l2() const { return log_n - log_n / 2; }
+    // NTT stage split: the column pass runs the first l1 stages, the row pass the other l2.  Any
+    // supported split gives the same words; the autotuner (fhe_context_autotune) picks one.
+    int l1_sel = 0;  // 0: log_n / 2
+    int l1() const { return l1_sel ? l1_sel : log_n / 2; }
+    int l2() const { return log_n - l1(); }
+    bool split_ok(int l) const { return l >= 6 && l <= 8 && log_n - l >= 6 && log_n - l <= 9; }
     NttTables ntt() const {
         return NttTables{d_mods.as<Mod>(), d_tw.as<TwPair>(), d_itw.as<TwPair>(), d_ninv.as<uint64_t>(), log_n,
                          l1(), l2()};

@@ -56,6 +56,9 @@ def _load():
     L.fhe_context_set_tensor_cores.argtypes = [_vp, ctypes.c_int]
     L.fhe_context_tensor_cores.argtypes = [_vp]
     L.fhe_context_status.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint)]
+    L.fhe_context_ntt_split.argtypes = [_vp]
+    L.fhe_context_set_ntt_split.argtypes = [_vp, ctypes.c_int]
+    L.fhe_context_autotune.argtypes = [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)]
     L.fhe_context_sizes.argtypes = [_vp] + [ctypes.POINTER(_u64)] + [ctypes.POINTER(_sz)] * 4
     L.fhe_context_moduli.argtypes = [_vp, ctypes.POINTER(_u64)]
     L.fhe_context_galois_elts.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(_sz)]
@@ -186,6 +189,38 @@ class Context:
     @tensor_cores.setter
     def tensor_cores(self, on):
         _check(lib.fhe_context_set_tensor_cores(self._h, int(bool(on))))
+
+    @property
+    def ntt_split(self):
+        """Number of NTT stages in the column pass (the row pass runs the rest)."""
+        return int(lib.fhe_context_ntt_split(self._h))
+
+    @ntt_split.setter
+    def ntt_split(self, l1):
+        _check(lib.fhe_context_set_ntt_split(self._h, int(l1)))
+
+    def autotune(self, cache_path=None):
+        """Chooses the NTT stage split by timing every supported one (forward + inverse on
+        scratch limbs).  With cache_path, a JSON file keyed by GPU, degree and modulus count
+        stores the choice so later contexts skip the timing.  Returns {"ntt_split": l1, ...}."""
+        import json
+        import torch
+        key = f"{torch.cuda.get_device_name()}|N={self.n}|moduli={len(self.moduli)}"
+        cache = {}
+        if cache_path and os.path.exists(cache_path):
+            with open(cache_path) as f:
+                cache = json.load(f)
+        if key in cache:
+            self.ntt_split = cache[key]["ntt_split"]
+            return dict(cache[key], cached=True)
+        l1, us = ctypes.c_int(), ctypes.c_float()
+        _check(lib.fhe_context_autotune(self._h, ctypes.byref(l1), ctypes.byref(us)))
+        result = {"ntt_split": int(l1.value), "roundtrip_us": float(us.value)}
+        if cache_path:
+            cache[key] = result
+            with open(cache_path, "w") as f:
+                json.dump(cache, f, indent=1, sort_keys=True)
+        return dict(result, cached=False)
 
     def device_status(self):
         """Reads and clears the device status word (0 = every bounded wait completed)."""

@@ -122,3 +122,37 @@ def test_bfv_hps_tensor_core_matches_oracle_and_cuda_core(pg, name):
     ctx.multiply_and_relin(ws, ts, ts, 1, k)
     _eq(ts, oc.bfv_mul_relin_hps(a, a, key), f"{name} BFV square_and_relin (tensor cores)")
     assert ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("log_n,splits", [(13, [6, 7]), (15, [6, 7, 8]), (16, [7, 8])])
+def test_every_ntt_split_gives_the_same_words(pg, log_n, splits):
+    """The autotuner's choice (column-pass stages l1) never changes a result."""
+    n = 1 << log_n
+    bits = [60] + [40] * 5 + [60, 60]
+    mods = pg.create_coeff_modulus(n, bits)
+    ctx = pg.Context(n, mods, 2)
+    oc = O.Context(log_n, mods, 6, 2)
+    ws = ctx.workspace()
+    rng = np.random.default_rng(log_n)
+    a = O.random_residues(rng, mods, n, 1)
+    key = O.random_residues(rng, mods, n, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), n)
+    k = pg.KeySwitchKey(pg.to_device(key))
+    ct = O.random_residues(rng, mods[:6], n, 2)
+    c2 = O.random_residues(rng, mods[:6], n, 1)[0]
+    want_ntt = oc.ntt_fwd(a[0])
+    want_ks = oc.keyswitch(6, ct, c2, key)
+    for l1 in splits:
+        ctx.ntt_split = l1
+        assert ctx.ntt_split == l1
+        t = pg.to_device(a)
+        ctx.ntt_forward(t, 1, len(mods))
+        _eq(t, want_ntt, f"forward NTT, split {l1}/{log_n - l1}")
+        ctx.ntt_inverse(t, 1, len(mods))
+        _eq(t, a, f"round trip, split {l1}/{log_n - l1}")
+        tk = pg.to_device(ct)
+        ctx.keyswitch(ws, tk, pg.to_device(c2), 1, k)
+        _eq(tk, want_ks, f"keyswitch, split {l1}/{log_n - l1}")
+    with pytest.raises(pg.InvalidArgument):
+        ctx.ntt_split = 5
+    tuned = ctx.autotune()
+    assert tuned["ntt_split"] in splits and ctx.ntt_split == tuned["ntt_split"]
