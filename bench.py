@@ -46,6 +46,21 @@ def dist_info():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def max_over_ranks(t, world, device):
+    """The slowest rank's time: replicas are timed independently and the job ends with the last."""
+    if world <= 1:
+        return t
+    import torch
+    tt = torch.tensor([t], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replica_throughput(steps, world, t):
+    """Whole-job throughput of `world` replicas that each ran `steps` operations in at most t s."""
+    return steps * world / t
+
+
 def random_residues(rng, moduli, n, polys):
     out = np.empty((polys, len(moduli), n), dtype=np.uint64)
     for k, q in enumerate(moduli):
@@ -340,11 +355,8 @@ def run_ours(args):
     t = timed(step, args.steps)
     launches = lib.fhe_kernel_launches() - l0
     barrier()
-    if world > 1:
-        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t = float(tt.item())
-    value = args.steps * world / t
+    t = max_over_ranks(t, world, "cuda")
+    value = replica_throughput(args.steps, world, t)
 
     # companion measurements on the same parameters (same timing rules)
     k2 = max(args.steps // 2, 10)
@@ -479,10 +491,7 @@ def run_ours(args):
     barrier()
     t_e2e = e2e_timed(args.steps)
     barrier()
-    if world > 1:
-        tt = torch.tensor([t_e2e], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+    t_e2e = max_over_ranks(t_e2e, world, "cuda")
     ck = clocks.stop()
 
     peak, peak_kind = measured_peaks()
@@ -492,7 +501,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
             "config": dict(CONFIG, ntt_split=f"{tuning['ntt_split']}+{16 - tuning['ntt_split']} (autotuned)"),
             "clocks": ck,
-            "e2e": {"value": args.steps * world / t_e2e, "unit": "ops/s",
+            "e2e": {"value": replica_throughput(args.steps, world, t_e2e), "unit": "ops/s",
                     "h2d_bytes_per_step": 2 * 2 * l * N * 8, "d2h_bytes_per_step": 2 * (l - 1) * N * 8},
             "gpu_launches": int(launches),
             "roofline": {"kernel": "ntt forward (column + row pass), 64 polys x 35 limbs, N=2^16",
