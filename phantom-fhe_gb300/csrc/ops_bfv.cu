@@ -186,26 +186,6 @@ struct TensorQrLoad {
 
 // ------------------------------------------------------------------ relinearisation (BFV)
 
-// Mod-up digit d into QlP limb jj from c2 in coefficient form: own limbs pass through,
-// the rest are sum_i [c2_i * partQlHatInv_i]_{q_i} * M_d[jj][i] mod p_jj.
-struct BfvBconvLoad {
-    const uint64_t *c2, *phi, *mat;
-    const Mod *mods;
-    int log_n, l, alpha, qlp;
-    __device__ __forceinline__ uint64_t operator()(int d, int jj, int tbl, uint32_t idx) const {
-        const int s0 = d * alpha, sz = min(alpha, l - s0);
-        if (jj >= s0 && jj < s0 + sz) return c2[((size_t)jj << log_n) + idx];
-        const uint64_t *m = mat + ((size_t)d * qlp + jj) * alpha;
-        u128 acc{0, 0};
-        for (int i = 0; i < sz; i++) {
-            const int qi = s0 + i;
-            const uint64_t y = mul_shoup(c2[((size_t)qi << log_n) + idx], phi[2 * qi], phi[2 * qi + 1], mods[qi].q);
-            mac(acc, y, __ldg(m + i));
-        }
-        return reduce128(acc, mods[tbl]);
-    }
-};
-
 // After the inverse NTT of cx: Q limbs unchanged, P limbs times PHatInv.
 struct BfvCxStore {
     uint64_t *cx;

@@ -93,38 +93,6 @@ struct TensorD2Load {
     }
 };
 
-// Base conversion of one digit into a complement limb (bconv_matmul_padded_unroll2_kernel,
-// src/rns_bconv.cu:455-485): sum_i y[s+i] * M_d[jj][i] mod p_jj.
-struct BconvLoad {
-    const uint64_t *y, *mat;
-    const Mod *mods;
-    int log_n, l, alpha, qlp;
-    __device__ __forceinline__ uint64_t operator()(int d, int jj, int tbl, uint32_t idx) const {
-        const int s0 = d * alpha, sz = min(alpha, l - s0);
-        const uint64_t *m = mat + ((size_t)d * qlp + jj) * alpha;
-        u128 acc{0, 0};
-        for (int i = 0; i < sz; i++) mac(acc, y[((size_t)(s0 + i) << log_n) + idx], __ldg(m + i));
-        return reduce128(acc, mods[tbl]);
-    }
-};
-
-// P -> q_j base conversion of the mod-down (bConv_BEHZ, src/rns_bconv.cu:212-229): yp holds
-// [x_k * PHatInv_k]_{p_k} in the P limbs of cx.
-struct PBconvLoad {
-    const uint64_t *cx;
-    long long cps;
-    const uint64_t *pmat;
-    const Mod *mods;
-    int log_n, l, nP;
-    __device__ __forceinline__ uint64_t operator()(int t, int j, int tbl, uint32_t idx) const {
-        const uint64_t *yp = cx + t * cps + ((size_t)l << log_n) + idx;
-        const uint64_t *m = pmat + (size_t)j * nP;
-        u128 acc{0, 0};
-        for (int k = 0; k < nP; k++) mac(acc, yp[(size_t)k << log_n], __ldg(m + k));
-        return reduce128(acc, mods[tbl]);
-    }
-};
-
 // Bases added to the mod-down result.
 struct InplaceBase {  // the ciphertext itself (keyswitch_inplace's add_to_ct_kernel)
     const uint64_t *ct;
@@ -154,25 +122,6 @@ struct FirstPolyBase {  // t = 0: g0, t = 1: 0 (Galois: c1 is wiped before the k
     int log_n;
     __device__ __forceinline__ uint64_t operator()(int t, int j, const Mod &, uint32_t idx) const {
         return t == 0 ? g0[((size_t)j << log_n) + idx] : 0;
-    }
-};
-
-// Row-pass store of step 5: out_t[j] = base + (cx_t[j] - v) * P^-1 mod q_j
-template <class Base>
-struct ModdownStore {
-    uint64_t *out0, *out1;  // limb j is written at limb j - jofs
-    int jofs;
-    const uint64_t *cx;
-    long long cps;
-    const uint64_t *pinv;
-    const Mod *mods;
-    int log_n;
-    Base base;
-    __device__ __forceinline__ void operator()(int t, int j, int tbl, uint32_t idx, uint64_t v) const {
-        const Mod m = mods[tbl];
-        const size_t o = ((size_t)j << log_n) + idx;
-        const uint64_t r = mul_shoup(sub_mod(cx[t * cps + o], v, m.q), pinv[2 * j], pinv[2 * j + 1], m.q);
-        (t == 0 ? out0 : out1)[((size_t)(j - jofs) << log_n) + idx] = add_mod(base(t, j, m, idx), r, m.q);
     }
 };
 
@@ -268,11 +217,37 @@ static void moddown_intt_p(const Context &c, const KsBuffers &b, int l, cudaStre
             ScaleStore{b.cx, cps, c.log_n, l, c.p_hat_inv.as<uint64_t>(), c.d_mods.as<Mod>()}, s);
 }
 
-// Step 5 over limbs [k0, k0 + nl) of both polynomials (limb k0 lands at out[0]),
-// intermediate in `mid` ([2][l][N]).
+// out_t[j] = base_t[j] + (cx_t[j] - v_t[j]) P^-1 for both polynomials and j < l, two coefficients
+// per thread (coalesced).  Each element is read and written by one thread, so out may alias the
+// base (in-place key switch; HMult's poly 1 output over a1, read only by the same element).
 template <class Base>
-static void moddown_ntt(const Context &c, const KsBuffers &b, uint64_t *mid, int l, int k0, int nl, uint64_t *out0,
-                        uint64_t *out1, Base base, cudaStream_t s) {
+__global__ void __launch_bounds__(256) moddown_combine(uint64_t *out0, uint64_t *out1, const uint64_t *v,
+                                                       long long vps, const uint64_t *cx, long long cps,
+                                                       const uint64_t *pinv, const Mod *mods, int log_n, int l,
+                                                       Base base) {
+    const size_t half = (size_t)1 << (log_n - 1), per_poly = (size_t)l * half;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * per_poly;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const int t = e >= per_poly;
+        const size_t r = e - t * per_poly;
+        const int j = (int)(r >> (log_n - 1));
+        const uint32_t idx = (uint32_t)(2 * (r & (half - 1)));
+        const size_t o = ((size_t)j << log_n) + idx;
+        const Mod m = mods[j];
+        const uint64_t pj = pinv[2 * j], pjs = pinv[2 * j + 1];
+        const ulonglong2 vv = *reinterpret_cast<const ulonglong2 *>(v + t * vps + o);
+        const ulonglong2 cc = *reinterpret_cast<const ulonglong2 *>(cx + t * cps + o);
+        const uint64_t y0 = add_mod(base(t, j, m, idx), mul_shoup(sub_mod(cc.x, vv.x, m.q), pj, pjs, m.q), m.q);
+        const uint64_t y1 = add_mod(base(t, j, m, idx + 1), mul_shoup(sub_mod(cc.y, vv.y, m.q), pj, pjs, m.q), m.q);
+        *reinterpret_cast<ulonglong2 *>((t == 0 ? out0 : out1) + o) = make_ulonglong2(y0, y1);
+    }
+}
+
+// Step 5 over all l limbs of both polynomials, intermediate in `mid` ([2][l][N]): the forward NTT
+// of delta (stored plainly), then the combine as one element-wise pass.
+template <class Base>
+static void moddown_ntt(const Context &c, const KsBuffers &b, uint64_t *mid, int l, uint64_t *out0, uint64_t *out1,
+                        Base base, cudaStream_t s) {
     const int qlp = l + c.nP;
     const long long cps = (long long)qlp << c.log_n;
     const long long mps = (long long)l << c.log_n;
@@ -287,8 +262,10 @@ static void moddown_ntt(const Context &c, const KsBuffers &b, uint64_t *mid, int
         });
     }
     PtrStore ms{mid, mps, c.log_n};
-    ModdownStore<Base> st{out0, out1, k0, b.cx, cps, c.p_inv.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, base};
-    ntt_fwd(c, 2 * nl, QlpMap{nl, k0, l, c.nQ}, PtrLoad{mid, mps, c.log_n}, ms, st, s);
+    ntt_fwd(c, 2 * l, QlpMap{l, 0, l, c.nQ}, PtrLoad{mid, mps, c.log_n}, ms, ms, s);
+    count_launch();
+    moddown_combine<Base><<<grid_for((size_t)l << c.log_n, 256), 256, 0, s>>>(
+            out0, out1, mid, mps, b.cx, cps, c.p_inv.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, l, base);
 }
 
 void ckks_keyswitch(const Context &c, const Workspace &w, uint64_t *ct, const uint64_t *c2, int l,
@@ -298,7 +275,7 @@ void ckks_keyswitch(const Context &c, const Workspace &w, uint64_t *ct, const ui
     modup_ckks(c, b, PtrLoad{c2, lps, c.log_n}, l, s);
     inner_product(c, b, PlainOwn{c2, c.log_n}, l, evk, s);
     moddown_intt_p(c, b, l, s);
-    moddown_ntt(c, b, b.tm, l, 0, l, ct, ct + lps, InplaceBase{ct, lps, c.log_n}, s);
+    moddown_ntt(c, b, b.tm, l, ct, ct + lps, InplaceBase{ct, lps, c.log_n}, s);
 }
 
 void ckks_mul_relin(const Context &c, const Workspace &w, uint64_t *ct1, const uint64_t *ct2, int l,
@@ -310,7 +287,7 @@ void ckks_mul_relin(const Context &c, const Workspace &w, uint64_t *ct1, const u
     inner_product(c, b, TensorOwn{a1, b1, c.log_n}, l, rlk, s);
     moddown_intt_p(c, b, l, s);
     // poly 0 goes to scratch first: poly 1's base still reads a0 at every position
-    moddown_ntt(c, b, b.tm, l, 0, l, b.g, ct1 + lps, TensorBase{ct1, ct2, lps, c.log_n}, s);
+    moddown_ntt(c, b, b.tm, l, b.g, ct1 + lps, TensorBase{ct1, ct2, lps, c.log_n}, s);
     cudaMemcpyAsync(ct1, b.g, lps * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);
 }
 
@@ -411,48 +388,46 @@ struct LastLimbStore {
     }
 };
 
-struct RescaleFusedLoad {
-    const uint64_t *cx;
-    long long cps;
-    const uint64_t *pmat, *pinv, *zc, *zd;
-    const Mod *mods;
-    int log_n, l, nP;
-    __device__ __forceinline__ uint64_t operator()(int t, int j, int tbl, uint32_t idx) const {
-        const Mod m = mods[tbl], ml = mods[l - 1];
-        const uint64_t *yp = cx + t * cps + ((size_t)l << log_n) + idx;
-        const uint64_t *pj = pmat + (size_t)j * nP, *pl = pmat + (size_t)(l - 1) * nP;
-        u128 aj{0, 0}, al{0, 0};
-        for (int k = 0; k < nP; k++) {
-            const uint64_t y = yp[(size_t)k << log_n];
-            mac(aj, y, __ldg(pj + k));
-            mac(al, y, __ldg(pl + k));
+// Final step of HMult + relin + rescale as one coalesced element-wise pass (two coefficients per
+// thread, 16-byte loads): out_t[j] = (d_j + cx_t[j] P^-1 - v_t[j]) q_last^-1, v = the forward NTT
+// of delta_j P^-1 + z, d_0 = a0 b0, d_1 = a0 b1 + a1 b0.  Kept out of the NTT's row pass, whose
+// store sweep would issue these scattered loads only after its butterflies.
+__global__ void __launch_bounds__(256) rescale_combine(uint64_t *out, const uint64_t *v, const uint64_t *cx,
+                                                       long long cps, const uint64_t *a, const uint64_t *b,
+                                                       long long lps, const uint64_t *pinv, const uint64_t *iq,
+                                                       const Mod *mods, int log_n, int lm1) {
+    const size_t half = (size_t)1 << (log_n - 1), per_poly = (size_t)lm1 * half;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * per_poly;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const int t = e >= per_poly;
+        const size_t r = e - t * per_poly;
+        const int j = (int)(r >> (log_n - 1));
+        const size_t o = ((size_t)j << log_n) + 2 * (r & (half - 1));
+        const Mod m = mods[j];
+        const uint64_t pj = pinv[2 * j], pjs = pinv[2 * j + 1], qj = iq[2 * j], qjs = iq[2 * j + 1];
+        const ulonglong2 vv = *reinterpret_cast<const ulonglong2 *>(v + (size_t)t * (lm1 << log_n) + o);
+        const ulonglong2 cc = *reinterpret_cast<const ulonglong2 *>(cx + t * cps + o);
+        const ulonglong2 a0 = *reinterpret_cast<const ulonglong2 *>(a + o);
+        const ulonglong2 b0 = *reinterpret_cast<const ulonglong2 *>(b + o);
+        uint64_t d0, d1;
+        if (t == 0) {
+            d0 = mul_mod(a0.x, b0.x, m);
+            d1 = mul_mod(a0.y, b0.y, m);
+        } else {
+            const ulonglong2 a1 = *reinterpret_cast<const ulonglong2 *>(a + lps + o);
+            const ulonglong2 b1 = *reinterpret_cast<const ulonglong2 *>(b + lps + o);
+            u128 s0 = mul_wide(a0.x, b1.x), s1 = mul_wide(a0.y, b1.y);
+            mac(s0, a1.x, b0.x);
+            mac(s1, a1.y, b0.y);
+            d0 = reduce128(s0, m);
+            d1 = reduce128(s1, m);
         }
-        const size_t o = ((size_t)t << log_n) + idx;
-        const uint64_t dl = reduce128(al, ml);
-        const uint64_t pl_inv = pinv[2 * (l - 1)], pl_inv_s = pinv[2 * (l - 1) + 1];
-        const uint64_t z = add_mod(zd[o], mul_shoup(sub_mod(zc[o], dl, ml.q), pl_inv, pl_inv_s, ml.q), ml.q);
-        const uint64_t dp = mul_shoup(reduce128(aj, m), pinv[2 * j], pinv[2 * j + 1], m.q);
-        return add_mod(dp, reduce64(z, m), m.q);
+        const uint64_t x0 = sub_mod(add_mod(d0, mul_shoup(cc.x, pj, pjs, m.q), m.q), vv.x, m.q);
+        const uint64_t x1 = sub_mod(add_mod(d1, mul_shoup(cc.y, pj, pjs, m.q), m.q), vv.y, m.q);
+        *reinterpret_cast<ulonglong2 *>(out + (size_t)t * (lm1 << log_n) + o) =
+                make_ulonglong2(mul_shoup(x0, qj, qjs, m.q), mul_shoup(x1, qj, qjs, m.q));
     }
-};
-
-struct RescaleFusedStore {
-    uint64_t *out;
-    long long ops;
-    const uint64_t *cx;
-    long long cps;
-    const uint64_t *pinv, *iq;
-    const Mod *mods;
-    int log_n;
-    TensorBase base;
-    __device__ __forceinline__ void operator()(int t, int j, int tbl, uint32_t idx, uint64_t v) const {
-        const Mod m = mods[tbl];
-        const size_t o = ((size_t)j << log_n) + idx;
-        const uint64_t cp = mul_shoup(cx[t * cps + o], pinv[2 * j], pinv[2 * j + 1], m.q);
-        const uint64_t x = sub_mod(add_mod(base(t, j, m, idx), cp, m.q), v, m.q);
-        out[t * ops + o] = mul_shoup(x, iq[2 * j], iq[2 * j + 1], m.q);
-    }
-};
+}
 
 void ckks_mul_relin_rescale(const Context &c, const Workspace &w, const uint64_t *ct1, const uint64_t *ct2,
                             uint64_t *out, int l, const uint64_t *const *rlk, cudaStream_t s) {
@@ -483,9 +458,11 @@ void ckks_mul_relin_rescale(const Context &c, const Workspace &w, const uint64_t
     }
     PtrStore ms{b.tm, ops, c.log_n};
     PtrLoad ld{b.tm, ops, c.log_n};
-    RescaleFusedStore st{out, ops, b.cx, cps, c.p_inv.as<uint64_t>(), lt.inv_qlast.as<uint64_t>(), mods, c.log_n,
-                         tb};
-    ntt_fwd(c, 2 * (l - 1), QlpMap{l - 1, 0, l, c.nQ}, ld, ms, st, s);
+    ntt_fwd(c, 2 * (l - 1), QlpMap{l - 1, 0, l, c.nQ}, ld, ms, ms, s);
+    count_launch();
+    rescale_combine<<<grid_for((size_t)(l - 1) << c.log_n, 256), 256, 0, s>>>(
+            out, b.tm, b.cx, cps, ct1, ct2, lps, c.p_inv.as<uint64_t>(), lt.inv_qlast.as<uint64_t>(), mods, c.log_n,
+            l - 1);
 }
 
 void ckks_tensor(const Context &c, uint64_t *ct1, const uint64_t *ct2, int l, cudaStream_t s);
@@ -512,7 +489,7 @@ void ckks_apply_galois(const Context &c, const Workspace &w, uint64_t *ct, int l
     modup_ckks(c, b, PtrLoad{g1, lps, c.log_n}, l, s);
     inner_product(c, b, PlainOwn{g1, c.log_n}, l, gk, s);
     moddown_intt_p(c, b, l, s);
-    moddown_ntt(c, b, b.tm, l, 0, l, ct, ct + lps, FirstPolyBase{b.g, c.log_n}, s);
+    moddown_ntt(c, b, b.tm, l, ct, ct + lps, FirstPolyBase{b.g, c.log_n}, s);
 }
 
 // ------------------------------------------------------------------ hoisting
@@ -602,7 +579,7 @@ void ckks_hoisting(const Context &c, const Workspace &w, uint64_t *ct, int l, co
                 b.cx, b.tm, c1, hs, c.d_mods.as<Mod>(), c.log_n, l, c.nQ, c.nP, c.beta(l), c.nQ + c.nP, acc);
     }
     moddown_intt_p(c, b, l, s);
-    moddown_ntt(c, b, b.tm, l, 0, l, ct, ct + lps, FirstPolyBase{acc0, c.log_n}, s);
+    moddown_ntt(c, b, b.tm, l, ct, ct + lps, FirstPolyBase{acc0, c.log_n}, s);
 }
 
 // Individual rotations sharing one mod-up of c1 (GB300 addition; the reference's
@@ -629,7 +606,7 @@ void ckks_rotations_hoisted(const Context &c, const Workspace &w, const uint64_t
                 b.cx, b.tm, c1, hs, c.d_mods.as<Mod>(), c.log_n, l, c.nQ, c.nP, c.beta(l), c.nQ + c.nP, false);
         moddown_intt_p(c, b, l, s);
         // the mod-down's scratch must not be tm (it still holds the shared mod-up)
-        moddown_ntt(c, b, b.h, l, 0, l, outs[i], outs[i] + lps, FirstPolyBase{b.g, c.log_n}, s);
+        moddown_ntt(c, b, b.h, l, outs[i], outs[i] + lps, FirstPolyBase{b.g, c.log_n}, s);
     }
 }
 
