@@ -208,21 +208,33 @@ struct BLastStore {
     }
 };
 
-struct BFinalStore {  // out = (d_j + cx_j P^-1 - v) q_last^-1
-    BItemsRef r;
-    const uint64_t *pinv;
-    const Mod *mods;
-    __device__ __forceinline__ void operator()(int poly, int j, int tbl, uint32_t idx, uint64_t v) const {
-        const int c = poly / kSub, t = poly % kSub, lc = r.it.l[c];
-        const Mod m = mods[tbl];
-        const size_t o = ((size_t)j << r.log_n) + idx;
-        const uint64_t cxv = r.it.ws[c][r.sl.cx + t * r.qlp_n(c) + o];
-        const uint64_t cp = mul_shoup(cxv, pinv[2 * j], pinv[2 * j + 1], m.q);
-        const uint64_t x = sub_mod(add_mod(tensor_term(r.it, c, t, j, idx, r.log_n, m), cp, m.q), v, m.q);
-        const uint64_t *iq = r.it.iq[c];
-        r.it.out[c][t * ((long long)(lc - 1) << r.log_n) + o] = mul_shoup(x, iq[2 * j], iq[2 * j + 1], m.q);
+// Final combine of every item, (item, polynomial) = block row: out = (d_j + cx_j P^-1 - v) q_last^-1
+// with v the forward NTT of w (stored plainly in the item's scratch), two coefficients per thread.
+__global__ void __launch_bounds__(256) batch_rescale_combine(BItemsRef r, Prefix pre, const uint64_t *pinv,
+                                                             const Mod *mods) {
+    const int c = pre.find(blockIdx.y), t = blockIdx.y - pre.p[c];
+    const int lc = r.it.l[c], log_n = r.log_n;
+    const size_t half = (size_t)1 << (log_n - 1), work = (size_t)(lc - 1) * half;
+    const uint64_t *ws = r.it.ws[c];
+    const uint64_t *v = ws + r.sl.tm + t * ((long long)(lc - 1) << log_n);
+    const uint64_t *cx = ws + r.sl.cx + t * r.qlp_n(c);
+    const uint64_t *iq = r.it.iq[c];
+    uint64_t *out = r.it.out[c] + t * ((long long)(lc - 1) << log_n);
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < work; e += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(e >> (log_n - 1));
+        const uint32_t idx = (uint32_t)(2 * (e & (half - 1)));
+        const size_t o = ((size_t)j << log_n) + idx;
+        const Mod m = mods[j];
+        const uint64_t pj = pinv[2 * j], pjs = pinv[2 * j + 1], qj = iq[2 * j], qjs = iq[2 * j + 1];
+        const ulonglong2 vv = ld2(v + o), cc = ld2(cx + o);
+        const uint64_t x0 = sub_mod(add_mod(tensor_term(r.it, c, t, j, idx, log_n, m), mul_shoup(cc.x, pj, pjs, m.q), m.q),
+                                    vv.x, m.q);
+        const uint64_t x1 = sub_mod(add_mod(tensor_term(r.it, c, t, j, idx + 1, log_n, m),
+                                            mul_shoup(cc.y, pj, pjs, m.q), m.q),
+                                    vv.y, m.q);
+        st2(out + o, mul_shoup(x0, qj, qjs, m.q), mul_shoup(x1, qj, qjs, m.q));
     }
-};
+}
 
 // ------------------------------------------------------------------ element-wise batch kernels
 
@@ -545,7 +557,10 @@ void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t it
             BFinalMap fm{make_prefix(count, [&](int i) { return 2 * (lvl(i) - 1); }), {}};
             for (int i = 0; i < count; i++) fm.l[i] = lvl(i);
             BScratch<3> w{r};
-            ntt_fwd2(c, fm.pre.p[count], fm, w, w, w, BFinalStore{r, c.p_inv.as<uint64_t>(), mods}, s);
+            ntt_fwd2(c, fm.pre.p[count], fm, w, w, w, w, s);
+            Prefix pre = make_prefix(count, [&](int) { return 2; });
+            count_launch();
+            batch_rescale_combine<<<dim3(gx, pre.p[count]), 256, 0, s>>>(r, pre, c.p_inv.as<uint64_t>(), mods);
         }
     }
 }
