@@ -407,7 +407,12 @@ def run_ours(args):
     t_batch = timed(lambda i: ctx.multiply_relin_rescale_batch(wsb, items, key, stream), kb) / kb
     t_loop = timed(lambda i: [ctx.multiply_relin_rescale(ws, x[0], x[1], x[2], x[3], key, stream) for x in items],
                    kb) / kb
-    del items, wsb
+    # the same 64 levels as a batch of key switches (ct += KeySwitch(c2)), and as single calls
+    ks_items = [(x[0], x[1][1], x[3]) for x in items]  # ct = the first operand, c2 = one poly of the second
+    ctx.keyswitch_batch(wsb, ks_items, key, stream)
+    t_ksb = timed(lambda i: ctx.keyswitch_batch(wsb, ks_items, key, stream), kb) / kb
+    t_ksl = timed(lambda i: [ctx.keyswitch(ws, x[0], x[1], x[2], key, stream) for x in ks_items], kb) / kb
+    del items, ks_items, wsb
 
     # BFV multiply + relinearise (HPS) at N = 2^15, 16x50-bit + 2x60-bit, t = 65537:
     # 128 operations captured in one CUDA graph, replayed
@@ -515,6 +520,8 @@ def run_ours(args):
                       "bfv_n15_ntt_split": btuning["ntt_split"],
                       "batch64_uneven_levels_ops_per_s": 64 * world / t_batch,
                       "batch64_as_single_calls_ops_per_s": 64 * world / t_loop,
+                      "keyswitch_batch64_uneven_levels_per_s": 64 * world / t_ksb,
+                      "keyswitch_batch64_as_single_calls_per_s": 64 * world / t_ksl,
                       "hrotate_step1_per_s": k2 * world / t_rot, "keyswitch_per_s": k2 * world / t_ks,
                       "tensor_core_bconv": tc_default, "tensor_core_status": tc_status,
                       "hmult_relin_rescale_cuda_core_bconv_ops_per_s": k2 * world / t_hm_cc,

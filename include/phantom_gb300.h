@@ -192,6 +192,19 @@ typedef struct fhe_ckks_mul_item {
 int fhe_ckks_multiply_relin_rescale_batch(const fhe_context *ctx, fhe_workspace *ws, const fhe_ckks_mul_item *items,
                                           size_t count, const uint64_t *const *rlk, void *stream);
 
+/* A batch of independent key switches (keyswitch_inplace, src/eval_key_switch.cu:95-182, CKKS,
+ * NTT form) at their own chain indices, sharing one key: items[i].ct (2 polys) += KeySwitch of
+ * items[i].c2 (1 poly).  Every pipeline step is one launch over up to 64 ciphertexts with the
+ * base conversions on the tensor cores; each result equals the single call's word for word.
+ * ws must come from fhe_workspace_create_batch. */
+typedef struct fhe_ks_item {
+    uint64_t *ct;
+    const uint64_t *c2;
+    size_t chain_index;
+} fhe_ks_item;
+int fhe_keyswitch_batch(const fhe_context *ctx, fhe_workspace *ws, const fhe_ks_item *items, size_t count,
+                        const uint64_t *const *evk, void *stream);
+
 /* apply_galois_inplace (include/evaluate.cuh:215, src/evaluate.cu:1567-1630), CKKS:
  * ct (2 polys) <- KeySwitch of the automorphism X -> X^galois_elt under gk. */
 int fhe_apply_galois(const fhe_context *ctx, fhe_workspace *ws, uint64_t *ct, size_t chain_index,

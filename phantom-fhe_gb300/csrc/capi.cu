@@ -421,6 +421,28 @@ int fhe_ckks_multiply_relin_rescale_batch(const fhe_context *ctx, fhe_workspace 
     });
 }
 
+int fhe_keyswitch_batch(const fhe_context *ctx, fhe_workspace *ws, const fhe_ks_item *items, size_t count,
+                        const uint64_t *const *evk, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        pfg::Workspace w = ws_of(ctx, ws);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("batched key switching needs a CKKS context");
+        need_keyswitching(c);
+        need_ptr(items, "items");
+        need_ptr(evk, "evk");
+        if (count == 0) return;
+        if (ws->items < std::min<size_t>(count, pfg::kBatchLaunch))
+            throw std::invalid_argument("workspace has too few ciphertext slots for this batch");
+        std::vector<pfg::KsItem> v;
+        for (size_t i = 0; i < count; i++) {
+            need_ptr(items[i].ct, "items[i].ct");
+            need_ptr(items[i].c2, "items[i].c2");
+            v.push_back(pfg::KsItem{items[i].ct, items[i].c2, level_of(c, items[i].chain_index)});
+        }
+        pfg::ckks_keyswitch_batch(c, w.base, ws->words / ws->items, v, evk, st(stream));
+    });
+}
+
 int galois_index(const pfg::Context &c, uint32_t elt) {
     auto it = std::find(c.galois_elts.begin(), c.galois_elts.end(), elt);
     return it == c.galois_elts.end() ? -1 : (int)(it - c.galois_elts.begin());

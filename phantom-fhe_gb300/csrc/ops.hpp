@@ -29,6 +29,12 @@ struct BatchItem {  // one HMult+relin+rescale of a batch: inputs at level l, ou
 };
 constexpr int kBatchLaunch = 64;  // ciphertexts per launch set (larger batches run in chunks)
 
+struct KsItem {  // one key switch of a batch: ct (2 polys, in place) += KeySwitch(c2), level l
+    uint64_t *ct;
+    const uint64_t *c2;
+    int l;
+};
+
 void ntt_forward(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s);
 void ntt_inverse(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s);
 
@@ -43,6 +49,8 @@ void ckks_mul_relin_rescale(const Context &c, const Workspace &w, const uint64_t
 // Batched HMult + relin + rescale; item i uses scratch ws_base + (i % 64) * item_words.
 void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t item_words,
                                   const std::vector<BatchItem> &items, const uint64_t *const *rlk, cudaStream_t s);
+void ckks_keyswitch_batch(const Context &c, uint64_t *ws_base, size_t item_words, const std::vector<KsItem> &items,
+                          const uint64_t *const *evk, cudaStream_t s);
 void ckks_rescale(const Context &c, const Workspace &w, const uint64_t *in, uint64_t *out, int size, int l,
                   cudaStream_t s);
 void ckks_apply_galois(const Context &c, const Workspace &w, uint64_t *ct, int l, const uint32_t *perm,

@@ -22,6 +22,7 @@ constexpr int kSub = 64;  // "poly" argument of batched functors = item * kSub +
 
 struct BatchItems {
     int count;
+    int keyswitch;  // 0: HMult (c2 = a1 * b1, rescale at the end); 1: key switch of (a = ct, b = c2)
     int l[kMaxBatch];
     const uint64_t *a[kMaxBatch], *b[kMaxBatch];
     uint64_t *out[kMaxBatch];
@@ -96,11 +97,12 @@ struct BLastLimbMap {  // item c, poly t: alpha P limbs, cx limb l-1, tensor lim
     }
 };
 
-struct BFinalMap {  // item c, poly t: limbs [0, l_c - 1)
+struct BFinalMap {  // item c, poly t: limbs [0, l_c - drop)
     Prefix pre;
     int l[kMaxBatch];
+    int drop;
     __device__ __forceinline__ bool operator()(int b, int &poly, int &j, int &tbl) const {
-        const int c = pre.find(b), r = b - pre.p[c], m = l[c] - 1;
+        const int c = pre.find(b), r = b - pre.p[c], m = l[c] - drop;
         const int t = r / m;
         j = r % m;
         poly = c * kSub + t;
@@ -115,7 +117,20 @@ struct BItemsRef {
     BatchItems it;
     ScratchLayout sl;
     int log_n, alpha;
+    int drop;  // limbs the operation drops: 1 (HMult + rescale) or 0 (key switch)
     __device__ __forceinline__ long long qlp_n(int c) const { return (long long)(it.l[c] + alpha) << log_n; }
+};
+
+struct BPMap {  // item c, poly t: the alpha P limbs of cx (key switch: inverse NTT before the mod-down)
+    Prefix pre;
+    int alpha, nQ;
+    __device__ __forceinline__ bool operator()(int b, int &poly, int &k, int &tbl) const {
+        const int c = pre.find(b), r = b - pre.p[c];
+        poly = c * kSub + r / alpha;
+        k = r % alpha;
+        tbl = nQ + k;
+        return true;
+    }
 };
 
 // tensor-product term t of item c at limb j: t = 0: a0*b0, 1: a0*b1 + a1*b0, 2: a1*b1
@@ -132,11 +147,18 @@ __device__ __forceinline__ uint64_t tensor_term(const BatchItems &it, int c, int
     return reduce128(acc, m);
 }
 
-struct BD2Load {  // mod-up inverse NTT input: d2 = a1 * b1
+// the polynomial that is key-switched: HMult's d2 = a1 * b1, or the given c2
+__device__ __forceinline__ uint64_t c2_term(const BatchItems &it, int c, int j, uint32_t idx, int log_n,
+                                            const Mod &m) {
+    if (it.keyswitch) return it.b[c][((size_t)j << log_n) + idx];
+    return tensor_term(it, c, 2, j, idx, log_n, m);
+}
+
+struct BD2Load {  // mod-up inverse NTT input: c2
     BItemsRef r;
     const Mod *mods;
     __device__ __forceinline__ uint64_t operator()(int poly, int k, int tbl, uint32_t idx) const {
-        return tensor_term(r.it, poly / kSub, 2, k, idx, r.log_n, mods[tbl]);
+        return c2_term(r.it, poly / kSub, k, idx, r.log_n, mods[tbl]);
     }
 };
 
@@ -157,9 +179,9 @@ struct BScratch {
         } else if (REGION == 2) {  // tm reused as [2][alpha+2][N]
             off = r.sl.tm;
             ss = (long long)(r.alpha + 2) << r.log_n;
-        } else {  // tm reused as [2][l-1][N]
+        } else {  // tm reused as [2][l - drop][N]
             off = r.sl.tm;
-            ss = (long long)(r.it.l[c] - 1) << r.log_n;
+            ss = (long long)(r.it.l[c] - r.drop) << r.log_n;
         }
         return r.it.ws[c] + off + sub * ss + ((long long)k << r.log_n) + idx;
     }
@@ -207,6 +229,28 @@ struct BLastStore {
         }
     }
 };
+
+// Key-switch combine of every item, (item, polynomial) = block row: ct_t[j] += (cx_t[j] - v) P^-1
+// (keyswitch_inplace's add_to_ct_kernel, src/rns_bconv.cu:763-769), two coefficients per thread.
+__global__ void __launch_bounds__(256) batch_keyswitch_combine(BItemsRef r, Prefix pre, const uint64_t *pinv,
+                                                               const Mod *mods) {
+    const int c = pre.find(blockIdx.y), t = blockIdx.y - pre.p[c];
+    const int lc = r.it.l[c], log_n = r.log_n;
+    const size_t half = (size_t)1 << (log_n - 1), work = (size_t)lc * half;
+    const uint64_t *ws = r.it.ws[c];
+    const uint64_t *v = ws + r.sl.tm + t * ((long long)lc << log_n);
+    const uint64_t *cx = ws + r.sl.cx + t * r.qlp_n(c);
+    uint64_t *ct = r.it.out[c] + t * ((long long)lc << log_n);
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < work; e += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(e >> (log_n - 1));
+        const size_t o = ((size_t)j << log_n) + 2 * (e & (half - 1));
+        const Mod m = mods[j];
+        const uint64_t pj = pinv[2 * j], pjs = pinv[2 * j + 1];
+        const ulonglong2 vv = ld2(v + o), cc = ld2(cx + o), b = ld2(ct + o);
+        st2(ct + o, add_mod(b.x, mul_shoup(sub_mod(cc.x, vv.x, m.q), pj, pjs, m.q), m.q),
+            add_mod(b.y, mul_shoup(sub_mod(cc.y, vv.y, m.q), pj, pjs, m.q), m.q));
+    }
+}
 
 // Final combine of every item, (item, polynomial) = block row: out = (d_j + cx_j P^-1 - v) q_last^-1
 // with v the forward NTT of w (stored plainly in the item's scratch), two coefficients per thread.
@@ -299,8 +343,8 @@ __global__ void __launch_bounds__(256) ks_inner_product_batch(BItemsRef r, const
             for (int d = 0; d < beta; d++) {
                 uint64_t x0, x1;
                 if (d == own_d) {
-                    x0 = tensor_term(r.it, c, 2, jj, (uint32_t)idx, log_n, m);
-                    x1 = tensor_term(r.it, c, 2, jj, (uint32_t)idx + 1, log_n, m);
+                    x0 = c2_term(r.it, c, jj, (uint32_t)idx, log_n, m);
+                    x1 = c2_term(r.it, c, jj, (uint32_t)idx + 1, log_n, m);
                 } else {
                     const ulonglong2 v = ld2(tm + (((size_t)d * qlp + jj) << log_n) + idx);
                     x0 = v.x;
@@ -413,6 +457,24 @@ struct BatchModupSrc {
     }
 };
 
+// Mod-down of a batched key switch (P -> Ql, no rescale): group = (item, polynomial).
+struct BatchModdownSrc {
+    uint64_t *ws[kMaxBatch];
+    const uint16_t *bmat[kMaxBatch];
+    const TcOutMeta *meta[kMaxBatch];
+    int nn[kMaxBatch];
+    int l[kMaxBatch];
+    long long cx_off, tm_off;
+    int alpha, log_n;
+    __device__ __forceinline__ TcGroup operator()(int gidx) const {
+        const int c = gidx >> 1, t = gidx & 1, lc = l[c];
+        uint64_t *w = ws[c];
+        const long long qlp_n = (long long)(lc + alpha) << log_n;
+        return TcGroup{w + cx_off + t * qlp_n + ((size_t)lc << log_n), w + tm_off + t * ((long long)lc << log_n),
+                       bmat[c], meta[c], nullptr, nullptr, alpha, lc, nn[c], lc};
+    }
+};
+
 // Step 6 of a batch (P -> Ql fused with the rescale): group = (item, polynomial).
 struct BatchRescaleSrc {
     uint64_t *ws[kMaxBatch];
@@ -455,6 +517,8 @@ void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t it
         r.sl = scratch_layout(c);
         r.log_n = c.log_n;
         r.alpha = alpha;
+        r.drop = 1;
+        r.it.keyswitch = 0;
         for (int i = 0; i < count; i++) {
             const BatchItem &b = items[base + i];
             const LevelTables &lt = *c.levels[b.l];
@@ -554,13 +618,126 @@ void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t it
         }
         // 7. forward NTT of w with the final combine
         {
-            BFinalMap fm{make_prefix(count, [&](int i) { return 2 * (lvl(i) - 1); }), {}};
+            BFinalMap fm{make_prefix(count, [&](int i) { return 2 * (lvl(i) - 1); }), {}, 1};
             for (int i = 0; i < count; i++) fm.l[i] = lvl(i);
             BScratch<3> w{r};
             ntt_fwd2(c, fm.pre.p[count], fm, w, w, w, w, s);
             Prefix pre = make_prefix(count, [&](int) { return 2; });
             count_launch();
             batch_rescale_combine<<<dim3(gx, pre.p[count]), 256, 0, s>>>(r, pre, c.p_inv.as<uint64_t>(), mods);
+        }
+    }
+}
+
+// Batched key switch (keyswitch_inplace, src/eval_key_switch.cu:95-182, over many ciphertexts at
+// uneven levels with one key): the HMult pipeline with c2 given instead of a1 * b1, the P limbs'
+// inverse NTT alone, the plain mod-down on the tensor cores and an in-place combine.  Without the
+// tensor-core conversions for every level present it runs the single-call key switch per item.
+void ckks_keyswitch_batch(const Context &c, uint64_t *ws_base, size_t item_words, const std::vector<KsItem> &items,
+                          const uint64_t *const *evk, cudaStream_t s) {
+    const Mod *mods = c.d_mods.as<Mod>();
+    const int alpha = c.nP, nQ = c.nQ;
+    const unsigned gx = (unsigned)std::max<uint64_t>(1, c.n / 512);
+    bool tc = c.tc_on;
+    for (const KsItem &k : items) tc = tc && c.levels[k.l]->tc_ok && c.levels[k.l]->tc_moddown_ok;
+    if (!tc) {
+        for (size_t i = 0; i < items.size(); i++)
+            ckks_keyswitch(c, Workspace{ws_base + (i % kMaxBatch) * item_words, item_words}, items[i].ct, items[i].c2,
+                           items[i].l, evk, s);
+        return;
+    }
+    for (size_t base = 0; base < items.size(); base += kMaxBatch) {
+        const int count = (int)std::min<size_t>(kMaxBatch, items.size() - base);
+        BItemsRef r{};
+        r.it.count = count;
+        r.it.keyswitch = 1;
+        r.sl = scratch_layout(c);
+        r.log_n = c.log_n;
+        r.alpha = alpha;
+        r.drop = 0;
+        for (int i = 0; i < count; i++) {
+            const KsItem &k = items[base + i];
+            const LevelTables &lt = *c.levels[k.l];
+            r.it.l[i] = k.l;
+            r.it.a[i] = k.ct;
+            r.it.b[i] = k.c2;
+            r.it.out[i] = k.ct;
+            r.it.ws[i] = ws_base + (size_t)i * item_words;
+            r.it.phi[i] = lt.part_hat_inv.as<uint64_t>();
+            r.it.mat[i] = lt.modup_mat.as<uint64_t>();
+            r.it.iq[i] = nullptr;
+        }
+        auto lvl = [&](int i) { return r.it.l[i]; };
+        auto beta_of = [&](int i) { return c.beta(lvl(i)); };
+        // 1-3. mod-up: inverse NTT of c2 (scaled), tensor-core conversion, forward NTT
+        {
+            Prefix pre = make_prefix(count, lvl);
+            BScratch<0> y{r};
+            ntt_inv2(c, pre.p[count], BSeqMap{pre}, BD2Load{r, mods}, y, y, BScaleYStore{r, mods}, s);
+        }
+        {
+            Prefix pre = make_prefix(count, beta_of);
+            BatchModupSrc src{};
+            src.pre = pre;
+            for (int i = 0; i < count; i++) {
+                const LevelTables &lt = *c.levels[lvl(i)];
+                src.ws[i] = r.it.ws[i];
+                src.bmat[i] = lt.tc_modup.as<uint16_t>();
+                src.meta[i] = lt.tc_modup_meta.as<TcOutMeta>();
+                src.nn[i] = lt.tc_modup_nn.as<int>();
+                src.l[i] = lvl(i);
+            }
+            src.y_off = r.sl.y;
+            src.tm_off = r.sl.tm;
+            src.alpha = alpha;
+            src.log_n = c.log_n;
+            src.kpad = c.tc_kpad;
+            tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, pre.p[count], mods, c.p_inv.as<uint64_t>(),
+                                   c.d_status.as<unsigned>(), s);
+        }
+        {
+            BModupMap mm{make_prefix(count, [&](int i) { return beta_of(i) * (lvl(i) + alpha); }), {}, nQ, alpha};
+            for (int i = 0; i < count; i++) mm.l[i] = lvl(i);
+            BScratch<1> tm{r};
+            ntt_fwd2(c, mm.pre.p[count], mm, tm, tm, tm, tm, s);
+        }
+        // 4. inner product, one block row per key limb
+        count_launch();
+        ks_inner_product_batch<<<dim3(gx, (unsigned)(nQ + alpha)), 256, 0, s>>>(r, evk, mods, nQ, nQ + alpha);
+        // 5. inverse NTT of the P limbs of both cx polynomials, times PHatInv
+        {
+            BPMap pm{make_prefix(count, [&](int) { return 2 * alpha; }), alpha, nQ};
+            BScratch<2> mid{r};
+            ntt_inv2(c, pm.pre.p[count], pm, BLastLoad{r, mods}, mid, mid,
+                     BLastStore{r, c.p_hat_inv.as<uint64_t>(), mods}, s);
+        }
+        // 6. delta = P -> Ql conversion on the tensor cores
+        {
+            BatchModdownSrc src{};
+            for (int i = 0; i < count; i++) {
+                const LevelTables &lt = *c.levels[lvl(i)];
+                src.ws[i] = r.it.ws[i];
+                src.bmat[i] = lt.tc_moddown.as<uint16_t>();
+                src.meta[i] = lt.tc_moddown_meta.as<TcOutMeta>();
+                src.nn[i] = lt.tc_moddown_nn;
+                src.l[i] = lvl(i);
+            }
+            src.cx_off = r.sl.cx;
+            src.tm_off = r.sl.tm;
+            src.alpha = alpha;
+            src.log_n = c.log_n;
+            tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, 2 * count, mods, c.p_inv.as<uint64_t>(),
+                                   c.d_status.as<unsigned>(), s);
+        }
+        // 7. forward NTT of delta, then ct += (cx - NTT(delta)) P^-1
+        {
+            BFinalMap fm{make_prefix(count, [&](int i) { return 2 * lvl(i); }), {}, 0};
+            for (int i = 0; i < count; i++) fm.l[i] = lvl(i);
+            BScratch<3> w{r};
+            ntt_fwd2(c, fm.pre.p[count], fm, w, w, w, w, s);
+            Prefix pre = make_prefix(count, [&](int) { return 2; });
+            count_launch();
+            batch_keyswitch_combine<<<dim3(gx, pre.p[count]), 256, 0, s>>>(r, pre, c.p_inv.as<uint64_t>(), mods);
         }
     }
 }

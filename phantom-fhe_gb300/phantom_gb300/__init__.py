@@ -43,6 +43,10 @@ class _MulItem(ctypes.Structure):
     _fields_ = [("ct1", _vp), ("ct2", _vp), ("out", _vp), ("chain_index", _sz)]
 
 
+class _KsItem(ctypes.Structure):
+    _fields_ = [("ct", _vp), ("c2", _vp), ("chain_index", _sz)]
+
+
 def _load():
     if not os.path.exists(LIB_PATH):
         raise ImportError(f"{LIB_PATH} is not built; run __graft_entry__.build()")
@@ -68,6 +72,7 @@ def _load():
     L.fhe_workspace_destroy.argtypes = [_vp]
     L.fhe_workspace_create_batch.argtypes = [_vp, _sz, ctypes.POINTER(_vp)]
     L.fhe_ckks_multiply_relin_rescale_batch.argtypes = [_vp, _vp, ctypes.POINTER(_MulItem), _sz, _vp, _vp]
+    L.fhe_keyswitch_batch.argtypes = [_vp, _vp, ctypes.POINTER(_KsItem), _sz, _vp, _vp]
     for f in ("fhe_ntt_forward", "fhe_ntt_inverse"):
         getattr(L, f).argtypes = [_vp, _vp, _sz, _sz, _sz, _vp]
     L.fhe_ckks_multiply.argtypes = [_vp, _vp, _vp, _sz, _vp]
@@ -277,6 +282,11 @@ class Context:
         arr = (_MulItem * len(items))(*[_MulItem(t1.data_ptr(), t2.data_ptr(), o.data_ptr(), c)
                                         for t1, t2, o, c in items])
         _check(lib.fhe_ckks_multiply_relin_rescale_batch(self._h, ws._h, arr, len(items), key.ptr, _stream(stream)))
+
+    def keyswitch_batch(self, ws, items, key, stream=None):
+        """items: list of (ct, c2, chain_index); each ct += KeySwitch(c2) in place, uneven levels."""
+        arr = (_KsItem * len(items))(*[_KsItem(ct.data_ptr(), c2.data_ptr(), ci) for ct, c2, ci in items])
+        _check(lib.fhe_keyswitch_batch(self._h, ws._h, arr, len(items), key.ptr, _stream(stream)))
 
     def apply_galois(self, ws, ct, chain_index, elt, key, stream=None):
         _check(lib.fhe_apply_galois(self._h, ws._h, _ptr(ct), chain_index, elt, key.ptr, _stream(stream)))

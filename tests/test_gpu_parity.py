@@ -374,3 +374,42 @@ def test_n16_batch_equals_single_calls(ckks16, pg):
         assert torch.equal(out, single), f"chain {ch}"
     a, b, l = host[0]
     _eq(items[0][2], oc.rescale(l, oc.ckks_mul_relin(l, a, b, key)), "batch item 0 vs oracle")
+
+
+def _ks_batch_case(pg, ctx, mods, chains, seed):
+    rng = np.random.default_rng(seed)
+    key = _key(rng, mods, ctx.dnum, ctx.n)
+    items, host = [], []
+    for ch in chains:
+        l = ctx.level(ch)
+        ct = O.random_residues(rng, mods[:l], ctx.n, 2)
+        c2 = O.random_residues(rng, mods[:l], ctx.n, 1)[0]
+        items.append((pg.to_device(ct), pg.to_device(c2), ch))
+        host.append((ct, c2, l))
+    return key, pg.KeySwitchKey(pg.to_device(key)), items, host
+
+
+def test_keyswitch_batch_uneven_levels(small, pg):
+    ctx, oc, mods, nq, ws = small
+    chains = [1, 5, 3, 2, 4, 1, 6, 3]
+    key, k, items, host = _ks_batch_case(pg, ctx, mods, chains, 95)
+    wsb = ctx.workspace(batch_items=len(chains))
+    ctx.keyswitch_batch(wsb, items, k)
+    for (ct, c2, l), (t, _, ch) in zip(host, items):
+        _eq(t, oc.keyswitch(l, ct, c2, key), f"batched key switch at chain {ch}")
+    assert ctx.device_status() == 0
+
+
+def test_n16_keyswitch_batch_equals_single_calls(ckks16, pg):
+    ctx, oc, mods, nq, ws = ckks16
+    rng_chains = np.random.default_rng(96)
+    chains = [int(31 - x) for x in rng_chains.integers(5, 31, size=10)]  # levels 5..30
+    key, k, items, host = _ks_batch_case(pg, ctx, mods, chains, 97)
+    singles = [t.clone() for t, _, _ in items]
+    wsb = ctx.workspace(batch_items=len(chains))
+    ctx.keyswitch_batch(wsb, items, k)
+    for (t, c2, ch), single in zip(items, singles):
+        ctx.keyswitch(ws, single, c2, ch, k)
+        assert torch.equal(t, single), f"chain {ch}"
+    ct, c2, l = host[0]
+    _eq(items[0][0], oc.keyswitch(l, ct, c2, key), "batched key switch item 0 vs oracle")
