@@ -413,3 +413,36 @@ def test_n16_keyswitch_batch_equals_single_calls(ckks16, pg):
         assert torch.equal(t, single), f"chain {ch}"
     ct, c2, l = host[0]
     _eq(items[0][0], oc.keyswitch(l, ct, c2, key), "batched key switch item 0 vs oracle")
+
+
+def test_n17_max_degree_keyswitch_and_fused(pg):
+    """The largest supported degree (2^17): key switch, HMult+relin+rescale and a rotation."""
+    n = 1 << 17
+    bits = [60, 50, 50, 50, 50, 50, 60, 60]
+    mods = pg.create_coeff_modulus(n, bits)
+    nq = 6
+    ctx = pg.Context(n, mods, 2)
+    oc = O.Context(17, mods, nq, 2)
+    ws = ctx.workspace()
+    rng = np.random.default_rng(170)
+    key = _key(rng, mods, ctx.dnum, n)
+    k = pg.KeySwitchKey(pg.to_device(key))
+    for chain in (1, 4):
+        l = ctx.level(chain)
+        ct = O.random_residues(rng, mods[:l], n, 2)
+        c2 = O.random_residues(rng, mods[:l], n, 1)[0]
+        t = pg.to_device(ct)
+        ctx.keyswitch(ws, t, pg.to_device(c2), chain, k)
+        _eq(t, oc.keyswitch(l, ct, c2, key), f"N=2^17 keyswitch chain {chain}")
+        a = O.random_residues(rng, mods[:l], n, 2)
+        b = O.random_residues(rng, mods[:l], n, 2)
+        out = torch.empty((2, l - 1, n), dtype=torch.int64, device="cuda")
+        ctx.multiply_relin_rescale(ws, pg.to_device(a), pg.to_device(b), out, chain, k)
+        _eq(out, oc.rescale(l, oc.ckks_mul_relin(l, a, b, key)), f"N=2^17 HMult+relin+rescale chain {chain}")
+    elt = pg.elt_from_step(1, n)
+    gks = [k if e == elt else None for e in ctx.galois_elts]
+    ct = O.random_residues(rng, mods[:nq], n, 2)
+    t = pg.to_device(ct)
+    ctx.rotate(ws, t, 1, 1, gks)
+    _eq(t, oc.ckks_apply_galois(nq, ct, elt, key), "N=2^17 rotate by 1")
+    assert ctx.device_status() == 0
