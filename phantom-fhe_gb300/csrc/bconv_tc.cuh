@@ -33,6 +33,11 @@ struct TcGroup {
     const TcOutMeta *meta;
     const uint64_t *zc, *zd;
     int sz, npos, nn, l;
+    // BFV mod-up (coefficient form): inputs are c2 itself; they are copied to `own` (the digit's
+    // own limbs of the mod-up buffer) and scaled by phi (partQlHatInv pairs, moduli from in_tbl0)
+    const uint64_t *phi = nullptr;
+    uint64_t *own = nullptr;
+    int in_tbl0 = 0;
 };
 
 // The tile pipeline; only thread 0 waits on the MMA barrier (bounded), the others sleep in
@@ -174,6 +179,17 @@ __global__ void __launch_bounds__(tc::kPipeThreads, 1)
                 s_bslot[sl] = bslot;
             }
         }
+        if (g.phi) {
+            const size_t n = (size_t)tile_of(i) * tc::kRows + r;
+            if (i0 < g.sz) {
+                g.own[((size_t)i0 << log_n) + n] = ya;
+                ya = mul_shoup(ya, g.phi[2 * i0], g.phi[2 * i0 + 1], mods[g.in_tbl0 + i0].q);
+            }
+            if (i0 + 4 < g.sz) {
+                g.own[((size_t)(i0 + 4) << log_n) + n] = yb;
+                yb = mul_shoup(yb, g.phi[2 * (i0 + 4)], g.phi[2 * (i0 + 4) + 1], mods[g.in_tbl0 + i0 + 4].q);
+            }
+        }
         uint8_t *a = sA + (i & 1) * ABYTES + (r & 7) * 16 + (r >> 3) * SBO;
         if (i0 < KC) *reinterpret_cast<uint4 *>(a + i0 * 128) = i0 < g.sz ? tc::bytes_bf16(ya) : make_uint4(0, 0, 0, 0);
         if (i0 + 4 < KC)
@@ -244,6 +260,26 @@ struct ModupSrc {
         const int s0 = d * alpha, sz = min(alpha, l - s0), qlp = l + alpha;
         return TcGroup{y + ((size_t)s0 << log_n), tm + (((size_t)d * qlp) << log_n), bmat + (size_t)d * 256 * kpad,
                        meta + d * tc::kMaxOut, nullptr, nullptr, sz, qlp - sz, nn[d], l};
+    }
+};
+
+// BFV mod-up of c2 (coefficient form): group = digit d; own limbs copied, inputs scaled in the fill.
+struct BfvModupSrc {
+    const uint64_t *c2;
+    uint64_t *tm;
+    const uint16_t *bmat;
+    const TcOutMeta *meta;
+    const int *nn;
+    const uint64_t *phi;  // partQlHatInv pairs per limb
+    int l, alpha, log_n, kpad;
+    __device__ __forceinline__ TcGroup operator()(int d) const {
+        const int s0 = d * alpha, sz = min(alpha, l - s0), qlp = l + alpha;
+        TcGroup g{c2 + ((size_t)s0 << log_n), tm + (((size_t)d * qlp) << log_n), bmat + (size_t)d * 256 * kpad,
+                  meta + d * tc::kMaxOut, nullptr, nullptr, sz, qlp - sz, nn[d], l};
+        g.phi = phi + 2 * s0;
+        g.own = tm + (((size_t)d * qlp + s0) << log_n);
+        g.in_tbl0 = s0;
+        return g;
     }
 };
 

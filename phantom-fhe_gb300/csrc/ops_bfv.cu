@@ -16,6 +16,7 @@
 #include <string>
 
 #include "bconv.cuh"
+#include "bconv_tc.cuh"
 #include "hps_tc.cuh"
 #include "keyswitch.cuh"
 #include "launch.cuh"
@@ -228,12 +229,20 @@ static void bfv_keyswitch_to(const Context &c, uint64_t *scratch, uint64_t *out,
     uint64_t *tm = scratch;
     uint64_t *cx = tm + ((size_t)beta * qlp << c.log_n);
     const long long tps = (long long)qlp << c.log_n;
-    with_digit_bound(alpha, [&]<int A>() {
-        count_launch();
-        modup_bconv<A, true><<<dim3((unsigned)std::max<uint64_t>(1, c.n / 512), beta), 256, 0, s>>>(
-                tm, c2, lt.part_hat_inv.as<uint64_t>(), lt.modup_mat.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, l,
-                c.nQ, alpha);
-    });
+    // with two or fewer limbs per digit the CUDA-core conversion is as fast (measured at alpha = 2)
+    if (c.tc_on && lt.tc_ok && alpha >= 3) {
+        const BfvModupSrc src{c2, tm, lt.tc_modup.as<uint16_t>(), lt.tc_modup_meta.as<TcOutMeta>(),
+                              lt.tc_modup_nn.as<int>(), lt.part_hat_inv.as<uint64_t>(), l, alpha, c.log_n, c.tc_kpad};
+        tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, beta, c.d_mods.as<Mod>(), c.p_inv.as<uint64_t>(),
+                               c.d_status.as<unsigned>(), s);
+    } else {
+        with_digit_bound(alpha, [&]<int A>() {
+            count_launch();
+            modup_bconv<A, true><<<dim3((unsigned)std::max<uint64_t>(1, c.n / 512), beta), 256, 0, s>>>(
+                    tm, c2, lt.part_hat_inv.as<uint64_t>(), lt.modup_mat.as<uint64_t>(), c.d_mods.as<Mod>(),
+                    c.log_n, l, c.nQ, alpha);
+        });
+    }
     PtrStore ts{tm, tps, c.log_n};
     ntt_fwd(c, beta * qlp, ModupMap{qlp, l, c.nQ, alpha, false}, PtrLoad{tm, tps, c.log_n}, ts, ts, s);
     const size_t work = ((size_t)qlp << c.log_n) / 2;

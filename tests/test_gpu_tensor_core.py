@@ -93,6 +93,7 @@ BFV_PARAMS = {
     "bfv_n12_4x50": (4096, [50, 50, 50, 50, 60, 60], 2, 65537),
     "bfv_n15_16x50": (32768, [50] * 16 + [60, 60], 2, 65537),
     "bfv_n13_6x40": (8192, [40] * 6 + [60], 1, 786433),
+    "bfv_n13_a3": (8192, [50] * 6 + [60] * 3, 3, 65537),  # key switch mod-up on the tensor cores
 }
 
 
