@@ -7,8 +7,15 @@
 //   PhantomCiphertext with the same save/load byte format           (include/ciphertext.h:7-308)
 //   PhantomRelinKey / PhantomGaloisKey load/save, public_keys_ptr()  (include/secretkey.h:102-219)
 //   phantom:: multiply_inplace, multiply_and_relin_inplace, relinearize_inplace, rescale_to_next(_inplace),
-//   mod_switch_to_next_inplace, apply_galois_inplace, rotate_inplace, hoisting_inplace, keyswitch_inplace
-//                                                                   (include/evaluate.cuh:12-246)
+//   mod_switch_to_next_inplace, apply_galois_inplace, rotate_inplace, hoisting_inplace, keyswitch_inplace,
+//   multiply_plain(_inplace), add(_inplace)                         (include/evaluate.cuh:12-246)
+//   PhantomPlaintext (CKKS, NTT form)                               (include/plaintext.h)
+//   PhantomCKKSEncoder encode / decode                              (include/ckks.h:88-150)
+//   PhantomSecretKey: gen_relinkey, create_galois_keys, encrypt_symmetric, decrypt (CKKS)
+//                                                                   (include/secretkey.h:276-330)
+// Randomness for keys and encryption comes from a host std::mt19937_64 (seeded from
+// std::random_device unless a seed is given) instead of the reference's device Salsa20; the
+// arithmetic runs on the GPU through the C ABI.
 // Device memory is owned as in the reference: cudaMallocAsync / cudaFreeAsync on
 // cudaStreamPerThread, and every evaluator call enqueues on cudaStreamPerThread.  Errors are
 // thrown as std::invalid_argument / std::logic_error with the library's message.
@@ -16,8 +23,12 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <bitset>
 #include <cmath>
+#include <complex>
 #include <cstdint>
+#include <random>
 #include <istream>
 #include <map>
 #include <memory>
@@ -314,6 +325,24 @@ public:
     }
     [[nodiscard]] std::size_t dnum() const noexcept { return keys_.size(); }
 
+    // Takes a generated key [dnum][2][QP][N] (device) as dnum size-2 ciphertexts at chain index 0.
+    void assign(const PhantomContext &context, const std::uint64_t *key, std::size_t dnum) {
+        keys_.clear();
+        keys_.resize(dnum);
+        const std::size_t words = 2 * context.coeff_modulus_size(0) * context.poly_modulus_degree();
+        std::vector<std::uint64_t> p(dnum);
+        for (std::size_t d = 0; d < dnum; d++) {
+            keys_[d].resize(context, 0, 2);
+            phantom::detail::cuda_check(cudaMemcpyAsync(keys_[d].data(), key + d * words, words * 8,
+                                                        cudaMemcpyDeviceToDevice, cudaStreamPerThread));
+            p[d] = reinterpret_cast<std::uint64_t>(keys_[d].data());
+        }
+        ptrs_.reset(dnum);
+        phantom::detail::cuda_check(
+                cudaMemcpyAsync(ptrs_.get(), p.data(), dnum * 8, cudaMemcpyHostToDevice, cudaStreamPerThread));
+        phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
+    }
+
     void save(std::ostream &os) const {
         const std::size_t dnum = keys_.size();
         os.write(reinterpret_cast<const char *>(&dnum), sizeof(std::size_t));
@@ -360,6 +389,7 @@ public:
         relin_keys_.resize(n);
         for (auto &k : relin_keys_) k.load(is);
     }
+    void push_back(PhantomRelinKey &&k) { relin_keys_.push_back(std::move(k)); }
     // host array of the per-element digit-pointer arrays, for fhe_rotate / fhe_hoisting
     [[nodiscard]] std::vector<const std::uint64_t *const *> key_table() const {
         std::vector<const std::uint64_t *const *> t;
@@ -369,6 +399,262 @@ public:
 
 private:
     std::vector<PhantomRelinKey> relin_keys_;
+};
+
+// CKKS plaintext in NTT form: [limbs][N] at a chain index, with its scale (include/plaintext.h).
+class PhantomPlaintext {
+public:
+    PhantomPlaintext() = default;
+    void resize(const PhantomContext &context, std::size_t chain_index) {
+        limbs_ = context.coeff_modulus_size(chain_index);
+        n_ = context.poly_modulus_degree();
+        chain_index_ = chain_index;
+        if (data_.size() != limbs_ * n_) data_.reset(limbs_ * n_);
+    }
+    [[nodiscard]] std::uint64_t *data() const noexcept { return data_.get(); }
+    [[nodiscard]] std::size_t chain_index() const noexcept { return chain_index_; }
+    [[nodiscard]] std::size_t coeff_modulus_size() const noexcept { return limbs_; }
+    [[nodiscard]] std::size_t poly_modulus_degree() const noexcept { return n_; }
+    [[nodiscard]] double scale() const noexcept { return scale_; }
+    void set_scale(double s) noexcept { scale_ = s; }
+    void set_chain_index(std::size_t c) noexcept { chain_index_ = c; }
+
+private:
+    std::size_t chain_index_ = 0, limbs_ = 0, n_ = 0;
+    double scale_ = 1.0;
+    PhantomDeviceBuffer data_;
+};
+
+namespace phantom::detail {
+// In-place radix-2 complex FFT of a power-of-two length: a_k <- sum_j a_j exp(sign * 2 pi i j k / len)
+// (iterative Cooley-Tukey, bit-reversal permutation first).
+inline void fft(std::vector<std::complex<double>> &a, int sign) {
+    const std::size_t len = a.size();
+    for (std::size_t i = 1, j = 0; i < len; i++) {
+        std::size_t bit = len >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) std::swap(a[i], a[j]);
+    }
+    const double pi = std::acos(-1.0);
+    for (std::size_t h = 1; h < len; h <<= 1) {
+        for (std::size_t k = 0; k < h; k++) {
+            const std::complex<double> w = std::polar(1.0, sign * pi * (double)k / (double)h);
+            for (std::size_t s = 0; s < len; s += 2 * h) {
+                const std::complex<double> u = a[s + k], v = a[s + k + h] * w;
+                a[s + k] = u + v;
+                a[s + k + h] = u - v;
+            }
+        }
+    }
+}
+}  // namespace phantom::detail
+
+// CKKS canonical embedding (PhantomCKKSEncoder, include/ckks.h:88-150): slot i of a plaintext
+// holds m(zeta^(5^i mod 2N)) / scale, zeta = exp(i pi / N), i < N / 2.  The embedding runs in FP64
+// on the host (one length-2N FFT); residues and the NTT run on the GPU.  decode reads the
+// plaintext's first limb, so the message must stay below q_0 / 2 in magnitude.
+class PhantomCKKSEncoder {
+public:
+    explicit PhantomCKKSEncoder(const PhantomContext &context) : n_(context.poly_modulus_degree()) {
+        group_.resize(n_ / 2);
+        std::uint64_t pos = 1;
+        for (std::size_t i = 0; i < n_ / 2; i++) {
+            group_[i] = pos;
+            pos = (pos * 5) % (2 * n_);
+        }
+    }
+    [[nodiscard]] std::size_t slot_count() const noexcept { return n_ / 2; }
+
+    void encode(const PhantomContext &context, const std::vector<std::complex<double>> &values, double scale,
+                PhantomPlaintext &destination, std::size_t chain_index = 1) const {
+        if (values.empty() || values.size() > n_ / 2) throw std::invalid_argument("need 1..N/2 slot values");
+        if (scale <= 0) throw std::invalid_argument("scale out of bounds");
+        std::vector<std::complex<double>> w(2 * n_);
+        for (std::size_t i = 0; i < values.size(); i++) w[group_[i]] = values[i];
+        phantom::detail::fft(w, -1);  // sum_i z_i zeta^(-g_i k)
+        destination.resize(context, chain_index);
+        const std::size_t limbs = destination.coeff_modulus_size();
+        std::vector<std::uint64_t> res(limbs * n_);
+        for (std::size_t k = 0; k < n_; k++) {
+            const double c = std::nearbyint(w[k].real() * (2.0 * scale / (double)n_));
+            if (!(std::fabs(c) < 4.6e18)) throw std::invalid_argument("encoded values are too large");
+            const auto v = static_cast<std::int64_t>(c);
+            for (std::size_t j = 0; j < limbs; j++) {
+                const auto q = static_cast<std::int64_t>(context.modulus(j));
+                std::int64_t r = v % q;
+                res[j * n_ + k] = static_cast<std::uint64_t>(r < 0 ? r + q : r);
+            }
+        }
+        phantom::detail::cuda_check(cudaMemcpyAsync(destination.data(), res.data(), res.size() * 8,
+                                                    cudaMemcpyHostToDevice, cudaStreamPerThread));
+        phantom::detail::check(fhe_ntt_forward(context.handle(), destination.data(), 1, limbs, 0, cudaStreamPerThread));
+        phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
+        destination.set_scale(scale);
+    }
+    void encode(const PhantomContext &context, const std::vector<double> &values, double scale,
+                PhantomPlaintext &destination, std::size_t chain_index = 1) const {
+        encode(context, std::vector<std::complex<double>>(values.begin(), values.end()), scale, destination,
+               chain_index);
+    }
+    template <class T>
+    [[nodiscard]] PhantomPlaintext encode(const PhantomContext &context, const std::vector<T> &values, double scale,
+                                          std::size_t chain_index = 1) const {
+        PhantomPlaintext p;
+        encode(context, values, scale, p, chain_index);
+        return p;
+    }
+
+    void decode(const PhantomContext &context, const PhantomPlaintext &plain,
+                std::vector<std::complex<double>> &destination) const {
+        const std::size_t limbs = plain.coeff_modulus_size();
+        PhantomDeviceBuffer t(limbs * n_);
+        phantom::detail::cuda_check(cudaMemcpyAsync(t.get(), plain.data(), limbs * n_ * 8, cudaMemcpyDeviceToDevice,
+                                                    cudaStreamPerThread));
+        phantom::detail::check(fhe_ntt_inverse(context.handle(), t.get(), 1, limbs, 0, cudaStreamPerThread));
+        std::vector<std::uint64_t> limb0(n_);
+        phantom::detail::cuda_check(
+                cudaMemcpyAsync(limb0.data(), t.get(), n_ * 8, cudaMemcpyDeviceToHost, cudaStreamPerThread));
+        phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
+        const std::uint64_t q = context.modulus(0);
+        std::vector<std::complex<double>> c(2 * n_);
+        for (std::size_t k = 0; k < n_; k++)
+            c[k] = limb0[k] > q / 2 ? -(double)(q - limb0[k]) : (double)limb0[k];
+        phantom::detail::fft(c, +1);  // v_j = sum_k c_k zeta^(j k)
+        destination.resize(n_ / 2);
+        for (std::size_t i = 0; i < n_ / 2; i++) destination[i] = c[group_[i]] / plain.scale();
+    }
+    void decode(const PhantomContext &context, const PhantomPlaintext &plain, std::vector<double> &destination) const {
+        std::vector<std::complex<double>> z;
+        decode(context, plain, z);
+        destination.resize(z.size());
+        for (std::size_t i = 0; i < z.size(); i++) destination[i] = z[i].real();
+    }
+    template <class T>
+    [[nodiscard]] std::vector<T> decode(const PhantomContext &context, const PhantomPlaintext &plain) const {
+        std::vector<T> d;
+        decode(context, plain, d);
+        return d;
+    }
+
+private:
+    std::size_t n_;
+    std::vector<std::uint64_t> group_;  // 5^i mod 2N
+};
+
+// Secret key (PhantomSecretKey, include/secretkey.h:276-330) for CKKS: uniform ternary s, the
+// reference's key and encryption formulas on the GPU, randomness from a host generator (uniform
+// a, centred binomial e: popcount of 21 bits minus popcount of 21 bits, as src/prng.cu:222-244).
+class PhantomSecretKey {
+public:
+    explicit PhantomSecretKey(const PhantomContext &context, std::uint64_t seed = std::random_device{}())
+        : rng_(seed) {
+        const std::size_t n = context.poly_modulus_degree(), qp = context.coeff_modulus_size(0);
+        std::uniform_int_distribution<int> tern(-1, 1);
+        std::vector<std::int64_t> s(n);
+        for (auto &v : s) v = tern(rng_);
+        std::vector<std::uint64_t> res(qp * n);
+        for (std::size_t j = 0; j < qp; j++) {
+            const std::uint64_t q = context.modulus(j);
+            for (std::size_t k = 0; k < n; k++) res[j * n + k] = s[k] < 0 ? q - 1 : (std::uint64_t)s[k];
+        }
+        s_ntt_.reset(qp * n);
+        phantom::detail::cuda_check(
+                cudaMemcpyAsync(s_ntt_.get(), res.data(), res.size() * 8, cudaMemcpyHostToDevice, cudaStreamPerThread));
+        phantom::detail::check(fhe_ntt_forward(context.handle(), s_ntt_.get(), 1, qp, 0, cudaStreamPerThread));
+        phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
+    }
+    PhantomSecretKey(const PhantomSecretKey &) = delete;
+    PhantomSecretKey &operator=(const PhantomSecretKey &) = delete;
+
+    [[nodiscard]] PhantomRelinKey gen_relinkey(const PhantomContext &context) { return kswitch_key(context, 0); }
+
+    [[nodiscard]] PhantomGaloisKey create_galois_keys(const PhantomContext &context) {
+        PhantomGaloisKey g;
+        for (std::uint32_t elt : context.galois_elts()) g.push_back(kswitch_key(context, elt));
+        return g;
+    }
+
+    void encrypt_symmetric(const PhantomContext &context, const PhantomPlaintext &plain,
+                           PhantomCiphertext &cipher) const {
+        const std::size_t n = context.poly_modulus_degree(), l = plain.coeff_modulus_size();
+        std::vector<std::uint64_t> a = uniform(context, 1, l);
+        std::vector<std::int64_t> e = error(1, n);
+        PhantomDeviceBuffer da(a.size()), de(e.size());
+        upload(da, a.data(), a.size());
+        upload(de, e.data(), e.size());
+        cipher.resize(context, plain.chain_index(), 2);
+        phantom::detail::check(fhe_ckks_encrypt_symmetric(context.handle(), plain.data(), s_ntt_.get(), da.get(),
+                                                          reinterpret_cast<const std::int64_t *>(de.get()),
+                                                          cipher.data(), plain.chain_index(), cudaStreamPerThread));
+        phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
+        cipher.set_scale(plain.scale());
+        cipher.set_ntt_form(true);
+    }
+    [[nodiscard]] PhantomCiphertext encrypt_symmetric(const PhantomContext &context,
+                                                      const PhantomPlaintext &plain) const {
+        PhantomCiphertext c;
+        encrypt_symmetric(context, plain, c);
+        return c;
+    }
+
+    void decrypt(const PhantomContext &context, const PhantomCiphertext &cipher, PhantomPlaintext &plain) {
+        if (cipher.size() != 2) throw std::invalid_argument("decrypt needs a size-2 ciphertext");
+        plain.resize(context, cipher.chain_index());
+        phantom::detail::check(fhe_ckks_decrypt(context.handle(), cipher.data(), s_ntt_.get(), plain.data(),
+                                                cipher.chain_index(), cudaStreamPerThread));
+        plain.set_scale(cipher.scale());
+    }
+    [[nodiscard]] PhantomPlaintext decrypt(const PhantomContext &context, const PhantomCiphertext &cipher) {
+        PhantomPlaintext p;
+        decrypt(context, cipher, p);
+        return p;
+    }
+
+private:
+    static void upload(PhantomDeviceBuffer &d, const void *h, std::size_t words) {
+        phantom::detail::cuda_check(cudaMemcpyAsync(d.get(), h, words * 8, cudaMemcpyHostToDevice, cudaStreamPerThread));
+        phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
+    }
+    std::vector<std::uint64_t> uniform(const PhantomContext &context, std::size_t polys, std::size_t limbs) const {
+        const std::size_t n = context.poly_modulus_degree();
+        std::vector<std::uint64_t> v(polys * limbs * n);
+        for (std::size_t p = 0; p < polys; p++)
+            for (std::size_t j = 0; j < limbs; j++) {
+                std::uniform_int_distribution<std::uint64_t> u(0, context.modulus(j) - 1);
+                for (std::size_t k = 0; k < n; k++) v[(p * limbs + j) * n + k] = u(rng_);
+            }
+        return v;
+    }
+    std::vector<std::int64_t> error(std::size_t polys, std::size_t n) const {
+        std::vector<std::int64_t> e(polys * n);
+        for (auto &x : e) {
+            const std::uint64_t r = rng_();
+            x = (std::int64_t)std::bitset<21>(r & 0x1FFFFFull).count() -
+                (std::int64_t)std::bitset<21>((r >> 21) & 0x1FFFFFull).count();
+        }
+        return e;
+    }
+    PhantomRelinKey kswitch_key(const PhantomContext &context, std::uint32_t elt) {
+        const std::size_t n = context.poly_modulus_degree(), qp = context.coeff_modulus_size(0);
+        std::size_t nq, np, nr, dnum;
+        std::uint64_t nn;
+        phantom::detail::check(fhe_context_sizes(context.handle(), &nn, &nq, &np, &nr, &dnum));
+        std::vector<std::uint64_t> a = uniform(context, dnum, qp);
+        std::vector<std::int64_t> e = error(dnum, n);
+        PhantomDeviceBuffer da(a.size()), de(e.size()), key(dnum * 2 * qp * n);
+        upload(da, a.data(), a.size());
+        upload(de, e.data(), e.size());
+        phantom::detail::check(fhe_kswitch_keygen(context.handle(), context.workspace(), elt, s_ntt_.get(), da.get(),
+                                                  reinterpret_cast<const std::int64_t *>(de.get()), key.get(),
+                                                  cudaStreamPerThread));
+        PhantomRelinKey k;
+        k.assign(context, key.get(), dnum);
+        return k;
+    }
+
+    mutable std::mt19937_64 rng_;
+    PhantomDeviceBuffer s_ntt_;  // [QP][N], NTT form
 };
 
 namespace phantom {
@@ -504,6 +790,40 @@ inline void hoisting_inplace(const PhantomContext &context, PhantomCiphertext &c
     const auto table = glk.key_table();
     detail::check(fhe_hoisting(context.handle(), context.workspace(), ct.data(), ct.chain_index(), steps.data(),
                                steps.size(), table.data(), cudaStreamPerThread));
+}
+
+// multiply_plain_inplace (include/evaluate.cuh:94, src/evaluate.cu:1224-1250, CKKS NTT form)
+inline void multiply_plain_inplace(const PhantomContext &context, PhantomCiphertext &encrypted,
+                                   const PhantomPlaintext &plain) {
+    if (encrypted.chain_index() != plain.chain_index()) throw std::invalid_argument("encrypted and plain parameter mismatch");
+    if (encrypted.size() != 2) throw std::invalid_argument("multiply_plain needs a size-2 ciphertext");
+    detail::check(fhe_ckks_multiply_plain(context.handle(), encrypted.data(), plain.data(), encrypted.data(),
+                                          encrypted.chain_index(), cudaStreamPerThread));
+    encrypted.set_scale(encrypted.scale() * plain.scale());
+}
+
+inline PhantomCiphertext multiply_plain(const PhantomContext &context, const PhantomCiphertext &encrypted,
+                                        const PhantomPlaintext &plain) {
+    PhantomCiphertext d = encrypted;
+    multiply_plain_inplace(context, d, plain);
+    return d;
+}
+
+// add_inplace (include/evaluate.cuh:46, src/evaluate.cu:116-198)
+inline void add_inplace(const PhantomContext &context, PhantomCiphertext &encrypted1,
+                        const PhantomCiphertext &encrypted2) {
+    detail::same_level(encrypted1, encrypted2);
+    if (encrypted1.size() != encrypted2.size()) throw std::invalid_argument("ciphertext sizes mismatch");
+    if (!detail::same_scale(encrypted1.scale(), encrypted2.scale())) throw std::invalid_argument("scale mismatch");
+    detail::check(fhe_ckks_add(context.handle(), encrypted1.data(), encrypted2.data(), encrypted1.data(),
+                               encrypted1.size(), encrypted1.chain_index(), cudaStreamPerThread));
+}
+
+inline PhantomCiphertext add(const PhantomContext &context, const PhantomCiphertext &encrypted1,
+                             const PhantomCiphertext &encrypted2) {
+    PhantomCiphertext d = encrypted1;
+    add_inplace(context, d, encrypted2);
+    return d;
 }
 
 }  // namespace phantom

@@ -2,7 +2,10 @@
 // program does: parameters, context, ciphertexts and keys loaded from streams in the
 // reference's byte format, evaluator calls, results saved in the same format.
 // Usage: compat_main <dir>   (reads a.bin b.bin rlk.bin gk.bin, writes out_*.bin)
+#include <complex>
+#include <cstdlib>
 #include <fstream>
+#include <random>
 #include <iostream>
 #include <sstream>
 #include <string>
@@ -87,6 +90,49 @@ int main(int argc, char **argv) {
         std::cerr << "expected std::invalid_argument for a chain-index mismatch\n";
         return 1;
     }
+    // end to end as in the reference's CKKS examples: keys, encode, encrypt, evaluate, decrypt, decode
+    {
+        PhantomCKKSEncoder encoder(context);
+        PhantomSecretKey sk(context, 42);
+        PhantomRelinKey rk = sk.gen_relinkey(context);
+        PhantomGaloisKey gks = sk.create_galois_keys(context);
+        const double scale = std::pow(2.0, 40);
+        const std::size_t slots = encoder.slot_count();
+        std::mt19937_64 g(7);
+        std::uniform_real_distribution<double> u(-0.7, 0.7);
+        std::vector<std::complex<double>> x(slots), y(slots);
+        for (std::size_t i = 0; i < slots; i++) {
+            x[i] = {u(g), u(g)};
+            y[i] = {u(g), u(g)};
+        }
+        PhantomPlaintext px = encoder.encode(context, x, scale), py = encoder.encode(context, y, scale);
+        PhantomCiphertext cx = sk.encrypt_symmetric(context, px), cy = sk.encrypt_symmetric(context, py);
+        double err = 0;
+        auto check = [&](const PhantomCiphertext &c, auto want, const char *what) {
+            PhantomPlaintext p = sk.decrypt(context, c);
+            std::vector<std::complex<double>> z = encoder.decode<std::complex<double>>(context, p);
+            double e = 0;
+            for (std::size_t i = 0; i < slots; i++) e = std::max(e, std::abs(z[i] - want(i)));
+            if (!(e < 1e-3)) {
+                std::cerr << what << ": max slot error " << e << "\n";
+                std::exit(1);
+            }
+            err = std::max(err, e);
+        };
+        check(cx, [&](std::size_t i) { return x[i]; }, "encrypt/decrypt");
+        PhantomCiphertext prod = multiply_and_relin(context, cx, cy, rk);
+        rescale_to_next_inplace(context, prod);
+        check(prod, [&](std::size_t i) { return x[i] * y[i]; }, "multiply_and_relin + rescale");
+        rotate_inplace(context, prod, 1, gks);
+        check(prod, [&](std::size_t i) { return x[(i + 1) % slots] * y[(i + 1) % slots]; }, "rotate by 1");
+        PhantomCiphertext mp = multiply_plain(context, cx, py);
+        rescale_to_next_inplace(context, mp);
+        check(mp, [&](std::size_t i) { return x[i] * y[i]; }, "multiply_plain + rescale");
+        PhantomCiphertext sum = add(context, cx, cy);
+        check(sum, [&](std::size_t i) { return x[i] + y[i]; }, "add");
+        std::cout << "ckks end to end max slot error " << err << "\n";
+    }
+
     cudaDeviceSynchronize();
     std::cout << "compat ok\n";
     return 0;

@@ -79,6 +79,7 @@ def test_cpp_layer_matches_oracle(compat_bin, tmp_path):
     r = subprocess.run([str(compat_bin), str(tmp_path)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert "compat ok" in r.stdout
+    assert "ckks end to end max slot error" in r.stdout  # keys, encode, encrypt, evaluate, decrypt, decode
 
     chain, scale, got = read_ct(tmp_path / "out_mul_rescale.bin")
     assert chain == 2 and scale == 2.0 ** 80 / mods[l - 1]
