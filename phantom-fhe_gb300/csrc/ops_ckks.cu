@@ -27,6 +27,7 @@
 #include "bconv_tc.cuh"
 #include "keyswitch.cuh"
 #include "launch.cuh"
+#include "ntt_small.cuh"
 #include "ops.hpp"
 
 namespace pfg {
@@ -52,29 +53,23 @@ size_t workspace_words(const Context &c) {
 
 // ------------------------------------------------------------------ NTT entry points
 
-// N = 2^12: one CTA holds a whole limb (16 coefficients per thread), so the transform is a
-// single pass — the row-pass kernel with the full length as its vector and no column stages.
+// N = 2^12 (batch-1 latency): one cluster of 8 CTAs per limb (ntt_small.cuh).
 template <bool FWD>
-static void ntt_single_pass_n12(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s) {
-    const long long ps = (long long)limbs << c.log_n;
-    NttTables T = c.ntt();
-    T.l1 = 0;
-    T.l2 = 12;
+static void ntt_n12_launch(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s) {
     count_launch();
-    PtrStore st{data, ps, c.log_n};
-    ntt_row_pass<12, FWD, true><<<dim3(1, (unsigned)(polys * limbs)), kNttThreads, 0, s>>>(
-            T, SeqMap{limbs, start}, PtrLoad{data, ps, c.log_n}, st);
+    ntt_n12<FWD><<<(unsigned)(polys * limbs * kSmallCluster), kSmallThreads, 0, s>>>(
+            data, (long long)limbs << c.log_n, limbs, start, c.ntt());
 }
 
 void ntt_forward(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s) {
-    if (c.log_n == 12) return ntt_single_pass_n12<true>(c, data, polys, limbs, start, s);
+    if (c.log_n == 12) return ntt_n12_launch<true>(c, data, polys, limbs, start, s);
     const long long ps = (long long)limbs << c.log_n;
     PtrStore st{data, ps, c.log_n};
     ntt_fwd(c, polys * limbs, SeqMap{limbs, start}, PtrLoad{data, ps, c.log_n}, st, st, s);
 }
 
 void ntt_inverse(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s) {
-    if (c.log_n == 12) return ntt_single_pass_n12<false>(c, data, polys, limbs, start, s);
+    if (c.log_n == 12) return ntt_n12_launch<false>(c, data, polys, limbs, start, s);
     const long long ps = (long long)limbs << c.log_n;
     PtrStore st{data, ps, c.log_n};
     ntt_inv(c, polys * limbs, SeqMap{limbs, start}, PtrLoad{data, ps, c.log_n}, st, st, s);
