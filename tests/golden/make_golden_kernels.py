@@ -1,0 +1,528 @@
+"""Golden vectors from PhantomFHE's own CUDA kernels, for pinning the oracle.
+
+TEST INFRASTRUCTURE ONLY.  Needs a GPU, torch, the oracle (for its tables, which
+tests/test_oracle.py pins to the reference's host code) and the reference kernels compiled
+device-only by `make -f oracle/Makefile.refgpu` (run where the reference checkout is; the
+cubins in oracle/_ref/ are then portable to any host with the driver).  Usage:
+
+    python tests/golden/make_golden_kernels.py OUT.json          # golden digests
+    python tests/golden/make_golden_kernels.py --time OUT.json   # GB300 timings of the same kernels
+
+Every case replays the reference's host-side launch sequence (grid, block, dynamic shared
+memory, argument order) for one operation, citing the host function it follows, on seeded
+uniform residues (numpy default_rng, `oracle.random_residues`), and records the SHA-256 of the
+output words (little-endian u64).  tests/test_oracle_ref_kernels.py recomputes each case with
+the oracle (CPU) and tests/test_gpu_ref_digests.py with this library's CUDA path, and both
+compare digests.
+"""
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", ".."))
+sys.path.insert(0, HERE)
+
+from oracle import oracle as O  # noqa: E402
+import refkern as R  # noqa: E402
+
+GRID_NTT, BLOCK_NTT, PAD = 4096, 128, 4   # include/common.h:23-30 (gridDimNTT, blockDimNTT, per_block_pad)
+BLOCK_GLB = 128                           # include/common.h:20 (blockDimGlb)
+
+
+def sample_size(n):
+    """SAMPLE_SIZE(n), include/ntt.cuh:131-153."""
+    return {2048: 64, 4096: 64, 8192: 128}.get(n, 256)
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<u8").tobytes()).hexdigest()
+
+
+def shoup(w, q):
+    return (int(w) << 64) // int(q)
+
+
+def dmod(mods):
+    """DModulus {value, const_ratio[0], const_ratio[1]} (include/ntt.cuh:6-32) per prime."""
+    rows = [[q] + O.barrett_ratio(q)[:2] for q in mods]
+    return np.array(rows, dtype=np.uint64)
+
+
+def pair(vals, mods):
+    v = np.array([int(x) for x in vals], dtype=np.uint64)
+    s = np.array([shoup(x, q) for x, q in zip(vals, mods)], dtype=np.uint64)
+    return R.dev(v, 8), R.dev(s, 8)
+
+
+class Tables:
+    """DNTTTable over a list of primes (include/ntt.cuh:34-124, src/context.cu:170-183)."""
+
+    def __init__(self, log_n, mods):
+        n = 1 << log_n
+        self.n, self.mods = n, list(mods)
+        tw, tws, itw, itws, ninv = [], [], [], [], []
+        for q in mods:
+            t = O.ntt_tables(log_n, q)
+            tw.append(t[0]), tws.append(t[1]), itw.append(t[2]), itws.append(t[3]), ninv.append(t[4])
+        self.tw, self.tws = R.dev(np.stack(tw), n), R.dev(np.stack(tws), n)
+        self.itw, self.itws = R.dev(np.stack(itw), n), R.dev(np.stack(itws), n)
+        self.ninv, self.ninvs = pair(ninv, mods)
+        self.mod = R.dev(dmod(mods), 8)
+
+
+class Kernels:
+    def __init__(self):
+        m = {s: R.Module(s) for s in ("fntt_2d", "intt_2d", "ntt_modup", "ntt_moddown", "rns_bconv",
+                                       "eval_key_switch", "rns", "polymath", "galois")}
+        self.m = m
+        k = lambda stem, name: m[stem].kernel(name)  # noqa: E731
+        self.f1, self.f2 = k("fntt_2d", "inplace_fnwt_radix8_phase1"), k("fntt_2d", "inplace_fnwt_radix8_phase2")
+        self.i1, self.i2 = k("intt_2d", "inplace_inwt_radix8_phase1"), k("intt_2d", "inplace_inwt_radix8_phase2")
+        self.i1_sp = k("intt_2d", "inplace_inwt_radix8_phase1_include_special_mod")
+        self.i2_sp = k("intt_2d", "inplace_inwt_radix8_phase2_include_special_mod")
+        self.mu_i1 = k("ntt_modup", "inwt_radix8_phase1")
+        self.mu_i2s = k("ntt_modup", "inplace_inwt_radix8_phase2_scale")
+        self.mu_f1x = k("ntt_modup", "inplace_fnwt_radix8_phase1_include_special_mod_exclude_range")
+        self.mu_f2x = k("ntt_modup", "inplace_fnwt_radix8_phase2_include_special_mod_exclude_range")
+        self.md_f1 = k("ntt_moddown", "inplace_fnwt_radix8_phase1")
+        self.md_f2 = k("ntt_moddown", "inplace_fnwt_radix8_phase2_fuse_moddown")
+        self.copy_partql = k("rns_bconv", "modup_copy_partQl_kernel")
+        self.bconv_padded = k("rns_bconv", "bconv_matmul_padded_unroll2_kernel")
+        self.bconv_mult = k("rns_bconv", "bconv_mult_unroll2_kernel")
+        self.bconv_matmul = k("rns_bconv", "bconv_matmul_unroll2_kernel")
+        self.bconv_hps = k("rns_bconv", "base_convert_matmul_hps_unroll2_kernel")
+        self.add_to_ct = k("rns_bconv", "add_to_ct_kernel")
+        self.ip = k("eval_key_switch", "key_switch_inner_prod_c2_and_evk")
+        self.dr_reduce = k("rns", "divide_and_round_reduce_q_last_kernel")
+        self.dr_scalar = k("rns", "divide_and_round_ntt_inv_scalar_kernel")
+        self.sr_qr_r = k("rns", "scaleAndRound_HPS_QR_R_kernel")
+        self.tensor = k("polymath", "tensor_prod_2x2_rns_poly")
+        self.galois = k("galois", "apply_galois_ntt_permutation")
+
+    # nwt_2d_radix8_forward_inplace, src/ntt/fntt_2d.cu:620-653
+    def ntt_fwd(self, T, buf, size, start):
+        n, s1 = T.n, sample_size(T.n)
+        self.f1(GRID_NTT, s1 // 8 * PAD, (s1 + PAD + 1) * PAD * 8, buf, T.tw, T.tws, T.mod, size, start, n, s1, PAD)
+        self.f2(GRID_NTT, BLOCK_NTT, BLOCK_NTT * 64, buf, T.tw, T.tws, T.mod, size, start, n, s1, n // s1)
+
+    # nwt_2d_radix8_backward_inplace, src/ntt/intt_2d.cu:724-757
+    def ntt_inv(self, T, buf, size, start):
+        n = T.n
+        s2 = sample_size(n)
+        s1 = n // s2
+        self.i1(GRID_NTT, BLOCK_NTT, BLOCK_NTT * 64, buf, T.itw, T.itws, T.mod, size, start, n, s1, s2)
+        self.i2(GRID_NTT, s1 // 8 * PAD, (s1 + PAD + 1) * PAD * 8, buf, T.itw, T.itws, T.ninv, T.ninvs, T.mod,
+                size, start, n, s1, PAD)
+
+
+def case_ntt(K, log_n, bits, seed):
+    n = 1 << log_n
+    mods = O.create_coeff_modulus(n, bits)
+    T = Tables(log_n, mods)
+    x = O.random_residues(np.random.default_rng(seed), mods, n, 1)[0]
+    buf = R.dev(x, n)
+    K.ntt_fwd(T, buf, len(mods), 0)
+    fwd = R.host(buf, x.size)
+    K.ntt_inv(T, buf, len(mods), 0)
+    inv = R.host(buf, x.size)
+    assert np.array_equal(inv, x.reshape(-1)), "reference NTT round trip"
+    return {"log_n": log_n, "bits": bits, "seed": seed, "forward": sha(fwd), "inverse_of_forward": sha(inv)}
+
+
+class KsLevel:
+    """DRNSTool tables of one data level for key switching (src/rns.cu:140-200)."""
+
+    def __init__(self, oc, T, l):
+        n, nq, a = oc.n, oc.n_q, oc.n_p
+        self.l, self.qlp, self.beta = l, l + a, (l + a - 1) // a
+        mods = T.mods
+        qlp_mods = mods[:l] + mods[nq:]
+        self.qlp_mods = qlp_mods
+        concat, self.digits = [], []
+        for d in range(self.beta):
+            phi, mat = oc.modup_tables(l, d)
+            sz = len(phi)
+            start = a * d
+            concat += [int(v) for v in phi]
+            compl = qlp_mods[:start] + qlp_mods[start + sz:]
+            self.digits.append(dict(start=start, sz=sz, ibase=R.dev(dmod(qlp_mods[start:start + sz]), 8),
+                                    obase=R.dev(dmod(compl), 8), osz=len(compl), mat=R.dev(mat, 8)))
+        self.part_inv, self.part_inv_s = pair(concat, mods[:l])
+        phi, mat, pinv = oc.moddown_tables(l)
+        self.p_hat_inv, self.p_hat_inv_s = pair(phi, mods[nq:])
+        self.p_to_ql = R.dev(mat, 8)
+        self.p_inv, self.p_inv_s = pair(pinv, mods[:l])
+        self.base_p = R.dev(dmod(mods[nq:]), 8)
+
+
+class Scratch:
+    """Device scratch buffers by name, allocated on first use and reused afterwards (so a
+    sequence can be captured into a CUDA graph after one warm-up run).  Every buffer the
+    reference allocates per call is fully written before it is read, so reuse changes no word."""
+
+    def __init__(self):
+        self.bufs, self.frozen = {}, False
+
+    def __call__(self, key, words):
+        t = self.bufs.get(key)
+        if t is None or t.numel() < words:
+            assert not self.frozen, f"allocation of {key} inside a capture"
+            t = self.bufs[key] = R.zeros(words)
+        return t
+
+
+def ref_keyswitch(K, T, oc, L, ct_d, c2_d, evk_ptrs, scratch=None, keep=False):
+    """keyswitch_inplace for CKKS, src/eval_key_switch.cu:95-182, with DRNSTool::modup
+    (src/rns_bconv.cu:530-628), key_switch_inner_prod (src/eval_key_switch.cu:71-92) and
+    DRNSTool::moddown_from_NTT (src/rns_bconv.cu:776-828).  ct_d (2 x l x N, device) is updated
+    in place; with keep=True returns the host copies of t_mod_up and cx."""
+    S = scratch or Scratch()
+    n, nq, a, qp = oc.n, oc.n_q, oc.n_p, oc.n_q + oc.n_p
+    l, qlp, beta = L.l, L.qlp, L.beta
+    s_fwd = sample_size(n)
+    s2_inv = sample_size(n)
+    s1_inv = n // s2_inv
+    t_mod_up = S("t_mod_up", beta * qlp * n + n)
+    t_cks = S("t_cks", l * n + n)
+    # modup: nwt_2d_radix8_backward_scale (src/ntt/ntt_modup.cu:356-393)
+    K.mu_i1(GRID_NTT, BLOCK_NTT, BLOCK_NTT * 64, t_cks, c2_d, T.itw, T.itws, T.mod, l, 0, n, s1_inv, s2_inv)
+    K.mu_i2s(GRID_NTT, s1_inv // 8 * PAD, (s1_inv + PAD + 1) * PAD * 8, t_cks, T.itw, T.itws, T.ninv, T.ninvs,
+             T.mod, l, 0, n, s1_inv, PAD, L.part_inv, L.part_inv_s)
+    K.copy_partql(n * l // BLOCK_GLB, BLOCK_GLB, 0, t_mod_up, c2_d, l * n, qlp * n, a * n)
+    for d, D in enumerate(L.digits):
+        part = R.Ptr(t_mod_up, d * qlp * n)
+        K.bconv_padded(n * D["osz"] // BLOCK_GLB // 2, BLOCK_GLB, 8 * D["osz"] * D["sz"], part,
+                       R.Ptr(t_cks, D["start"] * n), D["mat"], D["ibase"], D["sz"], D["obase"], D["osz"], n,
+                       D["start"], D["sz"])
+        # nwt_2d_radix8_forward_inplace_include_special_mod_exclude_range (src/ntt/ntt_modup.cu:610-657)
+        lo, hi = D["start"], D["start"] + D["sz"]
+        K.mu_f1x(GRID_NTT, s_fwd // 8 * PAD, (s_fwd + PAD + 1) * PAD * 8, part, T.tw, T.tws, T.mod, qlp, 0, qp, a,
+                 n, s_fwd, PAD, lo, hi)
+        K.mu_f2x(GRID_NTT, BLOCK_NTT, BLOCK_NTT * 64, part, T.tw, T.tws, T.mod, qlp, 0, qp, a, n, s_fwd,
+                 n // s_fwd, lo, hi)
+    tm = R.host(t_mod_up, beta * qlp * n) if keep else None
+    # inner product; reduction_threshold as src/eval_key_switch.cu:156-157
+    thr = (1 << (64 - int(np.log2(float(T.mods[0]))) - 1)) - 1
+    cx = S("cx", 2 * qlp * n + n)
+    K.ip(qlp * n // BLOCK_GLB, BLOCK_GLB, 0, cx, t_mod_up, evk_ptrs, T.mod, n, qp, qp * n, qlp, qlp * n, nq, l,
+         beta, thr)
+    cxh = R.host(cx, 2 * qlp * n) if keep else None
+    for i in range(2):
+        cx_i = R.Ptr(cx, i * qlp * n)
+        # nwt_2d_radix8_backward_inplace_include_special_mod (src/ntt/intt_2d.cu:796-834)
+        K.i1_sp(GRID_NTT, BLOCK_NTT, BLOCK_NTT * 64, cx_i, T.itw, T.itws, T.mod, a, l, qp, a, n, s1_inv, s2_inv)
+        K.i2_sp(GRID_NTT, s1_inv // 8 * PAD, (s1_inv + PAD + 1) * PAD * 8, cx_i, T.itw, T.itws, T.ninv, T.ninvs,
+                T.mod, a, l, qp, a, n, s1_inv, PAD)
+        # DBaseConverter::bConv_BEHZ (src/rns_bconv.cu:212-229), P -> Ql
+        temp = S("temp", a * n + n)
+        delta = S("delta", l * n + n)
+        K.bconv_mult(a * n // 2 // BLOCK_GLB, BLOCK_GLB, 0, temp, R.Ptr(cx, i * qlp * n + l * n), L.p_hat_inv,
+                     L.p_hat_inv_s, L.base_p, a, n)
+        K.bconv_matmul(l * n // 2 // BLOCK_GLB, BLOCK_GLB, 8 * l * a, delta, temp, L.p_to_ql, L.base_p, a, T.mod,
+                       l, n)
+        # nwt_2d_radix8_forward_inplace_fuse_moddown (src/ntt/ntt_moddown.cu:222-261)
+        K.md_f1(GRID_NTT, s_fwd // 8 * PAD, (s_fwd + PAD + 1) * PAD * 8, delta, T.tw, T.tws, T.mod, l, 0, n,
+                s_fwd, PAD)
+        K.md_f2(GRID_NTT, BLOCK_NTT, BLOCK_NTT * 64, cx_i, cx_i, L.p_inv, L.p_inv_s, delta, T.tw, T.tws, T.mod,
+                l, 0, n, s_fwd, n // s_fwd)
+    for i in range(2):
+        K.add_to_ct(l * n // BLOCK_GLB, BLOCK_GLB, 0, R.Ptr(ct_d, i * l * n), R.Ptr(cx, i * qlp * n), T.mod, n, l)
+    return tm, cxh
+
+
+def rescale_tables(T, l):
+    """inv_q_last_mod_q and its Shoup companions for level l (src/rns.cu:1160-1184)."""
+    return pair([pow(T.mods[l - 1], -1, q) for q in T.mods[:l - 1]], T.mods[:l - 1])
+
+
+def ref_rescale(K, T, src, dst, l, size, inv_tables=None):
+    """DRNSTool::divide_and_round_q_last_ntt, src/rns.cu:1160-1184: src (size x l x N, device;
+    its last limbs are turned to coefficient form, as the reference does) -> dst (size x (l-1) x N)."""
+    n = T.n
+    inv, inv_s = inv_tables or rescale_tables(T, l)
+    g = n * (l - 1) // BLOCK_GLB
+    s2 = sample_size(n)
+    s1 = n // s2
+    s = sample_size(n)
+    for i in range(size):
+        ci_in, ci_out = R.Ptr(src, i * l * n), R.Ptr(dst, i * (l - 1) * n)
+        # nwt_2d_radix8_backward_inplace(ci_in, tables, 1, l - 1): the last limb only
+        K.i1(GRID_NTT, BLOCK_NTT, BLOCK_NTT * 64, ci_in, T.itw, T.itws, T.mod, 1, l - 1, n, s1, s2)
+        K.i2(GRID_NTT, s1 // 8 * PAD, (s1 + PAD + 1) * PAD * 8, ci_in, T.itw, T.itws, T.ninv, T.ninvs, T.mod, 1,
+             l - 1, n, s1, PAD)
+        K.dr_reduce(g, BLOCK_GLB, 0, ci_out, ci_in, T.mod, n, l - 1)
+        K.f1(GRID_NTT, s // 8 * PAD, (s + PAD + 1) * PAD * 8, ci_out, T.tw, T.tws, T.mod, l - 1, 0, n, s, PAD)
+        K.f2(GRID_NTT, BLOCK_NTT, BLOCK_NTT * 64, ci_out, T.tw, T.tws, T.mod, l - 1, 0, n, s, n // s)
+        K.dr_scalar(g, BLOCK_GLB, 0, ci_out, ci_in, T.mod, inv, inv_s, n, l - 1)
+
+
+def key_setup(rng, mods, n, nq, special):
+    dnum = -(-nq // special)
+    evk = O.random_residues(rng, mods, n, 2 * dnum).reshape(dnum, 2, len(mods), n)
+    evk_t = R.dev(evk, n)
+    ptrs = np.array([evk_t.data_ptr() + 8 * d * 2 * len(mods) * n for d in range(dnum)], dtype=np.uint64)
+    return evk_t, R.dev(ptrs, 8)
+
+
+def case_keyswitch(K, log_n, bits, special, levels, seed):
+    n = 1 << log_n
+    mods = O.create_coeff_modulus(n, bits)
+    nq = len(bits) - special
+    oc = O.Context(log_n, mods, nq, special)
+    T = Tables(log_n, mods)
+    rng = np.random.default_rng(seed)
+    evk_t, evk_ptrs = key_setup(rng, mods, n, nq, special)
+    out = {"log_n": log_n, "bits": bits, "special": special, "seed": seed, "levels": {}}
+    for l in sorted(levels, reverse=True):  # inputs are drawn level by level, highest first
+        ct = O.random_residues(rng, mods[:l], n, 2)
+        c2 = O.random_residues(rng, mods[:l], n, 1)[0]
+        ct_d = R.dev(ct, n)
+        tm, cx = ref_keyswitch(K, T, oc, KsLevel(oc, T, l), ct_d, R.dev(c2, n), evk_ptrs, keep=True)
+        out["levels"][str(l)] = {"modup": sha(tm), "inner_product": sha(cx), "keyswitch": sha(R.host(ct_d, 2 * l * n))}
+    return out
+
+
+def case_hmult(K, log_n, bits, special, l, seed):
+    """CKKS multiply_and_relin_inplace (src/evaluate.cu:1061-1104: bgv_ckks_multiply's
+    tensor_prod_2x2_rns_poly, then relinearize_inplace :1342-1374, i.e. keyswitch_inplace with
+    c2 = the third polynomial) followed by rescale_to_next (:1545-1565)."""
+    n = 1 << log_n
+    mods = O.create_coeff_modulus(n, bits)
+    nq = len(bits) - special
+    oc = O.Context(log_n, mods, nq, special)
+    T = Tables(log_n, mods)
+    rng = np.random.default_rng(seed)
+    evk_t, evk_ptrs = key_setup(rng, mods, n, nq, special)
+    a = O.random_residues(rng, mods[:l], n, 2)
+    b = O.random_residues(rng, mods[:l], n, 2)
+    d = R.zeros(3 * l * n + n)
+    K.tensor(l * n // BLOCK_GLB, BLOCK_GLB, 0, R.dev(a, n), R.dev(b, n), T.mod, d, n, l)
+    ref_keyswitch(K, T, oc, KsLevel(oc, T, l), d, R.Ptr(d, 2 * l * n), evk_ptrs)
+    relin = R.host(d, 2 * l * n)
+    out = R.zeros(2 * (l - 1) * n + n)
+    ref_rescale(K, T, d, out, l, 2)
+    return {"log_n": log_n, "bits": bits, "special": special, "l": l, "seed": seed,
+            "multiply_and_relin": sha(relin), "rescaled": sha(R.host(out, 2 * (l - 1) * n))}
+
+
+def case_rescale(K, log_n, bits, special, l, seed):
+    """DRNSTool::divide_and_round_q_last_ntt, src/rns.cu:1160-1184, on a size-2 ciphertext."""
+    n = 1 << log_n
+    mods = O.create_coeff_modulus(n, bits)
+    T = Tables(log_n, mods)
+    ct = O.random_residues(np.random.default_rng(seed), mods[:l], n, 2)
+    src = R.dev(ct, n)
+    dst = R.zeros(2 * (l - 1) * n + n)
+    ref_rescale(K, T, src, dst, l, 2)
+    return {"log_n": log_n, "bits": bits, "special": special, "l": l, "seed": seed,
+            "rescale": sha(R.host(dst, 2 * (l - 1) * n))}
+
+
+def case_tensor_galois(K, log_n, bits, special, l, steps, seed):
+    """tensor_prod_2x2_rns_poly (src/polymath.cu:463-497, launched as src/evaluate.cu:379) and
+    apply_galois_ntt_permutation (src/galois.cu:11-18) with the oracle's permutation table."""
+    n = 1 << log_n
+    mods = O.create_coeff_modulus(n, bits)
+    T = Tables(log_n, mods)
+    rng = np.random.default_rng(seed)
+    a = O.random_residues(rng, mods[:l], n, 2)
+    b = O.random_residues(rng, mods[:l], n, 2)
+    out = R.zeros(3 * l * n + n)
+    K.tensor(l * n // BLOCK_GLB, BLOCK_GLB, 0, R.dev(a, n), R.dev(b, n), T.mod, out, n, l)
+    res = {"log_n": log_n, "bits": bits, "special": special, "l": l, "seed": seed,
+           "tensor": sha(R.host(out, 3 * l * n)), "galois": {}}
+    x = O.random_residues(rng, mods[:l], n, 1)[0]
+    xd = R.dev(x, n)
+    for step in steps:
+        elt = O.elt_from_step(step, n)
+        perm = torch.from_numpy(O.galois_perm(log_n, elt).view(np.int32).copy()).cuda()
+        dst = R.zeros(l * n + n)
+        K.galois(l * n // BLOCK_GLB, BLOCK_GLB, 0, dst, xd, perm, n, l)
+        res["galois"][str(step)] = {"elt": elt, "sha": sha(R.host(dst, l * n))}
+    return res
+
+
+def case_hps(K, log_n, bits, special, t, seed):
+    """DBaseConverter::bConv_HPS Q -> R (src/rns_bconv.cu:354-372) and
+    DRNSTool::scaleAndRound_HPS_QR_R (src/rns.cu:1740-1747), BFV at the top level."""
+    n = 1 << log_n
+    mods = O.create_coeff_modulus(n, bits)
+    nq = len(bits) - special
+    oc = O.Context(log_n, mods, nq, special, t)
+    q, r = mods[:nq], oc.r_moduli
+    big_q = 1
+    for v in q:
+        big_q *= v
+    hat = [big_q // v for v in q]
+    hat_inv, hat_inv_s = pair([pow(h % v, -1, v) for h, v in zip(hat, q)], q)
+    qhat_mod_r = R.dev(np.array([[h % rj for h in hat] for rj in r], dtype=np.uint64), 8)
+    alpha_q = R.dev(np.array([[(v * big_q) % rj for rj in r] for v in range(nq + 1)], dtype=np.uint64), 8)
+    qinv = R.dev(np.array([1.0 / float(v) for v in q], dtype=np.float64), 8)
+    base_q, base_r = R.dev(dmod(q), 8), R.dev(dmod(r), 8)
+    rng = np.random.default_rng(seed)
+    x = O.random_residues(rng, q, n, 1)[0]
+    temp = R.zeros(nq * n + n)
+    dst = R.zeros(len(r) * n + n)
+    K.bconv_mult(nq * n // 2 // BLOCK_GLB, BLOCK_GLB, 0, temp, R.dev(x, n), hat_inv, hat_inv_s, base_q, nq, n)
+    K.bconv_hps(len(r) * n // 2 // BLOCK_GLB, BLOCK_GLB, 8 * len(r) * nq, dst, temp, qhat_mod_r, alpha_q, qinv,
+                base_q, nq, base_r, len(r), n)
+    out = {"log_n": log_n, "bits": bits, "special": special, "t": t, "seed": seed,
+           "bconv_q_to_r": sha(R.host(dst, len(r) * n))}
+    frac, modr = oc.hps_tables()
+    xr = O.random_residues(rng, list(q) + list(r), n, 1)[0]
+    dst2 = R.zeros(len(r) * n + n)
+    K.sr_qr_r(n // BLOCK_GLB, BLOCK_GLB, 0, dst2, R.dev(xr, n), R.dev(modr, 8), R.dev(frac, 8), base_r, n, nq,
+              len(r))
+    out["scale_round_qr_r"] = sha(R.host(dst2, len(r) * n))
+    return out
+
+
+def graph_time(fn, inner, reps, scratch=()):
+    """Device time (ms) per call of fn(i), a sequence of reference launches and device copies:
+    one synchronous warm-up run (allocates scratch), then `inner` calls captured in one CUDA graph,
+    replayed `reps` times between CUDA events.  Host launch overhead is excluded, which can only
+    favour the reference."""
+    for i in range(inner):
+        fn(i)
+    torch.cuda.synchronize()
+    for S in scratch:
+        S.frozen = True
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        R.set_launch_mode(torch.cuda.current_stream().cuda_stream, sync=False)
+        try:
+            for i in range(inner):
+                fn(i)
+        finally:
+            R.set_launch_mode()
+    g.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        g.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / (reps * inner)
+
+
+def time_reference(K, path):
+    """Times the replayed reference sequences on the N=2^16, 1x60 + 29x40 + 5x60, dnum=6
+    parameter set at l=30 (HMult + relinearise + rescale, key switch, HRotate(1)), the forward
+    NTT over 64 x 35 limbs, and the N=2^12 3x60 NTT round trip.  Four ciphertexts are cycled
+    (working set > L2), one key shared, as in bench.py."""
+    res = {}
+    log_n, l, special = 16, 30, 5
+    n = 1 << log_n
+    bits = [60] + [40] * 29 + [60] * 5
+    mods = O.create_coeff_modulus(n, bits)
+    nq = len(bits) - special
+    oc = O.Context(log_n, mods, nq, special)
+    T = Tables(log_n, mods)
+    L = KsLevel(oc, T, l)
+    rt = rescale_tables(T, l)
+    rng = np.random.default_rng(7)
+    evk_t, evk_ptrs = key_setup(rng, mods, n, nq, special)
+    S = Scratch()
+    pairs = [(R.dev(O.random_residues(rng, mods[:l], n, 2), n), R.dev(O.random_residues(rng, mods[:l], n, 2), n))
+             for _ in range(4)]
+    d = [R.zeros(3 * l * n + n) for _ in range(4)]
+    cp = R.zeros(2 * l * n + n)
+    out = [R.zeros(2 * (l - 1) * n + n) for _ in range(4)]
+
+    def hmult(i):
+        a, b = pairs[i % 4]
+        K.tensor(l * n // BLOCK_GLB, BLOCK_GLB, 0, a, b, T.mod, d[i % 4], n, l)
+        ref_keyswitch(K, T, oc, L, d[i % 4], R.Ptr(d[i % 4], 2 * l * n), evk_ptrs, scratch=S)
+        cp[: 2 * l * n].copy_(d[i % 4][: 2 * l * n])  # mod_switch_scale_to_next's encrypted_copy
+        ref_rescale(K, T, cp, out[i % 4], l, 2, rt)
+
+    res["ckks_hmult_relin_rescale_n16_l30_ms"] = graph_time(hmult, 4, 10, (S,))
+
+    def keyswitch(i):
+        a, b = pairs[i % 4]
+        ref_keyswitch(K, T, oc, L, a, R.Ptr(b, 0), evk_ptrs, scratch=S)
+
+    res["ckks_keyswitch_n16_l30_ms"] = graph_time(keyswitch, 4, 10, (S,))
+
+    elt = O.elt_from_step(1, n)
+    perm = torch.from_numpy(O.galois_perm(log_n, elt).view(np.int32).copy()).cuda()
+    temp = R.zeros(l * n + n)
+
+    def rotate(i):
+        """apply_galois_inplace for CKKS, src/evaluate.cu:1567-1630."""
+        c = pairs[i % 4][0]
+        K.galois(l * n // BLOCK_GLB, BLOCK_GLB, 0, temp, c, perm, n, l)
+        c[: l * n].copy_(temp[: l * n])
+        K.galois(l * n // BLOCK_GLB, BLOCK_GLB, 0, temp, R.Ptr(c, l * n), perm, n, l)
+        c[l * n: 2 * l * n].zero_()
+        ref_keyswitch(K, T, oc, L, c, temp, evk_ptrs, scratch=S)
+
+    res["ckks_hrotate_step1_n16_l30_ms"] = graph_time(rotate, 4, 10, (S,))
+    del pairs, d, out, cp, evk_t, S
+    torch.cuda.empty_cache()
+
+    polys = 64
+    Tq = Tables(log_n, mods)
+    big = R.zeros(polys * len(mods) * n)
+
+    def ntt64(i):
+        for p in range(polys):
+            K.ntt_fwd(Tq, R.Ptr(big, p * len(mods) * n), len(mods), 0)
+
+    ms = graph_time(ntt64, 1, 10)
+    res["ntt_forward_n16_64x35_ms"] = ms
+    res["ntt_forward_n16_64x35_gbs"] = 16 * n * len(mods) * polys / (ms * 1e-3) / 1e9
+    del big
+    torch.cuda.empty_cache()
+
+    n12 = 4096
+    m12 = O.create_coeff_modulus(n12, [60, 60, 60])
+    T12 = Tables(12, m12)
+    b12 = R.dev(O.random_residues(rng, m12, n12, 1), n12)
+
+    def rt12(i):
+        K.ntt_fwd(T12, b12, 3, 0)
+        K.ntt_inv(T12, b12, 3, 0)
+
+    res["ntt_n12_3x60_roundtrip_graph_us"] = 1e3 * graph_time(rt12, 50, 20)
+    res["note"] = ("reference kernels compiled from source for sm_103a, replayed in CUDA graphs on the "
+                   "reference's own launch configuration; device time only (no host launch or allocation cost)")
+    with open(path, "w") as f:
+        json.dump(res, f, indent=1, sort_keys=True)
+    print(json.dumps(res))
+
+
+def main(path):
+    torch.zeros(1, device="cuda")
+    K = Kernels()
+    res = {
+        "ntt_n12_3x60": case_ntt(K, 12, [60, 60, 60], 1201),
+        "ntt_n16_4": case_ntt(K, 16, [60, 40, 40, 60], 1601),
+        "ntt_n13_5": case_ntt(K, 13, [50, 50, 50, 50, 60], 1301),
+        "ks_ckks_n12_a2": case_keyswitch(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, [5, 4, 2], 1202),
+        "ks_ckks_n13_a3": case_keyswitch(K, 13, [60] + [50] * 5 + [60] * 3, 3, [6, 4, 1], 1302),
+        "ks_ckks_n16_a5_l7": case_keyswitch(K, 16, [60] + [40] * 9 + [60] * 5, 5, [7], 1602),
+        "hmult_ckks_n12_a2": case_hmult(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, 1206),
+        "hmult_ckks_n16_l30": case_hmult(K, 16, [60] + [40] * 29 + [60] * 5, 5, 30, 1606),
+        "rescale_n12": case_rescale(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, 1203),
+        "tensor_galois_n12": case_tensor_galois(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, [1, -3, 7], 1204),
+        "hps_n12": case_hps(K, 12, [50, 50, 50, 50, 60, 60], 2, 65537, 1205),
+        "hps_n15": case_hps(K, 15, [50] * 16 + [60, 60], 2, 65537, 1501),
+    }
+    with open(path, "w") as f:
+        json.dump(res, f, indent=1, sort_keys=True)
+    print(json.dumps({k: "ok" for k in res}))
+
+
+if __name__ == "__main__":
+    if len(sys.argv) == 3 and sys.argv[1] == "--time":
+        torch.zeros(1, device="cuda")
+        time_reference(Kernels(), sys.argv[2])
+    else:
+        main(sys.argv[1])

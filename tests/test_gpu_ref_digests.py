@@ -1,0 +1,122 @@
+"""The GPU library against PhantomFHE's own compiled kernels, with no oracle in between.
+
+tests/golden/ref_kernels.json holds SHA-256 digests of the reference kernels' outputs on seeded
+inputs (tests/golden/make_golden_kernels.py).  These tests draw the same inputs, run them through
+this library's C ABI on the GPU (tensor-core and CUDA-core base conversions both), and compare
+digests: NTT/iNTT, the CKKS key switch, rescale and the tensor product."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+from oracle import oracle as O  # noqa: E402
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ref_kernels.json")
+with open(GOLDEN) as _f:
+    G = json.load(_f)
+
+
+def sha(t):
+    a = t.cpu().numpy().view(np.uint64) if isinstance(t, torch.Tensor) else t
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<u8").tobytes()).hexdigest()
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import phantom_gb300
+    return phantom_gb300
+
+
+@pytest.mark.parametrize("name", [k for k in G if k.startswith("ntt_")])
+def test_ntt_digests(pg, name):
+    g = G[name]
+    n = 1 << g["log_n"]
+    mods = pg.create_coeff_modulus(n, g["bits"])
+    ctx = pg.Context(n, mods, 1)
+    x = O.random_residues(np.random.default_rng(g["seed"]), mods, n, 1)
+    t = pg.to_device(x)
+    ctx.ntt_forward(t, 1, len(mods))
+    assert sha(t) == g["forward"]
+    ctx.ntt_inverse(t, 1, len(mods))
+    assert sha(t) == g["inverse_of_forward"]
+
+
+@pytest.mark.parametrize("name", [k for k in G if k.startswith("ks_")])
+def test_keyswitch_digests(pg, name):
+    g = G[name]
+    n = 1 << g["log_n"]
+    mods = pg.create_coeff_modulus(n, g["bits"])
+    nq = len(g["bits"]) - g["special"]
+    ctx = pg.Context(n, mods, g["special"])
+    ws = ctx.workspace()
+    rng = np.random.default_rng(g["seed"])
+    evk = O.random_residues(rng, mods, n, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), n)
+    key = pg.KeySwitchKey(pg.to_device(evk))
+    for l in sorted((int(k) for k in g["levels"]), reverse=True):  # the generator's draw order
+        ct = O.random_residues(rng, mods[:l], n, 2)
+        c2 = O.random_residues(rng, mods[:l], n, 1)[0]
+        for tc in (True, False):
+            ctx.tensor_cores = tc
+            t = pg.to_device(ct)
+            ctx.keyswitch(ws, t, pg.to_device(c2), nq - l + 1, key)
+            assert sha(t) == g["levels"][str(l)]["keyswitch"], f"level {l}, tensor_cores={tc}"
+        assert ctx.device_status() == 0
+
+
+def test_rescale_and_tensor_digests(pg):
+    g = G["rescale_n12"]
+    n, l = 1 << g["log_n"], g["l"]
+    mods = pg.create_coeff_modulus(n, g["bits"])
+    nq = len(g["bits"]) - g["special"]
+    ctx = pg.Context(n, mods, g["special"])
+    ws = ctx.workspace()
+    ct = O.random_residues(np.random.default_rng(g["seed"]), mods[:l], n, 2)
+    out = torch.empty((2, l - 1, n), dtype=torch.int64, device="cuda")
+    ctx.rescale_to_next(ws, pg.to_device(ct), out, 2, nq - l + 1)
+    assert sha(out) == g["rescale"]
+
+    g = G["tensor_galois_n12"]
+    l = g["l"]
+    rng = np.random.default_rng(g["seed"])
+    a = O.random_residues(rng, mods[:l], n, 2)
+    b = O.random_residues(rng, mods[:l], n, 2)
+    t = torch.zeros((3, l, n), dtype=torch.int64, device="cuda")
+    t[:2] = pg.to_device(a)
+    ctx.ckks_multiply(t, pg.to_device(b), nq - l + 1)
+    assert sha(t) == g["tensor"]
+
+
+@pytest.mark.parametrize("name", [k for k in G if k.startswith("hmult_")])
+def test_hmult_digests(pg, name):
+    """The fused HMult + relinearise + rescale kernel chain and the two-call form give the
+    reference's words (N=2^16, l=30, dnum=6 is the benchmark configuration)."""
+    g = G[name]
+    n, l = 1 << g["log_n"], g["l"]
+    mods = pg.create_coeff_modulus(n, g["bits"])
+    nq = len(g["bits"]) - g["special"]
+    ctx = pg.Context(n, mods, g["special"])
+    ws = ctx.workspace()
+    rng = np.random.default_rng(g["seed"])
+    evk = O.random_residues(rng, mods, n, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), n)
+    key = pg.KeySwitchKey(pg.to_device(evk))
+    a = O.random_residues(rng, mods[:l], n, 2)
+    b = O.random_residues(rng, mods[:l], n, 2)
+    chain = nq - l + 1
+    for tc in (True, False):
+        ctx.tensor_cores = tc
+        out = torch.empty((2, l - 1, n), dtype=torch.int64, device="cuda")
+        ctx.multiply_relin_rescale(ws, pg.to_device(a), pg.to_device(b), out, chain, key)
+        assert sha(out) == g["rescaled"], f"fused, tensor_cores={tc}"
+        ta = pg.to_device(a)
+        ctx.multiply_and_relin(ws, ta, pg.to_device(b), chain, key)
+        assert sha(ta) == g["multiply_and_relin"], f"multiply_and_relin, tensor_cores={tc}"
+        out2 = torch.empty((2, l - 1, n), dtype=torch.int64, device="cuda")
+        ctx.rescale_to_next(ws, ta, out2, 2, chain)
+        assert sha(out2) == g["rescaled"], f"two calls, tensor_cores={tc}"
+    assert ctx.device_status() == 0
