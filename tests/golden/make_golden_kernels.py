@@ -102,6 +102,10 @@ class Kernels:
         self.dr_scalar = k("rns", "divide_and_round_ntt_inv_scalar_kernel")
         self.sr_qr_r = k("rns", "scaleAndRound_HPS_QR_R_kernel")
         self.tensor = k("polymath", "tensor_prod_2x2_rns_poly")
+        self.f1_sp = k("fntt_2d", "inplace_fnwt_radix8_phase1_include_special_mod")
+        self.f2_sp = k("fntt_2d", "inplace_fnwt_radix8_phase2_include_special_mod")
+        self.bconv_mult1 = k("rns_bconv", "bconv_mult_kernel")
+        self.moddown_k = k("rns_bconv", "moddown_kernel")
         self.galois = k("galois", "apply_galois_ntt_permutation")
 
     # nwt_2d_radix8_forward_inplace, src/ntt/fntt_2d.cu:620-653
@@ -382,6 +386,131 @@ def case_hps(K, log_n, bits, special, t, seed):
     return out
 
 
+class HpsConv:
+    """DBaseConverter of the HPS bases (include/rns_bconv.cuh:26-60, src/host/rns.cu:420-470):
+    QHatInvModq of the input base, QHatModp [out][in], alphaQModp [(in + 1)][out], 1/q_i."""
+
+    def __init__(self, ibase, obase):
+        big = 1
+        for v in ibase:
+            big *= v
+        hat = [big // v for v in ibase]
+        self.ni, self.no = len(ibase), len(obase)
+        self.hat_inv, self.hat_inv_s = pair([pow(h % v, -1, v) for h, v in zip(hat, ibase)], ibase)
+        self.hat_mod = R.dev(np.array([[h % p for h in hat] for p in obase], dtype=np.uint64), 8)
+        self.alpha = R.dev(np.array([[(a * big) % p for p in obase] for a in range(len(ibase) + 1)],
+                                    dtype=np.uint64), 8)
+        self.inv = R.dev(np.array([1.0 / float(v) for v in ibase], dtype=np.float64), 8)
+        self.ib, self.ob = R.dev(dmod(ibase), 8), R.dev(dmod(obase), 8)
+
+    def run(self, K, dst, src, n, S):
+        """DBaseConverter::bConv_HPS, src/rns_bconv.cu:354-372."""
+        temp = S("hps_temp", self.ni * n + n)
+        K.bconv_mult(self.ni * n // 2 // BLOCK_GLB, BLOCK_GLB, 0, temp, src, self.hat_inv, self.hat_inv_s, self.ib,
+                     self.ni, n)
+        K.bconv_hps(self.no * n // 2 // BLOCK_GLB, BLOCK_GLB, 8 * self.no * self.ni, dst, temp, self.hat_mod,
+                    self.alpha, self.inv, self.ib, self.ni, self.ob, self.no, n)
+
+
+class BfvSetup:
+    def __init__(self, log_n, bits, special, t, rng):
+        n = 1 << log_n
+        self.n = n
+        self.mods = O.create_coeff_modulus(n, bits)
+        self.nq = nq = len(bits) - special
+        self.special = special
+        self.oc = O.Context(log_n, self.mods, nq, special, t)
+        q, r = self.mods[:nq], self.oc.r_moduli
+        self.q, self.r = q, r
+        self.T = Tables(log_n, self.mods)
+        self.Tqr = Tables(log_n, list(q) + list(r))
+        self.q_to_r, self.r_to_q = HpsConv(q, r), HpsConv(r, q)
+        frac, modr = self.oc.hps_tables()
+        self.frac, self.modr = R.dev(frac, 8), R.dev(modr, 8)
+        self.L = KsLevel(self.oc, self.T, nq)
+        self.evk_t, self.evk_ptrs = key_setup(rng, self.mods, n, nq, special)
+
+
+def ref_bfv_mul_relin(K, B, a_d, b_d, S):
+    """bfv_mul_relin_hps with mul_tech hps (src/evaluate.cu:820-1026): a_d (2 x Q x N, device) is
+    replaced by the relinearised product of a_d and b_d (coefficient form)."""
+    n, nq, nr = B.n, B.nq, len(B.r)
+    qr = nq + nr
+    a_ = B.special
+    qp = nq + a_
+    ct1 = S("bfv_ct1", 3 * qr * n + n)
+    ct2 = S("bfv_ct2", 2 * qr * n + n)
+    for src, dst in ((a_d, ct1), (b_d, ct2)):
+        for i in range(2):
+            dst[i * qr * n: i * qr * n + nq * n].copy_(src[i * nq * n: (i + 1) * nq * n])
+            B.q_to_r.run(K, R.Ptr(dst, i * qr * n + nq * n), R.Ptr(dst, i * qr * n), n, S)
+    for buf in (ct1, ct2):
+        for i in range(2):
+            K.ntt_fwd(B.Tqr, R.Ptr(buf, i * qr * n), qr, 0)
+    K.tensor(n * qr // BLOCK_GLB, BLOCK_GLB, 0, ct1, ct2, B.Tqr.mod, ct1, n, qr)
+    for i in range(3):
+        K.ntt_inv(B.Tqr, R.Ptr(ct1, i * qr * n), qr, 0)
+    out3 = S("bfv_out3", 3 * nq * n + n)
+    temp = S("bfv_rl", nr * n + n)
+    for i in range(3):
+        # DRNSTool::scaleAndRound_HPS_QR_R (src/rns.cu:1740-1747), then R -> Q
+        K.sr_qr_r(n // BLOCK_GLB, BLOCK_GLB, 0, temp, R.Ptr(ct1, i * qr * n), B.modr, B.frac, B.r_to_q.ib, n, nq, nr)
+        B.r_to_q.run(K, R.Ptr(out3, i * nq * n), temp, n, S)
+    # key switch of c2 in BFV mode: modup (src/rns_bconv.cu:530-628, scheme bfv)
+    L, T = B.L, B.T
+    l, qlp, beta = L.l, L.qlp, L.beta
+    c2 = R.Ptr(out3, 2 * nq * n)
+    t_mod_up = S("t_mod_up", beta * qlp * n + n)
+    t_cks = S("t_cks", l * n + n)
+    s = sample_size(n)
+    s2 = sample_size(n)
+    s1 = n // s2
+    K.copy_partql(n * l // BLOCK_GLB, BLOCK_GLB, 0, t_mod_up, c2, l * n, qlp * n, a_ * n)
+    for d, D in enumerate(L.digits):
+        part = R.Ptr(t_mod_up, d * qlp * n)
+        K.bconv_mult1(n * D["sz"] // BLOCK_GLB, BLOCK_GLB, 0, R.Ptr(t_cks, D["start"] * n),
+                      R.Ptr(out3, 2 * nq * n + D["start"] * n), R.Ptr(L.part_inv, D["start"]),
+                      R.Ptr(L.part_inv_s, D["start"]), D["ibase"], D["sz"], n)
+        K.bconv_padded(n * D["osz"] // BLOCK_GLB // 2, BLOCK_GLB, 8 * D["osz"] * D["sz"], part,
+                       R.Ptr(t_cks, D["start"] * n), D["mat"], D["ibase"], D["sz"], D["obase"], D["osz"], n,
+                       D["start"], D["sz"])
+        # nwt_2d_radix8_forward_inplace_include_special_mod (src/ntt/fntt_2d.cu:695-736)
+        K.f1_sp(GRID_NTT, s // 8 * PAD, (s + PAD + 1) * PAD * 8, part, T.tw, T.tws, T.mod, qlp, 0, qp, a_, n, s,
+                PAD)
+        K.f2_sp(GRID_NTT, BLOCK_NTT, BLOCK_NTT * 64, part, T.tw, T.tws, T.mod, qlp, 0, qp, a_, n, s, n // s)
+    thr = (1 << (64 - max(v.bit_length() for v in B.q) - 1)) - 1
+    cx = S("cx", 2 * qlp * n + n)
+    K.ip(qlp * n // BLOCK_GLB, BLOCK_GLB, 0, cx, t_mod_up, B.evk_ptrs, T.mod, n, qp, qp * n, qlp, qlp * n, nq, l,
+         beta, thr)
+    for i in range(2):
+        cx_i = R.Ptr(cx, i * qlp * n)
+        # moddown_from_NTT, scheme bfv (src/rns_bconv.cu:776-828)
+        K.i1_sp(GRID_NTT, BLOCK_NTT, BLOCK_NTT * 64, cx_i, T.itw, T.itws, T.mod, qlp, 0, qp, a_, n, s1, s2)
+        K.i2_sp(GRID_NTT, s1 // 8 * PAD, (s1 + PAD + 1) * PAD * 8, cx_i, T.itw, T.itws, T.ninv, T.ninvs, T.mod,
+                qlp, 0, qp, a_, n, s1, PAD)
+        temp2 = S("temp", a_ * n + n)
+        delta = S("delta", l * n + n)
+        K.bconv_mult(a_ * n // 2 // BLOCK_GLB, BLOCK_GLB, 0, temp2, R.Ptr(cx, i * qlp * n + l * n), L.p_hat_inv,
+                     L.p_hat_inv_s, L.base_p, a_, n)
+        K.bconv_matmul(l * n // 2 // BLOCK_GLB, BLOCK_GLB, 8 * l * a_, delta, temp2, L.p_to_ql, L.base_p, a_, T.mod,
+                       l, n)
+        K.moddown_k(l * n // BLOCK_GLB, BLOCK_GLB, 0, cx_i, cx_i, delta, T.mod, L.p_inv, L.p_inv_s, n, l)
+    for i in range(2):
+        K.add_to_ct(l * n // BLOCK_GLB, BLOCK_GLB, 0, R.Ptr(out3, i * nq * n), R.Ptr(cx, i * qlp * n), T.mod, n, l)
+    a_d[: 2 * nq * n].copy_(out3[: 2 * nq * n])
+
+
+def case_bfv(K, log_n, bits, special, t, seed):
+    rng = np.random.default_rng(seed)
+    B = BfvSetup(log_n, bits, special, t, rng)
+    a = O.random_residues(rng, B.q, B.n, 2)
+    b = O.random_residues(rng, B.q, B.n, 2)
+    a_d, b_d = R.dev(a, B.n), R.dev(b, B.n)
+    ref_bfv_mul_relin(K, B, a_d, b_d, Scratch())
+    return {"log_n": log_n, "bits": bits, "special": special, "t": t, "seed": seed,
+            "mul_relin": sha(R.host(a_d, 2 * B.nq * B.n))}
+
+
 def graph_time(fn, inner, reps, scratch=()):
     """Device time (ms) per call of fn(i), a sequence of reference launches and device copies:
     one synchronous warm-up run (allocates scratch), then `inner` calls captured in one CUDA graph,
@@ -481,6 +610,20 @@ def time_reference(K, path):
     del big
     torch.cuda.empty_cache()
 
+    rngb = np.random.default_rng(8)
+    B = BfvSetup(15, [50] * 16 + [60, 60], 2, 65537, rngb)
+    SB = Scratch()
+    bins = [(R.dev(O.random_residues(rngb, B.q, B.n, 2), B.n), R.dev(O.random_residues(rngb, B.q, B.n, 2), B.n))
+            for _ in range(4)]
+
+    def bfv(i):
+        a_d, b_d = bins[i % 4]
+        ref_bfv_mul_relin(K, B, a_d, b_d, SB)
+
+    res["bfv_mul_relin_n15_16x50_ms"] = graph_time(bfv, 4, 10, (SB,))
+    del B, SB, bins
+    torch.cuda.empty_cache()
+
     n12 = 4096
     m12 = O.create_coeff_modulus(n12, [60, 60, 60])
     T12 = Tables(12, m12)
@@ -514,6 +657,9 @@ def main(path):
         "tensor_galois_n12": case_tensor_galois(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, [1, -3, 7], 1204),
         "hps_n12": case_hps(K, 12, [50, 50, 50, 50, 60, 60], 2, 65537, 1205),
         "hps_n15": case_hps(K, 15, [50] * 16 + [60, 60], 2, 65537, 1501),
+        "bfv_n12_4x50": case_bfv(K, 12, [50, 50, 50, 50, 60, 60], 2, 65537, 1207),
+        "bfv_n13_a3": case_bfv(K, 13, [50] * 6 + [60] * 3, 3, 65537, 1303),
+        "bfv_n15_16x50": case_bfv(K, 15, [50] * 16 + [60, 60], 2, 65537, 1502),
     }
     with open(path, "w") as f:
         json.dump(res, f, indent=1, sort_keys=True)

@@ -120,3 +120,24 @@ def test_hmult_digests(pg, name):
         ctx.rescale_to_next(ws, ta, out2, 2, chain)
         assert sha(out2) == g["rescaled"], f"two calls, tensor_cores={tc}"
     assert ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("name", [k for k in G if k.startswith("bfv_")])
+def test_bfv_mul_relin_digests(pg, name):
+    g = G[name]
+    n = 1 << g["log_n"]
+    mods = pg.create_coeff_modulus(n, g["bits"])
+    nq = len(g["bits"]) - g["special"]
+    ctx = pg.Context(n, mods, g["special"], scheme=pg.SCHEME_BFV, plain_modulus=g["t"])
+    ws = ctx.workspace()
+    rng = np.random.default_rng(g["seed"])
+    evk = O.random_residues(rng, mods, n, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), n)
+    key = pg.KeySwitchKey(pg.to_device(evk))
+    a = O.random_residues(rng, mods[:nq], n, 2)
+    b = O.random_residues(rng, mods[:nq], n, 2)
+    for tc in (True, False):
+        ctx.tensor_cores = tc
+        ta = pg.to_device(a)
+        ctx.multiply_and_relin(ws, ta, pg.to_device(b), 1, key)
+        assert sha(ta) == g["mul_relin"], f"tensor_cores={tc}"
+    assert ctx.device_status() == 0

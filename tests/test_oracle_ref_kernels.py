@@ -124,3 +124,20 @@ def test_hmult_matches_reference_kernels(golden, name):
     relin = oc.ckks_mul_relin(l, a, b, evk)
     assert sha(relin) == g["multiply_and_relin"]
     assert sha(oc.rescale(l, relin)) == g["rescaled"]
+
+
+@pytest.mark.parametrize("name", _cases("bfv_"))
+def test_bfv_mul_relin_matches_reference_kernels(golden, name):
+    """The whole bfv_mul_relin_hps sequence (HPS conversions with FP64 corrections, NTTs over
+    QlRl, tensor, scale-and-round, key switch in coefficient form) as the reference runs it."""
+    g = golden[name]
+    n = 1 << g["log_n"]
+    mods = O.create_coeff_modulus(n, g["bits"])
+    nq = len(g["bits"]) - g["special"]
+    oc = O.Context(g["log_n"], mods, nq, g["special"], g["t"])
+    rng = np.random.default_rng(g["seed"])
+    dnum = -(-nq // g["special"])
+    evk = O.random_residues(rng, mods, n, 2 * dnum).reshape(dnum, 2, len(mods), n)
+    a = O.random_residues(rng, mods[:nq], n, 2)
+    b = O.random_residues(rng, mods[:nq], n, 2)
+    assert sha(oc.bfv_mul_relin_hps(a, b, evk)) == g["mul_relin"]
