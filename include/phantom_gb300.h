@@ -96,6 +96,14 @@ int fhe_context_ntt_split(const fhe_context *ctx);
 int fhe_context_set_ntt_split(fhe_context *ctx, int l1);
 int fhe_context_autotune(fhe_context *ctx, int *chosen_l1, float *best_us);
 
+/* NTT passes over at most `tiles` tiles of 4096 coefficients (limbs x N / 4096) run the
+ * 8-coefficients-per-thread kernels, which finish a tile in about half the time of the
+ * 16-per-thread kernels and so suit launches of a few waves; larger passes run 16 per thread.
+ * -1 restores the default (512 tiles, measured on GB300); 0 disables the small
+ * kernels.  Every setting gives the same words.  No counterpart in the reference. */
+int fhe_context_ntt_small_launch(const fhe_context *ctx);
+int fhe_context_set_ntt_small_launch(fhe_context *ctx, int tiles);
+
 /* Reads and clears the context's device status word (synchronises the device).  Non-zero
  * means a bounded wait inside a tensor-core kernel gave up and that call's output is invalid.
  * No counterpart in the reference. */

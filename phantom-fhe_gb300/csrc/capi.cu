@@ -2,6 +2,7 @@
 // reference's error classes, chain-index bookkeeping, and dispatch to the kernels.
 #include <algorithm>
 #include <atomic>
+#include <cstdint>
 #include <cstring>
 #include <new>
 #include <stdexcept>
@@ -141,6 +142,19 @@ int fhe_context_set_ntt_split(fhe_context *ctx, int l1) {
         pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
         if (!c.split_ok(l1)) throw std::invalid_argument("unsupported NTT stage split for this degree");
         c.l1_sel = l1;
+    }, false);
+}
+
+int fhe_context_ntt_small_launch(const fhe_context *ctx) {
+    if (!ctx || !ctx->c) return 0;
+    return (int)std::min<long long>(ctx->c->ntt_small_limit(), INT32_MAX);
+}
+
+int fhe_context_set_ntt_small_launch(fhe_context *ctx, int tiles) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        if (tiles < -1) throw std::invalid_argument("small-launch bound must be >= -1");
+        c.ntt_small_tiles = tiles;
     }, false);
 }
 

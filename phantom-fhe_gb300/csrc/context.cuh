@@ -20,6 +20,12 @@
 
 namespace pfg {
 
+// Default small-launch bound for the 8-coefficients-per-thread NTT passes, in 4096-coefficient
+// tiles.  Measured on GB300 (N = 2^16, 30 + 5 primes; N = 2^15 BFV): passes of up to ~500 tiles
+// (the 30-limb inverse transform of a key switch, the 12-limb mod-down transform) are about 1 %
+// faster end to end with 8 per thread; passes of 528 tiles and more are faster with 16.
+constexpr int kNttSmallLaunchTiles = 512;
+
 // values of phantom::scheme_type (include/host/encryptionparams.h)
 enum Scheme { kSchemeNone = 0, kSchemeBGV = 1, kSchemeBFV = 2, kSchemeCKKS = 3 };
 enum MulTech { kMulNone = 0, kMulBEHZ = 1, kMulHPS = 2, kMulHPSOverQ = 3, kMulHPSOverQLeveled = 4 };
@@ -101,6 +107,10 @@ struct Context {
     // NTT stage split: the column pass runs the first l1 stages, the row pass the other l2.  Any
     // supported split gives the same words; the autotuner (fhe_context_autotune) picks one.
     int l1_sel = 0;  // 0: log_n / 2
+    // NTT passes over at most this many 4096-coefficient tiles run 8 coefficients per thread
+    // (NttShape<8>); larger ones 16.  -1: the default, kNttSmallLaunchTiles.
+    int ntt_small_tiles = -1;
+    long long ntt_small_limit() const { return ntt_small_tiles >= 0 ? ntt_small_tiles : kNttSmallLaunchTiles; }
     int l1() const { return l1_sel ? l1_sel : log_n / 2; }
     int l2() const { return log_n - l1(); }
     bool split_ok(int l) const { return l >= 6 && l <= 8 && log_n - l >= 6 && log_n - l <= 9; }

@@ -84,31 +84,51 @@ struct ScaleStore {
 
 // ---------------------------------------------------------------- pass launchers
 
-template <bool FWD, bool LAST, class Map, class Load, class Store>
-void col_pass(const Context &c, int blocks, Map m, Load ld, Store st, cudaStream_t s) {
-    dim3 grid((unsigned)(c.n / kTileElems), (unsigned)blocks);
+template <bool FWD, bool LAST, int E, class Map, class Load, class Store>
+void col_pass_e(const Context &c, dim3 grid, Map m, Load ld, Store st, cudaStream_t s) {
+    constexpr int NT = NttShape<E>::kThreads;
     const NttTables T = c.ntt();
-    count_launch();
     switch (c.l1()) {
-        case 6: ntt_col_pass<6, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
-        case 7: ntt_col_pass<7, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
-        case 8: ntt_col_pass<8, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
+        case 6: ntt_col_pass<6, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
+        case 7: ntt_col_pass<7, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
+        case 8: ntt_col_pass<8, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
         default: break;
     }
 }
 
-template <bool FWD, bool LAST, class Map, class Load, class Store>
-void row_pass(const Context &c, int blocks, Map m, Load ld, Store st, cudaStream_t s) {
-    dim3 grid((unsigned)(c.n / kTileElems), (unsigned)blocks);
+template <bool FWD, bool LAST, int E, class Map, class Load, class Store>
+void row_pass_e(const Context &c, dim3 grid, Map m, Load ld, Store st, cudaStream_t s) {
+    constexpr int NT = NttShape<E>::kThreads;
     const NttTables T = c.ntt();
-    count_launch();
     switch (c.l2()) {
-        case 6: ntt_row_pass<6, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
-        case 7: ntt_row_pass<7, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
-        case 8: ntt_row_pass<8, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
-        case 9: ntt_row_pass<9, FWD, LAST><<<grid, kNttThreads, 0, s>>>(T, m, ld, st); break;
+        case 6: ntt_row_pass<6, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
+        case 7: ntt_row_pass<7, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
+        case 8: ntt_row_pass<8, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
+        case 9: ntt_row_pass<9, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
         default: break;
     }
+}
+
+// One pass over `blocks` limbs (blockIdx.y) of N / 4096 tiles each (blockIdx.x); launches of at
+// most c.ntt_small_limit() tiles take the 8-coefficients-per-thread kernels.
+template <bool FWD, bool LAST, class Map, class Load, class Store>
+void col_pass(const Context &c, int blocks, Map m, Load ld, Store st, cudaStream_t s) {
+    const dim3 grid((unsigned)(c.n / kTileElems), (unsigned)blocks);
+    count_launch();
+    if ((long long)grid.x * grid.y <= c.ntt_small_limit())
+        col_pass_e<FWD, LAST, 8>(c, grid, m, ld, st, s);
+    else
+        col_pass_e<FWD, LAST, 16>(c, grid, m, ld, st, s);
+}
+
+template <bool FWD, bool LAST, class Map, class Load, class Store>
+void row_pass(const Context &c, int blocks, Map m, Load ld, Store st, cudaStream_t s) {
+    const dim3 grid((unsigned)(c.n / kTileElems), (unsigned)blocks);
+    count_launch();
+    if ((long long)grid.x * grid.y <= c.ntt_small_limit())
+        row_pass_e<FWD, LAST, 8>(c, grid, m, ld, st, s);
+    else
+        row_pass_e<FWD, LAST, 16>(c, grid, m, ld, st, s);
 }
 
 // Forward transform: column pass (load functor) -> row pass (store functor); the

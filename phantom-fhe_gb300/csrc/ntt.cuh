@@ -10,7 +10,8 @@
 // the same row, so a transform is two passes: a column pass and a row pass.  Each CTA
 // stages a tile of V whole vectors (columns or rows, V*M = 4096 coefficients, 34 KB) in
 // shared memory with one coalesced sweep, runs all of that pass's stages as register
-// phases of up to four radix-2 stages (16 coefficients per thread, Harvey lazy butterflies,
+// phases of up to four radix-2 stages (16 coefficients per thread; 8 and radix-8 phases for small
+// launches, see NttShape; Harvey lazy butterflies,
 // twiddle and Shoup quotient fetched as one 16-byte pair), and writes the tile back with one
 // coalesced sweep.  Every launch covers all limbs (and polynomials) of an operation; the
 // load and store sweeps take functors so neighbouring element-wise work (base-conversion
@@ -32,35 +33,45 @@ __device__ __forceinline__ TwPair ld_tw(const TwPair *t, uint32_t idx) {
     return TwPair{v.x, v.y};
 }
 
-constexpr int kNttThreads = 256;
 constexpr int kTileElems = 4096;  // V * M coefficients per CTA
 
-__host__ __device__ constexpr int ntt_num_phases(int lm) { return (lm + 3) / 4; }
-__host__ __device__ constexpr int ntt_phase_len(int lm, int ph) {
-    return lm / ntt_num_phases(lm) + (ph < lm % ntt_num_phases(lm) ? 1 : 0);
+// E coefficients per thread: 16 (radix-16 register phases, 256 threads per tile) for large
+// launches, or 8 (radix-8 phases, 512 threads per tile: half the serial work per thread, so
+// about half the time per tile) for launches of a few waves, which are latency-bound.
+template <int E>
+struct NttShape {
+    static_assert(E == 8 || E == 16, "8 or 16 coefficients per thread");
+    static constexpr int LGE = E == 16 ? 4 : 3;
+    static constexpr int kThreads = kTileElems / E;
+    static constexpr int kMinBlocks = E == 16 ? 3 : 2;
+};
+
+__host__ __device__ constexpr int ntt_num_phases(int lm, int lge) { return (lm + lge - 1) / lge; }
+__host__ __device__ constexpr int ntt_phase_len(int lm, int ph, int lge) {
+    return lm / ntt_num_phases(lm, lge) + (ph < lm % ntt_num_phases(lm, lge) ? 1 : 0);
 }
-__host__ __device__ constexpr int ntt_phase_start(int lm, int ph) {
-    return ph == 0 ? 0 : ntt_phase_start(lm, ph - 1) + ntt_phase_len(lm, ph - 1);
+__host__ __device__ constexpr int ntt_phase_start(int lm, int ph, int lge) {
+    return ph == 0 ? 0 : ntt_phase_start(lm, ph - 1, lge) + ntt_phase_len(lm, ph - 1, lge);
 }
 __host__ __device__ constexpr int pad_idx(int x) { return x + (x >> 4); }
 
 // Position inside the vector of member j of thread u's gg-th butterfly group in the phase
 // covering local stages [SA, SA + K): groups are {(hi * 2^K + j) * tmin + lo}, tmin = M >> (SA+K).
-template <int LM, int K, int SA>
+template <int LM, int K, int SA, int E>
 __device__ __forceinline__ int grp_elem(int u, int gg, int j) {
-    constexpr int M = 1 << LM, TPV = M / 16, TMIN = M >> (SA + K);
+    constexpr int M = 1 << LM, TPV = M / E, TMIN = M >> (SA + K);
     const int g = u + gg * TPV;
     return ((g / TMIN) * (1 << K) + j) * TMIN + (g % TMIN);
 }
 
 // Forward (Cooley-Tukey, Harvey lazy: inputs < 4q, outputs < 4q) stages [SA, SA+K) on the
-// 16 registers of thread u.  Twiddle for local stage s of vector `row`:
+// E registers of thread u.  Twiddle for local stage s of vector `row`:
 // tw[(1 << (loff + s)) + (row << s) + (element >> (LM - s))].  All of a group's twiddle pairs
 // are fetched before its butterflies so their latency overlaps.
-template <int LM, int K, int SA>
-__device__ __forceinline__ void fwd_regs(uint64_t (&x)[16], int u, const TwPair *tw, int loff, uint32_t row,
+template <int LM, int K, int SA, int E>
+__device__ __forceinline__ void fwd_regs(uint64_t (&x)[E], int u, const TwPair *tw, int loff, uint32_t row,
                                          uint64_t q) {
-    constexpr int M = 1 << LM, TPV = M / 16, G = 16 >> K, GS = 1 << K, TMIN = M >> (SA + K);
+    constexpr int M = 1 << LM, TPV = M / E, G = E >> K, GS = 1 << K, TMIN = M >> (SA + K);
     const uint64_t q2 = 2 * q;
 #pragma unroll
     for (int gg = 0; gg < G; gg++) {
@@ -91,10 +102,10 @@ __device__ __forceinline__ void fwd_regs(uint64_t (&x)[16], int u, const TwPair 
 // Inverse (Gentleman-Sande, inputs < 2q, outputs < 2q) stages SA+K-1 .. SA.  The global
 // stage-0 butterfly (loff == 0, local stage 0) scales its sum by n^-1; its difference twiddle
 // already carries n^-1 (src/host/ntt.cu:53-55).
-template <int LM, int K, int SA>
-__device__ __forceinline__ void inv_regs(uint64_t (&x)[16], int u, const TwPair *itw, int loff, uint32_t row,
+template <int LM, int K, int SA, int E>
+__device__ __forceinline__ void inv_regs(uint64_t (&x)[E], int u, const TwPair *itw, int loff, uint32_t row,
                                          uint64_t q, uint64_t ninv, uint64_t ninv_s) {
-    constexpr int M = 1 << LM, TPV = M / 16, G = 16 >> K, GS = 1 << K, TMIN = M >> (SA + K);
+    constexpr int M = 1 << LM, TPV = M / E, G = E >> K, GS = 1 << K, TMIN = M >> (SA + K);
     const uint64_t q2 = 2 * q;
 #pragma unroll
     for (int gg = 0; gg < G; gg++) {
@@ -123,49 +134,49 @@ __device__ __forceinline__ void inv_regs(uint64_t (&x)[16], int u, const TwPair 
     }
 }
 
-template <int LM, int K, int SA>
-__device__ __forceinline__ void grp_store(const uint64_t (&x)[16], uint64_t *vec, int u) {
-    constexpr int G = 16 >> K, GS = 1 << K;
+template <int LM, int K, int SA, int E>
+__device__ __forceinline__ void grp_store(const uint64_t (&x)[E], uint64_t *vec, int u) {
+    constexpr int G = E >> K, GS = 1 << K;
 #pragma unroll
     for (int gg = 0; gg < G; gg++)
 #pragma unroll
-        for (int j = 0; j < GS; j++) vec[pad_idx(grp_elem<LM, K, SA>(u, gg, j))] = x[gg * GS + j];
+        for (int j = 0; j < GS; j++) vec[pad_idx(grp_elem<LM, K, SA, E>(u, gg, j))] = x[gg * GS + j];
 }
 
-template <int LM, int K, int SA>
-__device__ __forceinline__ void grp_load(uint64_t (&x)[16], const uint64_t *vec, int u) {
-    constexpr int G = 16 >> K, GS = 1 << K;
+template <int LM, int K, int SA, int E>
+__device__ __forceinline__ void grp_load(uint64_t (&x)[E], const uint64_t *vec, int u) {
+    constexpr int G = E >> K, GS = 1 << K;
 #pragma unroll
     for (int gg = 0; gg < G; gg++)
 #pragma unroll
-        for (int j = 0; j < GS; j++) x[gg * GS + j] = vec[pad_idx(grp_elem<LM, K, SA>(u, gg, j))];
+        for (int j = 0; j < GS; j++) x[gg * GS + j] = vec[pad_idx(grp_elem<LM, K, SA, E>(u, gg, j))];
 }
 
 // Phase order: forward runs phases 0..NPH-1, inverse NPH-1..0.
-template <int LM, bool FWD, int PI>
+template <int LM, bool FWD, int PI, int E>
 struct PhaseAt {
-    static constexpr int NPH = ntt_num_phases(LM);
+    static constexpr int NPH = ntt_num_phases(LM, NttShape<E>::LGE);
     static constexpr int PH = FWD ? PI : NPH - 1 - PI;
-    static constexpr int K = ntt_phase_len(LM, PH);
-    static constexpr int SA = ntt_phase_start(LM, PH);
+    static constexpr int K = ntt_phase_len(LM, PH, NttShape<E>::LGE);
+    static constexpr int SA = ntt_phase_start(LM, PH, NttShape<E>::LGE);
 };
 
 // Runs processing steps PI..NPH-1 on the registers; between steps the vector goes through
 // shared memory (group_store, barrier, group_load of the next step's groups).
-template <int LM, bool FWD, int PI>
-__device__ __forceinline__ void run_phases(uint64_t (&x)[16], uint64_t *vec, int u, const TwPair *tw, int loff,
+template <int LM, bool FWD, int PI, int E>
+__device__ __forceinline__ void run_phases(uint64_t (&x)[E], uint64_t *vec, int u, const TwPair *tw, int loff,
                                            uint32_t row, uint64_t q, uint64_t ninv, uint64_t ninv_s) {
-    using P = PhaseAt<LM, FWD, PI>;
+    using P = PhaseAt<LM, FWD, PI, E>;
     if constexpr (FWD)
-        fwd_regs<LM, P::K, P::SA>(x, u, tw, loff, row, q);
+        fwd_regs<LM, P::K, P::SA, E>(x, u, tw, loff, row, q);
     else
-        inv_regs<LM, P::K, P::SA>(x, u, tw, loff, row, q, ninv, ninv_s);
+        inv_regs<LM, P::K, P::SA, E>(x, u, tw, loff, row, q, ninv, ninv_s);
     if constexpr (PI + 1 < P::NPH) {
-        using Q = PhaseAt<LM, FWD, PI + 1>;
-        grp_store<LM, P::K, P::SA>(x, vec, u);
+        using Q = PhaseAt<LM, FWD, PI + 1, E>;
+        grp_store<LM, P::K, P::SA, E>(x, vec, u);
         __syncthreads();
-        grp_load<LM, Q::K, Q::SA>(x, vec, u);
-        run_phases<LM, FWD, PI + 1>(x, vec, u, tw, loff, row, q, ninv, ninv_s);
+        grp_load<LM, Q::K, Q::SA, E>(x, vec, u);
+        run_phases<LM, FWD, PI + 1, E>(x, vec, u, tw, loff, row, q, ninv, ninv_s);
     }
 }
 
@@ -190,13 +201,14 @@ struct NttTables {
 // Column pass: vectors are V consecutive columns, each of M = N1 elements (stride N2).  Thread
 // t works on column t % V, so every global access of a warp covers whole 128-byte row
 // segments; the first and last register phases load and store global memory directly.
-template <int LM, bool FWD, bool LAST, class Map, class Load, class Store>
-__global__ void __launch_bounds__(kNttThreads, 3) ntt_col_pass(NttTables T, Map map, Load ld, Store st) {
+template <int LM, bool FWD, bool LAST, class Map, class Load, class Store, int E = 16>
+__global__ void __launch_bounds__(NttShape<E>::kThreads, NttShape<E>::kMinBlocks)
+        ntt_col_pass(NttTables T, Map map, Load ld, Store st) {
     constexpr int M = 1 << LM;
     constexpr int V = kTileElems / M;
     constexpr int VP = M + M / 16 + 1;  // padded vector length (odd: column sweeps hit distinct banks)
-    using F = PhaseAt<LM, FWD, 0>;
-    using L = PhaseAt<LM, FWD, F::NPH - 1>;
+    using F = PhaseAt<LM, FWD, 0, E>;
+    using L = PhaseAt<LM, FWD, F::NPH - 1, E>;
     __shared__ uint64_t sm[V * VP];
     int poly, k, tbl;
     if (!map((int)blockIdx.y, poly, k, tbl)) return;  // uniform per block, before any barrier
@@ -204,20 +216,21 @@ __global__ void __launch_bounds__(kNttThreads, 3) ntt_col_pass(NttTables T, Map 
     const int n2 = 1 << T.l2;
     const int v = threadIdx.x % V, u = threadIdx.x / V;
     const uint32_t col = blockIdx.x * V + v;
-    uint64_t x[16];
+    uint64_t x[E];
 #pragma unroll
-    for (int gg = 0; gg < (16 >> F::K); gg++)
+    for (int gg = 0; gg < (E >> F::K); gg++)
 #pragma unroll
         for (int j = 0; j < (1 << F::K); j++)
-            x[gg * (1 << F::K) + j] = ld(poly, k, tbl, (uint32_t)grp_elem<LM, F::K, F::SA>(u, gg, j) * n2 + col);
+            x[gg * (1 << F::K) + j] = ld(poly, k, tbl, (uint32_t)grp_elem<LM, F::K, F::SA, E>(u, gg, j) * n2 + col);
     uint64_t ni = 0, nis = 0;
     if constexpr (!FWD) {
         ni = T.ninv[2 * tbl];
         nis = T.ninv[2 * tbl + 1];
     }
-    run_phases<LM, FWD, 0>(x, sm + v * VP, u, (FWD ? T.tw : T.itw) + ((size_t)tbl << T.log_n), 0, 0u, q, ni, nis);
+    run_phases<LM, FWD, 0, E>(x, sm + v * VP, u, (FWD ? T.tw : T.itw) + ((size_t)tbl << T.log_n), 0, 0u, q, ni,
+                              nis);
 #pragma unroll
-    for (int gg = 0; gg < (16 >> L::K); gg++)
+    for (int gg = 0; gg < (E >> L::K); gg++)
 #pragma unroll
         for (int j = 0; j < (1 << L::K); j++) {
             uint64_t y = x[gg * (1 << L::K) + j];
@@ -225,21 +238,23 @@ __global__ void __launch_bounds__(kNttThreads, 3) ntt_col_pass(NttTables T, Map 
                 if (FWD) y = csub(y, 2 * q);
                 y = csub(y, q);
             }
-            st(poly, k, tbl, (uint32_t)grp_elem<LM, L::K, L::SA>(u, gg, j) * n2 + col, y);
+            st(poly, k, tbl, (uint32_t)grp_elem<LM, L::K, L::SA, E>(u, gg, j) * n2 + col, y);
         }
 }
 
 // Row pass: vectors are V consecutive rows of M = N2 contiguous elements.  The forward pass
 // loads its first phase directly (lane-contiguous) and stores through a coalesced sweep;
 // the inverse pass loads through the sweep and stores its last phase directly.
-template <int LM, bool FWD, bool LAST, class Map, class Load, class Store>
-__global__ void __launch_bounds__(kNttThreads, 3) ntt_row_pass(NttTables T, Map map, Load ld, Store st) {
+template <int LM, bool FWD, bool LAST, class Map, class Load, class Store, int E = 16>
+__global__ void __launch_bounds__(NttShape<E>::kThreads, NttShape<E>::kMinBlocks)
+        ntt_row_pass(NttTables T, Map map, Load ld, Store st) {
     constexpr int M = 1 << LM;
-    constexpr int TPV = M / 16;
+    constexpr int TPV = M / E;
     constexpr int V = kTileElems / M;
     constexpr int VP = M + M / 16 + 1;
-    using F = PhaseAt<LM, FWD, 0>;
-    using L = PhaseAt<LM, FWD, F::NPH - 1>;
+    constexpr int NT = NttShape<E>::kThreads;
+    using F = PhaseAt<LM, FWD, 0, E>;
+    using L = PhaseAt<LM, FWD, F::NPH - 1, E>;
     __shared__ uint64_t sm[V * VP];
     int poly, k, tbl;
     if (!map((int)blockIdx.y, poly, k, tbl)) return;  // uniform per block, before any barrier
@@ -248,42 +263,42 @@ __global__ void __launch_bounds__(kNttThreads, 3) ntt_row_pass(NttTables T, Map 
     const int vv = threadIdx.x / TPV, u = threadIdx.x % TPV;
     const uint32_t row = blockIdx.x * V + vv;
     uint64_t *vec = sm + vv * VP;
-    uint64_t x[16];
+    uint64_t x[E];
     if constexpr (FWD) {
 #pragma unroll
-        for (int gg = 0; gg < (16 >> F::K); gg++)
+        for (int gg = 0; gg < (E >> F::K); gg++)
 #pragma unroll
             for (int j = 0; j < (1 << F::K); j++)
-                x[gg * (1 << F::K) + j] = ld(poly, k, tbl, base + vv * M + grp_elem<LM, F::K, F::SA>(u, gg, j));
+                x[gg * (1 << F::K) + j] = ld(poly, k, tbl, base + vv * M + grp_elem<LM, F::K, F::SA, E>(u, gg, j));
     } else {
 #pragma unroll 4
-        for (int i = threadIdx.x; i < V * M; i += kNttThreads) sm[(i / M) * VP + pad_idx(i % M)] = ld(poly, k, tbl, base + i);
+        for (int i = threadIdx.x; i < V * M; i += NT) sm[(i / M) * VP + pad_idx(i % M)] = ld(poly, k, tbl, base + i);
         __syncthreads();
-        grp_load<LM, F::K, F::SA>(x, vec, u);
+        grp_load<LM, F::K, F::SA, E>(x, vec, u);
     }
     uint64_t ni = 0, nis = 0;
     if constexpr (!FWD) {
         ni = T.ninv[2 * tbl];
         nis = T.ninv[2 * tbl + 1];
     }
-    run_phases<LM, FWD, 0>(x, vec, u, (FWD ? T.tw : T.itw) + ((size_t)tbl << T.log_n), T.l1, row, q, ni, nis);
+    run_phases<LM, FWD, 0, E>(x, vec, u, (FWD ? T.tw : T.itw) + ((size_t)tbl << T.log_n), T.l1, row, q, ni, nis);
     if constexpr (FWD) {
-        grp_store<LM, L::K, L::SA>(x, vec, u);
+        grp_store<LM, L::K, L::SA, E>(x, vec, u);
         __syncthreads();
 #pragma unroll 4
-        for (int i = threadIdx.x; i < V * M; i += kNttThreads) {
+        for (int i = threadIdx.x; i < V * M; i += NT) {
             uint64_t y = sm[(i / M) * VP + pad_idx(i % M)];
             if (LAST) y = csub(csub(y, 2 * q), q);
             st(poly, k, tbl, base + i, y);
         }
     } else {
 #pragma unroll
-        for (int gg = 0; gg < (16 >> L::K); gg++)
+        for (int gg = 0; gg < (E >> L::K); gg++)
 #pragma unroll
             for (int j = 0; j < (1 << L::K); j++) {
                 uint64_t y = x[gg * (1 << L::K) + j];
                 if (LAST) y = csub(y, q);
-                st(poly, k, tbl, base + vv * M + grp_elem<LM, L::K, L::SA>(u, gg, j), y);
+                st(poly, k, tbl, base + vv * M + grp_elem<LM, L::K, L::SA, E>(u, gg, j), y);
             }
     }
 }

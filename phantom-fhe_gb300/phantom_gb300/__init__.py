@@ -62,6 +62,8 @@ def _load():
     L.fhe_context_status.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint)]
     L.fhe_context_ntt_split.argtypes = [_vp]
     L.fhe_context_set_ntt_split.argtypes = [_vp, ctypes.c_int]
+    L.fhe_context_ntt_small_launch.argtypes = [_vp]
+    L.fhe_context_set_ntt_small_launch.argtypes = [_vp, ctypes.c_int]
     L.fhe_context_autotune.argtypes = [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)]
     L.fhe_context_sizes.argtypes = [_vp] + [ctypes.POINTER(_u64)] + [ctypes.POINTER(_sz)] * 4
     L.fhe_context_moduli.argtypes = [_vp, ctypes.POINTER(_u64)]
@@ -203,6 +205,15 @@ class Context:
     @ntt_split.setter
     def ntt_split(self, l1):
         _check(lib.fhe_context_set_ntt_split(self._h, int(l1)))
+
+    @property
+    def ntt_small_launch(self):
+        """NTT passes over at most this many 4096-coefficient tiles use 8 coefficients per thread."""
+        return int(lib.fhe_context_ntt_small_launch(self._h))
+
+    @ntt_small_launch.setter
+    def ntt_small_launch(self, tiles):
+        _check(lib.fhe_context_set_ntt_small_launch(self._h, int(tiles)))
 
     def autotune(self, cache_path=None):
         """Chooses the NTT stage split by timing every supported one (forward + inverse on

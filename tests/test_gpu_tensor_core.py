@@ -157,3 +157,42 @@ def test_every_ntt_split_gives_the_same_words(pg, log_n, splits):
         ctx.ntt_split = 5
     tuned = ctx.autotune()
     assert tuned["ntt_split"] in splits and ctx.ntt_split == tuned["ntt_split"]
+
+
+@pytest.mark.parametrize("log_n", [12, 13, 16])
+def test_small_launch_kernels_give_the_same_words(pg, log_n):
+    """NTT passes with 8 coefficients per thread (small launches) and with 16 give the same
+    words: every pass forced to one shape, then the other, on the NTT, a key switch and HMult."""
+    n = 1 << log_n
+    bits = [60] + [40] * 5 + [60, 60]
+    mods = pg.create_coeff_modulus(n, bits)
+    ctx = pg.Context(n, mods, 2)
+    oc = O.Context(log_n, mods, 6, 2)
+    ws = ctx.workspace()
+    rng = np.random.default_rng(100 + log_n)
+    x = O.random_residues(rng, mods, n, 2)
+    key = O.random_residues(rng, mods, n, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), n)
+    k = pg.KeySwitchKey(pg.to_device(key))
+    ct = O.random_residues(rng, mods[:6], n, 2)
+    c2 = O.random_residues(rng, mods[:6], n, 1)[0]
+    a = O.random_residues(rng, mods[:6], n, 2)
+    b = O.random_residues(rng, mods[:6], n, 2)
+    want_ntt = oc.ntt_fwd(x.reshape(-1, n), tbl=list(range(len(mods))) * 2).reshape(x.shape)
+    want_ks = oc.keyswitch(6, ct, c2, key)
+    want_hm = oc.rescale(6, oc.ckks_mul_relin(6, a, b, key))
+    for tiles in (0, 1 << 30, -1):
+        ctx.ntt_small_launch = tiles
+        t = pg.to_device(x)
+        ctx.ntt_forward(t, 2, len(mods))
+        _eq(t, want_ntt, f"forward NTT, small-launch bound {tiles}")
+        ctx.ntt_inverse(t, 2, len(mods))
+        _eq(t, x, f"round trip, small-launch bound {tiles}")
+        tk = pg.to_device(ct)
+        ctx.keyswitch(ws, tk, pg.to_device(c2), 1, k)
+        _eq(tk, want_ks, f"keyswitch, small-launch bound {tiles}")
+        out = torch.empty((2, 5, n), dtype=torch.int64, device="cuda")
+        ctx.multiply_relin_rescale(ws, pg.to_device(a), pg.to_device(b), out, 1, k)
+        _eq(out, want_hm, f"HMult, small-launch bound {tiles}")
+    assert ctx.ntt_small_launch == 512
+    with pytest.raises(pg.InvalidArgument):
+        ctx.ntt_small_launch = -2
