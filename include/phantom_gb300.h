@@ -281,6 +281,29 @@ int fhe_ckks_decrypt(const fhe_context *ctx, const uint64_t *ct, const uint64_t 
 int fhe_kswitch_keygen(const fhe_context *ctx, fhe_workspace *ws, uint32_t galois_elt, const uint64_t *s_ntt,
                        const uint64_t *a, const int64_t *e, uint64_t *key, void *stream);
 
+/* The reference's device samplers, bit for bit (src/prng.cu:17-244): the same 64-byte seed gives
+ * the same polynomial as the reference's sample_uniform_poly / sample_ternary_poly /
+ * sample_error_poly.  seed is a host pointer to 64 bytes (global_variables::prng_seed_byte_count);
+ * the generator reads the first 56.
+ *   fhe_sample_uniform: out [limbs][N], limb k uniform modulo QP prime k (limbs <= |QP|).
+ *   fhe_sample_ternary: out [N] int64 in {-1, 0, 1}; fhe_sample_cbd: out [N] int64 in [-21, 21]
+ *   (the reference's per-limb residues of the same values). */
+int fhe_sample_uniform(const fhe_context *ctx, const uint8_t *seed, size_t limbs, uint64_t *out, void *stream);
+int fhe_sample_ternary(const fhe_context *ctx, const uint8_t *seed, int64_t *out, void *stream);
+int fhe_sample_cbd(const fhe_context *ctx, const uint8_t *seed, int64_t *out, void *stream);
+
+/* PhantomSecretKey::gen_secretkey (src/secretkey.cu:343-380) with the seed its random_bytes
+ * would have drawn: s_ntt [QP][N] = NTT(ternary(seed)). */
+int fhe_secret_key_from_seed(const fhe_context *ctx, fhe_workspace *ws, const uint8_t *seed, uint64_t *s_ntt,
+                             void *stream);
+
+/* generate_one_kswitch_key (src/secretkey.cu:297-341, encrypt_zero_symmetric :232-295) with the
+ * reference's samplers: digit d's a = uniform(seeds_a + 64 d) over QP (NTT form as drawn) and
+ * its error cbd(seeds_e + 64 d); otherwise as fhe_kswitch_keygen.  seeds_a and seeds_e are host
+ * arrays of dnum 64-byte seeds. */
+int fhe_kswitch_keygen_seeded(const fhe_context *ctx, fhe_workspace *ws, uint32_t galois_elt, const uint64_t *s_ntt,
+                              const uint8_t *seeds_a, const uint8_t *seeds_e, uint64_t *key, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -827,3 +827,93 @@ void orc_bfv_mul_relin_hps(const orc_ctx *c, const uint64_t *a, const uint64_t *
     memcpy(out, o3, 2 * qn * 8);
     free(ea); free(eb); free(t3); free(rt); free(o3);
 }
+
+/* ------------------------------------------------------------------ samplers and key generation */
+
+/* The reference's generator (src/prng.cu:17-131): the Salsa20/20 core over a state whose words
+ * 0-7 and 10-15 are the first 56 seed bytes (little-endian) and words 8-9 the 64-bit nonce, with
+ * the input state added back; one call gives 16 output words. */
+static uint32_t rotl32(uint32_t v, int c) { return (v << c) | (v >> (32 - c)); }
+
+static void salsa_core(const uint8_t *seed, uint64_t nonce, uint32_t out[16]) {
+    uint32_t s[16], x[16];
+    for (int i = 0; i < 14; i++) {
+        const uint8_t *b = seed + 4 * i;
+        uint32_t w = (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+        s[i < 8 ? i : i + 2] = w;
+    }
+    s[8] = (uint32_t)nonce;
+    s[9] = (uint32_t)(nonce >> 32);
+    memcpy(x, s, sizeof(x));
+    static const int qr[8][4] = {{0, 4, 8, 12}, {5, 9, 13, 1}, {10, 14, 2, 6}, {15, 3, 7, 11},
+                                 {0, 1, 2, 3},  {5, 6, 7, 4},  {10, 11, 8, 9}, {15, 12, 13, 14}};
+    for (int r = 0; r < 10; r++)
+        for (int k = 0; k < 8; k++) {
+            uint32_t *a = &x[qr[k][0]], *b = &x[qr[k][1]], *c = &x[qr[k][2]], *d = &x[qr[k][3]];
+            *b ^= rotl32(*a + *d, 7);
+            *c ^= rotl32(*b + *a, 9);
+            *d ^= rotl32(*c + *b, 13);
+            *a ^= rotl32(*d + *c, 18);
+        }
+    for (int i = 0; i < 16; i++) out[i] = x[i] + s[i];
+}
+
+void orc_sample_uniform(const orc_ctx *c, const uint8_t *seed, int limbs, uint64_t *out) {
+    const size_t per = (size_t)c->n / 8, total = per * (size_t)limbs;
+    const uint64_t retry = (uint64_t)limbs * (uint64_t)c->n;
+    for (size_t t = 0; t < total; t++) {
+        const uint64_t q = c->mod[t / per];
+        const uint64_t limit = ~0ull - (~0ull % q) - 1;
+        uint32_t w[16];
+        salsa_core(seed, t, w);
+        uint64_t tries = 1;
+        for (int i = 0; i < 8; i++) {
+            uint64_t v = (uint64_t)w[2 * i] | ((uint64_t)w[2 * i + 1] << 32);
+            while (v > limit) { /* a whole new block, same word position (src/prng.cu:180-186) */
+                salsa_core(seed, t + tries * retry, w);
+                tries++;
+                v = (uint64_t)w[2 * i] | ((uint64_t)w[2 * i + 1] << 32);
+            }
+            out[t * 8 + i] = v % q;
+        }
+    }
+}
+
+static int popc8(uint32_t b) { return __builtin_popcount(b & 0xFF); }
+
+void orc_sample_small(const orc_ctx *c, const uint8_t *seed, int kind, int64_t *out) {
+    for (int i = 0; i < c->n; i++) {
+        uint32_t w[16];
+        salsa_core(seed, (uint64_t)i, w);
+        const uint32_t b0 = w[0] & 0xFF, b1 = (w[0] >> 8) & 0xFF, b2 = (w[0] >> 16) & 0xFF, b3 = w[0] >> 24;
+        const uint32_t b4 = w[1] & 0xFF, b5 = (w[1] >> 8) & 0xFF;
+        if (kind == 0)
+            out[i] = (int64_t)(b0 % 3) - 1; /* src/prng.cu:146-153 */
+        else
+            out[i] = (int64_t)(popc8(b0) + popc8(b1) + popc8(b2 & 0x1F)) -
+                     (int64_t)(popc8(b3) + popc8(b4) + popc8(b5 & 0x1F)); /* src/prng.cu:231-240 */
+    }
+}
+
+/* generate_one_kswitch_key (src/secretkey.cu:297-341): key[d] = (-(a_d s + e_d) + (P mod q_j) s_src
+ * on digit d's limbs, a_d); a [dnum][QP][N] NTT form, e_ntt [dnum][QP][N], s and s_src [QP][N]. */
+void orc_kswitch_key_combine(const orc_ctx *c, const uint64_t *s, const uint64_t *s_src, const uint64_t *a,
+                             const uint64_t *e_ntt, uint64_t *key) {
+    const int qp = c->nQ + c->nP, dnum = (c->nQ + c->nP - 1) / c->nP;
+    const size_t n = (size_t)c->n, qpn = (size_t)qp * n;
+    for (int d = 0; d < dnum; d++)
+        for (int j = 0; j < qp; j++) {
+            const uint64_t q = c->mod[j];
+            uint64_t pm = 1;
+            for (int k = c->nQ; k < qp; k++) pm = orc_mulmod(pm, c->mod[k] % q, q);
+            const int own = j < c->nQ && j >= d * c->nP && j < (d + 1) * c->nP;
+            for (size_t i = 0; i < n; i++) {
+                const size_t x = (size_t)j * n + i;
+                const uint64_t as = (uint64_t)(((u128)a[d * qpn + x] * s[x] + e_ntt[d * qpn + x]) % q);
+                uint64_t b = as ? q - as : 0;
+                if (own) b = (uint64_t)(((u128)b + orc_mulmod(pm, s_src[x], q)) % q);
+                key[2 * d * qpn + x] = b;
+                key[2 * d * qpn + qpn + x] = a[d * qpn + x];
+            }
+        }
+}

@@ -119,6 +119,15 @@ void orc_hps_scale_round_qr_r(const orc_ctx *ctx, const uint64_t *in, uint64_t *
 void orc_bfv_mul_relin_hps(const orc_ctx *ctx, const uint64_t *a, const uint64_t *b,
                            const uint64_t *rlk, uint64_t *out);
 
+/* ---- the reference's samplers (src/prng.cu:17-244) and key combination ---- */
+/* uniform [limbs][N] modulo QP primes 0..limbs-1 (sample_uniform_poly); 64-byte seed */
+void orc_sample_uniform(const orc_ctx *ctx, const uint8_t *seed, int limbs, uint64_t *out);
+/* kind 0: ternary (sample_ternary_poly), 1: centred binomial (sample_error_poly); out [N] */
+void orc_sample_small(const orc_ctx *ctx, const uint8_t *seed, int kind, int64_t *out);
+/* generate_one_kswitch_key's combination (src/secretkey.cu:297-341, polymath.cu:318-370) */
+void orc_kswitch_key_combine(const orc_ctx *ctx, const uint64_t *s, const uint64_t *s_src, const uint64_t *a,
+                             const uint64_t *e_ntt, uint64_t *key);
+
 /* ---- table access for golden checks ---- */
 /* modup constants for level l, digit d: partQlHatInv (size_d) and the size_d x (l+nP-size_d)
  * base-change matrix (row = output prime). */

@@ -77,6 +77,9 @@ def lib():
         L.orc_modup_tables.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _u64p, _u64p]
         L.orc_moddown_tables.argtypes = [ctypes.c_void_p, ctypes.c_int, _u64p, _u64p, _u64p]
         L.orc_hps_tables.argtypes = [ctypes.c_void_p, _dblp, _u64p]
+        L.orc_sample_uniform.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, _u64p]
+        L.orc_sample_small.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
+        L.orc_kswitch_key_combine.argtypes = [ctypes.c_void_p, _u64p, _u64p, _u64p, _u64p, _u64p]
         _lib = L
     return _lib
 
@@ -293,6 +296,26 @@ class Context:
         pinv = np.zeros(l, dtype=np.uint64)
         lib().orc_moddown_tables(self._h, l, p64(phi), p64(mat), p64(pinv))
         return phi, mat, pinv
+
+    def sample_uniform(self, seed, limbs):
+        """The reference's sample_uniform_poly: [limbs][N] modulo QP primes 0..limbs-1."""
+        out = np.zeros((limbs, self.n), dtype=np.uint64)
+        lib().orc_sample_uniform(self._h, bytes(seed), limbs, p64(out))
+        return out
+
+    def sample_small(self, seed, kind):
+        """kind 0: sample_ternary_poly, 1: sample_error_poly, as signed integers [N]."""
+        out = np.zeros(self.n, dtype=np.int64)
+        lib().orc_sample_small(self._h, bytes(seed), kind, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+        return out
+
+    def kswitch_key_combine(self, s, s_src, a, e_ntt):
+        dnum = (self.n_q + self.n_p - 1) // self.n_p
+        qp = self.n_q + self.n_p
+        key = np.zeros((dnum, 2, qp, self.n), dtype=np.uint64)
+        lib().orc_kswitch_key_combine(self._h, p64(np.ascontiguousarray(s)), p64(np.ascontiguousarray(s_src)),
+                                      p64(np.ascontiguousarray(a)), p64(np.ascontiguousarray(e_ntt)), p64(key))
+        return key
 
     def hps_tables(self):
         frac = np.zeros(self.n_q, dtype=np.float64)

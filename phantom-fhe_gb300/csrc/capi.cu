@@ -602,7 +602,63 @@ int fhe_kswitch_keygen(const fhe_context *ctx, fhe_workspace *ws, uint32_t galoi
         if (galois_elt && galois_index(c, galois_elt) < 0) throw std::invalid_argument("Galois elt not present");
         const size_t need = (size_t)(c.beta(c.nQ) + 1) * (c.nQ + c.nP) * c.n + 64;
         if (w.words < need) throw std::logic_error("workspace too small for key generation");
-        pfg::kswitch_keygen(c, galois_elt, s_ntt, a, e, key, w.base, st(stream));
+        pfg::kswitch_keygen(c, galois_elt, s_ntt, a, (size_t)(c.nQ + c.nP) * c.n, e, key, w.base, st(stream));
+    });
+}
+
+int fhe_sample_uniform(const fhe_context *ctx, const uint8_t *seed, size_t limbs, uint64_t *out, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        need_ptr(seed, "seed");
+        need_ptr(out, "out");
+        if (limbs < 1 || limbs > (size_t)(c.nQ + c.nP)) throw std::invalid_argument("limbs out of range");
+        pfg::sample_uniform(c, seed, (int)limbs, out, st(stream));
+    });
+}
+
+int fhe_sample_ternary(const fhe_context *ctx, const uint8_t *seed, int64_t *out, void *stream) {
+    return guarded([&] {
+        need_ptr(seed, "seed");
+        need_ptr(out, "out");
+        pfg::sample_small(ctx_of(ctx), seed, 0, out, st(stream));
+    });
+}
+
+int fhe_sample_cbd(const fhe_context *ctx, const uint8_t *seed, int64_t *out, void *stream) {
+    return guarded([&] {
+        need_ptr(seed, "seed");
+        need_ptr(out, "out");
+        pfg::sample_small(ctx_of(ctx), seed, 1, out, st(stream));
+    });
+}
+
+int fhe_secret_key_from_seed(const fhe_context *ctx, fhe_workspace *ws, const uint8_t *seed, uint64_t *s_ntt,
+                             void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        pfg::Workspace w = ws_of(ctx, ws);
+        need_ptr(seed, "seed");
+        need_ptr(s_ntt, "s_ntt");
+        if (w.words < (size_t)c.n) throw std::logic_error("workspace too small for key generation");
+        pfg::secret_key_from_seed(c, seed, s_ntt, reinterpret_cast<int64_t *>(w.base), st(stream));
+    });
+}
+
+int fhe_kswitch_keygen_seeded(const fhe_context *ctx, fhe_workspace *ws, uint32_t galois_elt, const uint64_t *s_ntt,
+                              const uint8_t *seeds_a, const uint8_t *seeds_e, uint64_t *key, void *stream) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        pfg::Workspace w = ws_of(ctx, ws);
+        need_keyswitching(c);
+        need_ptr(s_ntt, "s");
+        need_ptr(seeds_a, "seeds_a");
+        need_ptr(seeds_e, "seeds_e");
+        need_ptr(key, "key");
+        if (galois_elt && galois_index(c, galois_elt) < 0) throw std::invalid_argument("Galois elt not present");
+        const int dnum = c.beta(c.nQ);
+        const size_t need = (size_t)(dnum + 1) * (c.nQ + c.nP) * c.n + 64 + (size_t)dnum * c.n;
+        if (w.words < need) throw std::logic_error("workspace too small for key generation");
+        pfg::kswitch_keygen_seeded(c, galois_elt, s_ntt, seeds_a, seeds_e, key, w.base, st(stream));
     });
 }
 

@@ -73,8 +73,18 @@ void ckks_bsgs_matvec(Context &c, const Workspace &w, uint64_t *scratch, const u
 void ckks_encrypt_sk(const Context &c, const uint64_t *m, const uint64_t *s_ntt, const uint64_t *a, const int64_t *e,
                      uint64_t *out, int l, cudaStream_t st);
 void ckks_decrypt(const Context &c, const uint64_t *ct, const uint64_t *s_ntt, uint64_t *m, int l, cudaStream_t st);
-void kswitch_keygen(Context &c, uint32_t elt, const uint64_t *s_ntt, const uint64_t *a, const int64_t *e,
-                    uint64_t *key, uint64_t *scratch, cudaStream_t st);
+// a: digit d's uniform polynomial at a + d * a_stride (words)
+void kswitch_keygen(Context &c, uint32_t elt, const uint64_t *s_ntt, const uint64_t *a, size_t a_stride,
+                    const int64_t *e, uint64_t *key, uint64_t *scratch, cudaStream_t st);
+// dst[k][i] = e[i] mod q_k over the first `limbs` QP primes
+void small_to_rns_launch(const Context &c, uint64_t *dst, const int64_t *e, int limbs, cudaStream_t st);
+
+// The reference's device samplers (prng.cu) and key generation from seeds (64-byte seeds).
+void sample_uniform(const Context &c, const uint8_t *seed, int limbs, uint64_t *out, cudaStream_t s);
+void sample_small(const Context &c, const uint8_t *seed, int kind, int64_t *out, cudaStream_t s);
+void secret_key_from_seed(const Context &c, const uint8_t *seed, uint64_t *s_ntt, int64_t *scratch, cudaStream_t s);
+void kswitch_keygen_seeded(Context &c, uint32_t elt, const uint64_t *s_ntt, const uint8_t *seeds_a,
+                           const uint8_t *seeds_e, uint64_t *key, uint64_t *scratch, cudaStream_t s);
 
 // BFV (coefficient form).
 void bfv_keyswitch(const Context &c, const Workspace &w, uint64_t *ct, const uint64_t *c2, int l,

@@ -248,16 +248,16 @@ void ckks_decrypt(const Context &c, const uint64_t *ct, const uint64_t *s_ntt, u
 }
 
 // key[d] = (-(a_d s + e_d) + (P mod q_j) s_from on digit d's Q limbs, a_d) over all QP limbs
-__global__ void kswitch_key_combine(uint64_t *key, const uint64_t *a, const uint64_t *e_ntt, const uint64_t *s,
-                                    const uint64_t *s_from, const uint64_t *p_mod_q, const Mod *mods, int log_n,
-                                    int qp, int nQ, int alpha, int dnum) {
+__global__ void kswitch_key_combine(uint64_t *key, const uint64_t *a, size_t a_stride, const uint64_t *e_ntt,
+                                    const uint64_t *s, const uint64_t *s_from, const uint64_t *p_mod_q,
+                                    const Mod *mods, int log_n, int qp, int nQ, int alpha, int dnum) {
     const size_t qpn = (size_t)qp << log_n, total = (size_t)dnum * qpn;
     for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
         const int d = (int)(x / qpn);
         const size_t r = x - (size_t)d * qpn;
         const int j = (int)(r >> log_n);
         const Mod md = mods[j];
-        const uint64_t av = a[x];
+        const uint64_t av = a[(size_t)d * a_stride + r];  // may alias key's second half (same word)
         uint64_t b = sub_mod(0, add_mod(mul_mod(av, s[r], md), e_ntt[x], md.q), md.q);
         if (j < nQ && j >= d * alpha && j < d * alpha + alpha) b = add_mod(b, mul_mod(p_mod_q[j], s_from[r], md), md.q);
         key[(size_t)d * 2 * qpn + r] = b;
@@ -278,8 +278,14 @@ __global__ void permute_kernel(uint64_t *dst, const uint64_t *src, const uint32_
 
 // s_from: 0 = relinearisation (s^2), else the Galois element (sigma(s)).  `scratch` holds
 // (dnum + 1) x QP x N + 64 words.
-void kswitch_keygen(Context &c, uint32_t elt, const uint64_t *s_ntt, const uint64_t *a, const int64_t *e,
-                    uint64_t *key, uint64_t *scratch, cudaStream_t st) {
+void small_to_rns_launch(const Context &c, uint64_t *dst, const int64_t *e, int limbs, cudaStream_t st) {
+    count_launch();
+    small_to_rns<<<grid_lin((size_t)limbs << c.log_n), 256, 0, st>>>(dst, e, c.d_mods.as<Mod>(), c.log_n, limbs,
+                                                                     1 << 30, 0);
+}
+
+void kswitch_keygen(Context &c, uint32_t elt, const uint64_t *s_ntt, const uint64_t *a, size_t a_stride,
+                    const int64_t *e, uint64_t *key, uint64_t *scratch, cudaStream_t st) {
     const int qp = c.nQ + c.nP, dnum = c.beta(c.nQ);
     const size_t qpn = (size_t)qp << c.log_n;
     uint64_t *s_from = scratch, *e_ntt = scratch + qpn;
@@ -303,7 +309,7 @@ void kswitch_keygen(Context &c, uint32_t elt, const uint64_t *s_ntt, const uint6
     uint64_t *pq_d = scratch + (size_t)(dnum + 1) * qpn;
     cudaMemcpyAsync(pq_d, pq.data(), c.nQ * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
     count_launch();
-    kswitch_key_combine<<<grid_lin((size_t)dnum * qpn), 256, 0, st>>>(key, a, e_ntt, s_ntt, s_from, pq_d,
+    kswitch_key_combine<<<grid_lin((size_t)dnum * qpn), 256, 0, st>>>(key, a, a_stride, e_ntt, s_ntt, s_from, pq_d,
                                                                        c.d_mods.as<Mod>(), c.log_n, qp, c.nQ, c.nP,
                                                                        dnum);
     cudaStreamSynchronize(st);  // the host copy of P mod q_j must outlive the transfer

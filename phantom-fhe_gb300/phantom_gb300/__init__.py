@@ -99,6 +99,12 @@ def _load():
     L.fhe_ckks_encrypt_symmetric.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]
     L.fhe_ckks_decrypt.argtypes = [_vp, _vp, _vp, _vp, _sz, _vp]
     L.fhe_kswitch_keygen.argtypes = [_vp, _vp, ctypes.c_uint32, _vp, _vp, _vp, _vp, _vp]
+    L.fhe_sample_uniform.argtypes = [_vp, ctypes.c_char_p, _sz, _vp, _vp]
+    L.fhe_sample_ternary.argtypes = [_vp, ctypes.c_char_p, _vp, _vp]
+    L.fhe_sample_cbd.argtypes = [_vp, ctypes.c_char_p, _vp, _vp]
+    L.fhe_secret_key_from_seed.argtypes = [_vp, _vp, ctypes.c_char_p, _vp, _vp]
+    L.fhe_kswitch_keygen_seeded.argtypes = [_vp, _vp, ctypes.c_uint32, _vp, ctypes.c_char_p, ctypes.c_char_p, _vp,
+                                            _vp]
     return L
 
 
@@ -352,6 +358,35 @@ class Context:
         """galois_elt 0: relinearisation key (s^2); else the Galois key of that element."""
         _check(lib.fhe_kswitch_keygen(self._h, ws._h, galois_elt, _ptr(s_ntt), _ptr(a), _ptr(e), _ptr(key),
                                       _stream(stream)))
+
+    # --- the reference's samplers (64-byte seeds, bytes)
+    @staticmethod
+    def _seed(seed, count=1):
+        seed = bytes(seed)
+        if len(seed) != 64 * count:
+            raise InvalidArgument(-1, f"expected {count} seed(s) of 64 bytes")
+        return seed
+
+    def sample_uniform(self, seed, limbs, out, stream=None):
+        """out [limbs][N] (int64 view of uint64): the reference's sample_uniform_poly."""
+        _check(lib.fhe_sample_uniform(self._h, self._seed(seed), limbs, _ptr(out), _stream(stream)))
+
+    def sample_ternary(self, seed, out, stream=None):
+        """out [N] int64 in {-1, 0, 1}: the reference's sample_ternary_poly."""
+        _check(lib.fhe_sample_ternary(self._h, self._seed(seed), _ptr(out), _stream(stream)))
+
+    def sample_cbd(self, seed, out, stream=None):
+        """out [N] int64: the reference's sample_error_poly (centred binomial)."""
+        _check(lib.fhe_sample_cbd(self._h, self._seed(seed), _ptr(out), _stream(stream)))
+
+    def secret_key_from_seed(self, ws, seed, s_ntt, stream=None):
+        """s_ntt [QP][N]: the reference's gen_secretkey for this seed."""
+        _check(lib.fhe_secret_key_from_seed(self._h, ws._h, self._seed(seed), _ptr(s_ntt), _stream(stream)))
+
+    def kswitch_keygen_seeded(self, ws, galois_elt, s_ntt, seeds_a, seeds_e, key, stream=None):
+        """The reference's generate_one_kswitch_key with dnum seeds for a and for the errors."""
+        _check(lib.fhe_kswitch_keygen_seeded(self._h, ws._h, galois_elt, _ptr(s_ntt), self._seed(seeds_a, self.dnum),
+                                             self._seed(seeds_e, self.dnum), _ptr(key), _stream(stream)))
 
 
 class Workspace:

@@ -78,7 +78,7 @@ class Tables:
 class Kernels:
     def __init__(self):
         m = {s: R.Module(s) for s in ("fntt_2d", "intt_2d", "ntt_modup", "ntt_moddown", "rns_bconv",
-                                       "eval_key_switch", "rns", "polymath", "galois")}
+                                       "eval_key_switch", "rns", "polymath", "galois", "prng")}
         self.m = m
         k = lambda stem, name: m[stem].kernel(name)  # noqa: E731
         self.f1, self.f2 = k("fntt_2d", "inplace_fnwt_radix8_phase1"), k("fntt_2d", "inplace_fnwt_radix8_phase2")
@@ -106,6 +106,12 @@ class Kernels:
         self.f2_sp = k("fntt_2d", "inplace_fnwt_radix8_phase2_include_special_mod")
         self.bconv_mult1 = k("rns_bconv", "bconv_mult_kernel")
         self.moddown_k = k("rns_bconv", "moddown_kernel")
+        self.s_uniform = k("prng", "sample_uniform_poly")
+        self.s_ternary = k("prng", "sample_ternary_poly")
+        self.s_error = k("prng", "sample_error_poly")
+        self.mul_poly = k("polymath", "multiply_rns_poly")
+        self.mul_add_neg = k("polymath", "multiply_and_add_negate_rns_poly")
+        self.temp_mod_add = k("polymath", "multiply_temp_mod_and_add_rns_poly")
         self.galois = k("galois", "apply_galois_ntt_permutation")
 
     # nwt_2d_radix8_forward_inplace, src/ntt/fntt_2d.cu:620-653
@@ -511,6 +517,63 @@ def case_bfv(K, log_n, bits, special, t, seed):
             "mul_relin": sha(R.host(a_d, 2 * B.nq * B.n))}
 
 
+def seed_dev(seed):
+    """A 64-byte seed in device memory (the reference's prng_seed arrays)."""
+    return R.dev(np.frombuffer(seed, dtype="<u8").astype(np.uint64), 8)
+
+
+def case_prng_keygen(K, log_n, bits, special, seed):
+    """The reference's samplers (src/prng.cu:135-244, launched as src/secretkey.cu does, grid
+    N * limbs / 128) and key generation from seeds: gen_secretkey (src/secretkey.cu:343-380),
+    compute_secret_key_array (:196-230) and generate_one_kswitch_key (:297-341) with
+    encrypt_zero_symmetric (:232-295) for the relinearisation key."""
+    n = 1 << log_n
+    mods = O.create_coeff_modulus(n, bits)
+    nq, qp = len(bits) - special, len(bits)
+    assert nq % special == 0, "the reference's key generation takes dnum = nQ / alpha"
+    dnum = nq // special
+    T = Tables(log_n, mods)
+    rng = np.random.default_rng(seed)
+    seed_u, seed_t, seed_e, seed_s = (rng.bytes(64) for _ in range(4))
+    seeds_a = [rng.bytes(64) for _ in range(dnum)]
+    seeds_e = [rng.bytes(64) for _ in range(dnum)]
+    g = n * qp // BLOCK_GLB
+    out = {"log_n": log_n, "bits": bits, "special": special, "seed": seed}
+    u = R.zeros(qp * n + n)
+    K.s_uniform(g, BLOCK_GLB, 0, u, seed_dev(seed_u), T.mod, n, qp)
+    out["uniform"] = sha(R.host(u, qp * n))
+    K.s_ternary(g, BLOCK_GLB, 0, u, seed_dev(seed_t), T.mod, n, qp)
+    out["ternary"] = sha(R.host(u, qp * n))
+    K.s_error(g, BLOCK_GLB, 0, u, seed_dev(seed_e), T.mod, n, qp)
+    out["error"] = sha(R.host(u, qp * n))
+    # gen_secretkey, then s^2
+    sk = R.zeros(qp * n + n)
+    K.s_ternary(g, BLOCK_GLB, 0, sk, seed_dev(seed_s), T.mod, n, qp)
+    K.ntt_fwd(T, sk, qp, 0)
+    out["secret_key"] = sha(R.host(sk, qp * n))
+    s2 = R.zeros(qp * n + n)
+    K.mul_poly(g, BLOCK_GLB, 0, sk, sk, T.mod, s2, n, qp)
+    # generate_one_kswitch_key(s^2)
+    pk = [R.zeros(2 * qp * n + n) for _ in range(dnum)]
+    for d in range(dnum):
+        err = R.zeros(qp * n + n)
+        K.s_error(g, BLOCK_GLB, 0, err, seed_dev(seeds_e[d]), T.mod, n, qp)
+        K.s_uniform(g, BLOCK_GLB, 0, R.Ptr(pk[d], qp * n), seed_dev(seeds_a[d]), T.mod, n, qp)
+        K.ntt_fwd(T, err, qp, 0)
+        K.mul_add_neg(g, BLOCK_GLB, 0, R.Ptr(pk[d], qp * n), sk, err, T.mod, pk[d], n, qp)
+    ptrs = R.dev(np.array([t.data_ptr() for t in pk], dtype=np.uint64), 8)
+    pmod = [1] * nq
+    for j in range(nq):
+        for p in mods[nq:]:
+            pmod[j] = pmod[j] * p % mods[j]
+    pm, pms = pair(pmod, mods[:nq])
+    K.temp_mod_add(n * dnum * special // BLOCK_GLB, BLOCK_GLB, 0, s2, ptrs, T.mod, ptrs, n, dnum, special, pm, pms)
+    out["relin_key"] = sha(np.concatenate([R.host(t, 2 * qp * n) for t in pk]))
+    out["seeds"] = {"uniform": seed_u.hex(), "ternary": seed_t.hex(), "error": seed_e.hex(), "secret": seed_s.hex(),
+                    "a": [x.hex() for x in seeds_a], "e": [x.hex() for x in seeds_e]}
+    return out
+
+
 def graph_time(fn, inner, reps, scratch=()):
     """Device time (ms) per call of fn(i), a sequence of reference launches and device copies:
     one synchronous warm-up run (allocates scratch), then `inner` calls captured in one CUDA graph,
@@ -657,6 +720,8 @@ def main(path):
         "tensor_galois_n12": case_tensor_galois(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, [1, -3, 7], 1204),
         "hps_n12": case_hps(K, 12, [50, 50, 50, 50, 60, 60], 2, 65537, 1205),
         "hps_n15": case_hps(K, 15, [50] * 16 + [60, 60], 2, 65537, 1501),
+        "prng_keygen_n12": case_prng_keygen(K, 12, [60, 40, 40, 40, 60, 60], 2, 1208),
+        "prng_keygen_n13_a3": case_prng_keygen(K, 13, [60] + [50] * 5 + [60] * 3, 3, 1304),
         "bfv_n12_4x50": case_bfv(K, 12, [50, 50, 50, 50, 60, 60], 2, 65537, 1207),
         "bfv_n13_a3": case_bfv(K, 13, [50] * 6 + [60] * 3, 3, 65537, 1303),
         "bfv_n15_16x50": case_bfv(K, 15, [50] * 16 + [60, 60], 2, 65537, 1502),

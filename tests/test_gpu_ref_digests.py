@@ -141,3 +141,36 @@ def test_bfv_mul_relin_digests(pg, name):
         ctx.multiply_and_relin(ws, ta, pg.to_device(b), 1, key)
         assert sha(ta) == g["mul_relin"], f"tensor_cores={tc}"
     assert ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("name", [k for k in G if k.startswith("prng_")])
+def test_samplers_and_seeded_keygen_digests(pg, name):
+    """The same seeds give the reference's polynomials and keys word for word."""
+    g = G[name]
+    n = 1 << g["log_n"]
+    mods = pg.create_coeff_modulus(n, g["bits"])
+    qp = len(g["bits"])
+    ctx = pg.Context(n, mods, g["special"])
+    ws = ctx.workspace()
+    sd = {k: bytes.fromhex(v) for k, v in g["seeds"].items() if isinstance(v, str)}
+    u = torch.empty((qp, n), dtype=torch.int64, device="cuda")
+    ctx.sample_uniform(sd["uniform"], qp, u)
+    assert sha(u) == g["uniform"]
+    small = torch.empty(n, dtype=torch.int64, device="cuda")
+
+    def residues(t):
+        v = t.cpu().numpy()
+        return np.stack([np.where(v < 0, np.uint64(q) - (-v).astype(np.uint64), v.astype(np.uint64)) for q in mods])
+
+    ctx.sample_ternary(sd["ternary"], small)
+    assert sha(residues(small)) == g["ternary"]
+    ctx.sample_cbd(sd["error"], small)
+    assert sha(residues(small)) == g["error"]
+    s = torch.empty((qp, n), dtype=torch.int64, device="cuda")
+    ctx.secret_key_from_seed(ws, sd["secret"], s)
+    assert sha(s) == g["secret_key"]
+    key = torch.empty((ctx.dnum, 2, qp, n), dtype=torch.int64, device="cuda")
+    ctx.kswitch_keygen_seeded(ws, 0, s, b"".join(bytes.fromhex(h) for h in g["seeds"]["a"]),
+                              b"".join(bytes.fromhex(h) for h in g["seeds"]["e"]), key)
+    assert sha(key) == g["relin_key"]
+    assert ctx.device_status() == 0

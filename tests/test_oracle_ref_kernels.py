@@ -141,3 +141,29 @@ def test_bfv_mul_relin_matches_reference_kernels(golden, name):
     a = O.random_residues(rng, mods[:nq], n, 2)
     b = O.random_residues(rng, mods[:nq], n, 2)
     assert sha(oc.bfv_mul_relin_hps(a, b, evk)) == g["mul_relin"]
+
+
+def _residues(v, mods, n):
+    """Signed small polynomial -> [len(mods)][N] residues (as the reference's samplers store it)."""
+    return np.stack([np.where(v < 0, np.uint64(q) - (-v).astype(np.uint64), v.astype(np.uint64)) for q in mods])
+
+
+@pytest.mark.parametrize("name", _cases("prng_"))
+def test_samplers_and_seeded_keygen_match_reference_kernels(golden, name):
+    """The reference's Salsa20-based samplers (uniform with its rejection rule, ternary, centred
+    binomial) and its seeded secret/relinearisation key generation."""
+    g = golden[name]
+    n = 1 << g["log_n"]
+    mods = O.create_coeff_modulus(n, g["bits"])
+    nq, qp = len(g["bits"]) - g["special"], len(g["bits"])
+    oc = O.Context(g["log_n"], mods, nq, g["special"])
+    sd = {k: bytes.fromhex(v) for k, v in g["seeds"].items() if isinstance(v, str)}
+    assert sha(oc.sample_uniform(sd["uniform"], qp)) == g["uniform"]
+    assert sha(_residues(oc.sample_small(sd["ternary"], 0), mods, n)) == g["ternary"]
+    assert sha(_residues(oc.sample_small(sd["error"], 1), mods, n)) == g["error"]
+    s = oc.ntt_fwd(_residues(oc.sample_small(sd["secret"], 0), mods, n))
+    assert sha(s) == g["secret_key"]
+    s2 = np.array([[int(x) * int(x) % q for x in row] for row, q in zip(s, mods)], dtype=np.uint64)
+    a = np.stack([oc.sample_uniform(bytes.fromhex(h), qp) for h in g["seeds"]["a"]])
+    e = np.stack([oc.ntt_fwd(_residues(oc.sample_small(bytes.fromhex(h), 1), mods, n)) for h in g["seeds"]["e"]])
+    assert sha(oc.kswitch_key_combine(s, s2, a, e)) == g["relin_key"]
