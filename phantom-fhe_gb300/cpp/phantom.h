@@ -24,7 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <bitset>
+#include <array>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -547,21 +547,25 @@ private:
 // a, centred binomial e: popcount of 21 bits minus popcount of 21 bits, as src/prng.cu:222-244).
 class PhantomSecretKey {
 public:
+    // The secret key and every later key or encryption draw their randomness through the
+    // reference's own device samplers (fhe_sample_*), each call keyed by a fresh 64-byte seed as
+    // the reference's random_bytes supplies one; here the seeds come from a 64-bit generator
+    // seeded by std::random_device, or by `seed` for reproducible runs.
     explicit PhantomSecretKey(const PhantomContext &context, std::uint64_t seed = std::random_device{}())
         : rng_(seed) {
         const std::size_t n = context.poly_modulus_degree(), qp = context.coeff_modulus_size(0);
-        std::uniform_int_distribution<int> tern(-1, 1);
-        std::vector<std::int64_t> s(n);
-        for (auto &v : s) v = tern(rng_);
-        std::vector<std::uint64_t> res(qp * n);
-        for (std::size_t j = 0; j < qp; j++) {
-            const std::uint64_t q = context.modulus(j);
-            for (std::size_t k = 0; k < n; k++) res[j * n + k] = s[k] < 0 ? q - 1 : (std::uint64_t)s[k];
-        }
         s_ntt_.reset(qp * n);
-        phantom::detail::cuda_check(
-                cudaMemcpyAsync(s_ntt_.get(), res.data(), res.size() * 8, cudaMemcpyHostToDevice, cudaStreamPerThread));
-        phantom::detail::check(fhe_ntt_forward(context.handle(), s_ntt_.get(), 1, qp, 0, cudaStreamPerThread));
+        const auto sd = seed_bytes();
+        phantom::detail::check(fhe_secret_key_from_seed(context.handle(), context.workspace(), sd.data(), s_ntt_.get(),
+                                                        cudaStreamPerThread));
+        phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
+    }
+    // gen_secretkey with the seed its random_bytes would have returned: the reference's key.
+    PhantomSecretKey(const PhantomContext &context, const std::array<std::uint8_t, 64> &seed) : rng_(0) {
+        const std::size_t n = context.poly_modulus_degree(), qp = context.coeff_modulus_size(0);
+        s_ntt_.reset(qp * n);
+        phantom::detail::check(fhe_secret_key_from_seed(context.handle(), context.workspace(), seed.data(),
+                                                        s_ntt_.get(), cudaStreamPerThread));
         phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
     }
     PhantomSecretKey(const PhantomSecretKey &) = delete;
@@ -578,11 +582,11 @@ public:
     void encrypt_symmetric(const PhantomContext &context, const PhantomPlaintext &plain,
                            PhantomCiphertext &cipher) const {
         const std::size_t n = context.poly_modulus_degree(), l = plain.coeff_modulus_size();
-        std::vector<std::uint64_t> a = uniform(context, 1, l);
-        std::vector<std::int64_t> e = error(1, n);
-        PhantomDeviceBuffer da(a.size()), de(e.size());
-        upload(da, a.data(), a.size());
-        upload(de, e.data(), e.size());
+        PhantomDeviceBuffer da(l * n), de(n);
+        const auto sa = seed_bytes(), se = seed_bytes();
+        phantom::detail::check(fhe_sample_uniform(context.handle(), sa.data(), l, da.get(), cudaStreamPerThread));
+        phantom::detail::check(fhe_sample_cbd(context.handle(), se.data(), reinterpret_cast<std::int64_t *>(de.get()),
+                                              cudaStreamPerThread));
         cipher.resize(context, plain.chain_index(), 2);
         phantom::detail::check(fhe_ckks_encrypt_symmetric(context.handle(), plain.data(), s_ntt_.get(), da.get(),
                                                           reinterpret_cast<const std::int64_t *>(de.get()),
@@ -612,42 +616,28 @@ public:
     }
 
 private:
-    static void upload(PhantomDeviceBuffer &d, const void *h, std::size_t words) {
-        phantom::detail::cuda_check(cudaMemcpyAsync(d.get(), h, words * 8, cudaMemcpyHostToDevice, cudaStreamPerThread));
-        phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
-    }
-    std::vector<std::uint64_t> uniform(const PhantomContext &context, std::size_t polys, std::size_t limbs) const {
-        const std::size_t n = context.poly_modulus_degree();
-        std::vector<std::uint64_t> v(polys * limbs * n);
-        for (std::size_t p = 0; p < polys; p++)
-            for (std::size_t j = 0; j < limbs; j++) {
-                std::uniform_int_distribution<std::uint64_t> u(0, context.modulus(j) - 1);
-                for (std::size_t k = 0; k < n; k++) v[(p * limbs + j) * n + k] = u(rng_);
-            }
-        return v;
-    }
-    std::vector<std::int64_t> error(std::size_t polys, std::size_t n) const {
-        std::vector<std::int64_t> e(polys * n);
-        for (auto &x : e) {
+    std::array<std::uint8_t, 64> seed_bytes() const {
+        std::array<std::uint8_t, 64> b;
+        for (std::size_t i = 0; i < 64; i += 8) {
             const std::uint64_t r = rng_();
-            x = (std::int64_t)std::bitset<21>(r & 0x1FFFFFull).count() -
-                (std::int64_t)std::bitset<21>((r >> 21) & 0x1FFFFFull).count();
+            for (std::size_t k = 0; k < 8; k++) b[i + k] = (std::uint8_t)(r >> (8 * k));
         }
-        return e;
+        return b;
     }
     PhantomRelinKey kswitch_key(const PhantomContext &context, std::uint32_t elt) {
         const std::size_t n = context.poly_modulus_degree(), qp = context.coeff_modulus_size(0);
         std::size_t nq, np, nr, dnum;
         std::uint64_t nn;
         phantom::detail::check(fhe_context_sizes(context.handle(), &nn, &nq, &np, &nr, &dnum));
-        std::vector<std::uint64_t> a = uniform(context, dnum, qp);
-        std::vector<std::int64_t> e = error(dnum, n);
-        PhantomDeviceBuffer da(a.size()), de(e.size()), key(dnum * 2 * qp * n);
-        upload(da, a.data(), a.size());
-        upload(de, e.data(), e.size());
-        phantom::detail::check(fhe_kswitch_keygen(context.handle(), context.workspace(), elt, s_ntt_.get(), da.get(),
-                                                  reinterpret_cast<const std::int64_t *>(de.get()), key.get(),
-                                                  cudaStreamPerThread));
+        std::vector<std::uint8_t> sa(64 * dnum), se(64 * dnum);
+        for (std::size_t d = 0; d < dnum; d++) {
+            const auto a = seed_bytes(), e = seed_bytes();
+            std::copy(a.begin(), a.end(), sa.begin() + 64 * d);
+            std::copy(e.begin(), e.end(), se.begin() + 64 * d);
+        }
+        PhantomDeviceBuffer key(dnum * 2 * qp * n);
+        phantom::detail::check(fhe_kswitch_keygen_seeded(context.handle(), context.workspace(), elt, s_ntt_.get(),
+                                                         sa.data(), se.data(), key.get(), cudaStreamPerThread));
         PhantomRelinKey k;
         k.assign(context, key.get(), dnum);
         return k;
