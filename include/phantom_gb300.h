@@ -281,6 +281,23 @@ int fhe_ckks_decrypt(const fhe_context *ctx, const uint64_t *ct, const uint64_t 
 int fhe_kswitch_keygen(const fhe_context *ctx, fhe_workspace *ws, uint32_t galois_elt, const uint64_t *s_ntt,
                        const uint64_t *a, const int64_t *e, uint64_t *key, void *stream);
 
+/* BFV plaintexts, word for word as the reference:
+ *   fhe_bfv_encode   PhantomBatchEncoder::encode (src/batchencoder.cu:51-92): values (device,
+ *                    count <= N slots; int64 values below zero are taken plus t) -> pt [N] mod t.
+ *                    Needs t prime and t = 1 mod 2N.
+ *   fhe_bfv_decode   PhantomBatchEncoder::decode (:100-118): pt [N] -> values [N].
+ *   fhe_bfv_encrypt_symmetric  PhantomSecretKey::encrypt_symmetric for BFV (src/secretkey.cu:
+ *                    463-485, scalingvariant.cu:10-31) at the first data level: a = uniform
+ *                    [nQ][N] (as fhe_sample_uniform draws it), e = int64 [N]; out [2][nQ][N].
+ *   fhe_bfv_decrypt  PhantomSecretKey::decrypt for BFV (src/secretkey.cu:571-635) with the HPS
+ *                    scale-and-round (src/rns.cu:1519-1665): pt [N] mod t. */
+int fhe_bfv_encode(const fhe_context *ctx, const uint64_t *values, size_t count, uint64_t *pt, void *stream);
+int fhe_bfv_decode(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *pt, uint64_t *values, void *stream);
+int fhe_bfv_encrypt_symmetric(const fhe_context *ctx, const uint64_t *pt, const uint64_t *s_ntt, const uint64_t *a,
+                              const int64_t *e, uint64_t *out, void *stream);
+int fhe_bfv_decrypt(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *ct, size_t chain_index,
+                    const uint64_t *s_ntt, uint64_t *pt, void *stream);
+
 /* The reference's device samplers, bit for bit (src/prng.cu:17-244): the same 64-byte seed gives
  * the same polynomial as the reference's sample_uniform_poly / sample_ternary_poly /
  * sample_error_poly.  seed is a host pointer to 64 bytes (global_variables::prng_seed_byte_count);

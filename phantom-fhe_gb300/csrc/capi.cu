@@ -606,6 +606,56 @@ int fhe_kswitch_keygen(const fhe_context *ctx, fhe_workspace *ws, uint32_t galoi
     });
 }
 
+int fhe_bfv_encode(const fhe_context *ctx, const uint64_t *values, size_t count, uint64_t *pt, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        need_ptr(pt, "pt");
+        if (count && !values) throw std::invalid_argument("values is null");
+        if (count > c.n) throw std::logic_error("values_matrix size is too large");
+        pfg::bfv_encode(c, values, count, pt, st(stream));
+    });
+}
+
+int fhe_bfv_decode(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *pt, uint64_t *values, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        pfg::Workspace w = ws_of(ctx, ws);
+        need_ptr(pt, "pt");
+        need_ptr(values, "values");
+        if (w.words < c.n) throw std::logic_error("workspace too small");
+        pfg::bfv_decode(c, pt, values, w.base, st(stream));
+    });
+}
+
+int fhe_bfv_encrypt_symmetric(const fhe_context *ctx, const uint64_t *pt, const uint64_t *s_ntt, const uint64_t *a,
+                              const int64_t *e, uint64_t *out, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        if (c.scheme != pfg::kSchemeBFV) throw std::invalid_argument("BFV context required");
+        need_ptr(pt, "pt");
+        need_ptr(s_ntt, "s_ntt");
+        need_ptr(a, "a");
+        need_ptr(e, "e");
+        need_ptr(out, "out");
+        pfg::bfv_encrypt_sk(c, pt, s_ntt, a, e, out, st(stream));
+    });
+}
+
+int fhe_bfv_decrypt(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *ct, size_t chain_index,
+                    const uint64_t *s_ntt, uint64_t *pt, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        pfg::Workspace w = ws_of(ctx, ws);
+        if (c.scheme != pfg::kSchemeBFV) throw std::invalid_argument("BFV context required");
+        need_ptr(ct, "ct");
+        need_ptr(s_ntt, "s_ntt");
+        need_ptr(pt, "pt");
+        const int l = level_of(c, chain_index);
+        if (w.words < ((size_t)l << c.log_n)) throw std::logic_error("workspace too small");
+        pfg::bfv_decrypt(c, ct, l, s_ntt, pt, w.base, st(stream));
+    });
+}
+
 int fhe_sample_uniform(const fhe_context *ctx, const uint8_t *seed, size_t limbs, uint64_t *out, void *stream) {
     return guarded([&] {
         const pfg::Context &c = ctx_of(ctx);

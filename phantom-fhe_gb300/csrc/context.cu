@@ -59,6 +59,79 @@ const uint32_t *Context::perm_table(uint32_t elt) {
     return p;
 }
 
+// PhantomBatchEncoder::populate_matrix_reps_index_map (src/batchencoder.cu:25-49), the BFV
+// scaling-variant constants (src/rns.cu negQl_mod_t, tInv_mod_q) and the HPS decryption tables
+// (src/rns.cu:583-668), per data level.
+static uint64_t reverse_low_bits(uint64_t v, int bits) {
+    uint64_t r = 0;
+    for (int i = 0; i < bits; i++) r |= ((v >> i) & 1) << (bits - 1 - i);
+    return r;
+}
+
+static int bit_count(uint64_t v) {
+    int b = 0;
+    while (v) {
+        b++;
+        v >>= 1;
+    }
+    return b;
+}
+
+static void bfv_plain_tables(Context &c, const std::vector<uint64_t> &Q) {
+    using namespace host;
+    using u128 = unsigned __int128;
+    const uint64_t n = c.n, t = c.t;
+    const int nQ = c.nQ;
+    if (c.plain_tbl >= 0) {
+        std::vector<uint32_t> map(n);
+        const uint64_t m = 2 * n, half = n / 2;
+        uint64_t pos = 1;
+        for (uint64_t i = 0; i < half; i++) {
+            map[i] = (uint32_t)reverse_low_bits((pos - 1) >> 1, c.log_n);
+            map[half + i] = (uint32_t)reverse_low_bits((m - pos - 1) >> 1, c.log_n);
+            pos = (pos * 5) & (m - 1);
+        }
+        up(c.bfv_index_map, map);
+    }
+    uint64_t qt = 1;
+    for (uint64_t q : Q) qt = mulmod(qt, q % t, t);
+    c.neg_q_mod_t = qt ? t - qt : 0;
+    c.neg_q_mod_t_shoup = shoup(c.neg_q_mod_t, t);
+    std::vector<uint64_t> tinv(2 * nQ);
+    for (int i = 0; i < nQ; i++) {
+        tinv[2 * i] = invmod(t % Q[i], Q[i]);
+        tinv[2 * i + 1] = shoup(tinv[2 * i], Q[i]);
+    }
+    up(c.bfv_t_inv, tinv);
+    uint64_t qmax = 0;
+    for (uint64_t q : Q) qmax = std::max(qmax, q);
+    c.q_msb = bit_count(qmax);
+    c.t_msb = bit_count(t);
+    const int hf = c.q_msb >> 1;
+    std::vector<uint64_t> mt((size_t)nQ * nQ * 2, 0), mtb((size_t)nQ * nQ * 2, 0);
+    std::vector<double> fr((size_t)nQ * nQ, 0.0), frb((size_t)nQ * nQ, 0.0);
+    for (int l = 1; l <= nQ; l++) {
+        const std::vector<uint64_t> Ql(Q.begin(), Q.begin() + l);
+        for (int i = 0; i < l; i++) {
+            const uint64_t q = Q[i], hat_inv = invmod(prod_mod(Ql, i, q), q);
+            const size_t r = (size_t)(l - 1) * nQ + i;
+            const u128 v = (u128)t * hat_inv;
+            mt[2 * r] = (uint64_t)((v / q) % t);
+            mt[2 * r + 1] = shoup(mt[2 * r], t);
+            fr[r] = (double)(uint64_t)(v % q) / (double)q;
+            const uint64_t hat_inv_b = (uint64_t)(((u128)hat_inv << hf) % q);
+            const u128 vb = (u128)t * hat_inv_b;
+            mtb[2 * r] = (uint64_t)((vb / q) % t);
+            mtb[2 * r + 1] = shoup(mtb[2 * r], t);
+            frb[r] = (double)(uint64_t)(vb % q) / (double)q;
+        }
+    }
+    up(c.dec_mod_t, mt);
+    up(c.dec_mod_t_b, mtb);
+    up(c.dec_frac, fr);
+    up(c.dec_frac_b, frb);
+}
+
 std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, const std::vector<uint64_t> &coeff_modulus,
                                       int special_size, uint64_t plain_modulus,
                                       const std::vector<uint32_t> &galois_elts) {
@@ -123,10 +196,23 @@ std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, cons
         all_tw.insert(all_tw.end(), tw.begin(), tw.end());
         all_itw.insert(all_itw.end(), itw.begin(), itw.end());
     }
+    // BFV batching: t prime and 1 mod 2N gives the plaintext NTT (gpu_plain_tables)
+    if (scheme == kSchemeBFV && plain_modulus > 2 && plain_modulus % (2 * n) == 1 && host::is_prime(plain_modulus)) {
+        c->plain_tbl = (int)np;
+        modw.push_back(plain_modulus);
+        modw.push_back(0);
+        modw.push_back(0);
+        barrett(plain_modulus, modw[3 * np + 1], modw[3 * np + 2]);
+        ninv.resize(2 * np + 2);
+        ntt_tables(log_n, plain_modulus, tw, itw, ninv[2 * np], ninv[2 * np + 1]);
+        all_tw.insert(all_tw.end(), tw.begin(), tw.end());
+        all_itw.insert(all_itw.end(), itw.begin(), itw.end());
+    }
     up(c->d_mods, modw);
     up(c->d_tw, all_tw);
     up(c->d_itw, all_itw);
     up(c->d_ninv, ninv);
+    if (scheme == kSchemeBFV) bfv_plain_tables(*c, Q);
 
     std::vector<uint64_t> pmat((size_t)nQ * nP), pinv(2 * nQ);
     if (nP > 0) {

@@ -93,6 +93,19 @@ struct Context {
     DevBuf tc_hps_q2r, tc_hps_r2q, tc_hps_scale;
     int tc_hps_kp_q2r = 0, tc_hps_kp_r2q = 0, tc_hps_kp_scale = 0;
     bool tc_hps_ok = false;
+    // BFV plaintexts (PhantomBatchEncoder, src/batchencoder.cu; encrypt's scaling variant,
+    // src/scalingvariant.cu; HPS decryption, src/rns.cu:1519-1665): the NTT table of t at index
+    // plain_tbl (-1 when t is not 1 mod 2N: no batching), the slot -> coefficient map, -Q mod t and
+    // t^-1 mod q_i, and per data level l (rows (l - 1) * nQ .. + l) the decryption constants
+    // floor(t QHatInv_i / q_i) mod t (value, Shoup) and frac(t QHatInv_i / q_i), plus the same
+    // with QHatInv_i * 2^(qMSB / 2) for the split variants.
+    int plain_tbl = -1;
+    DevBuf bfv_index_map;  // [N] u32
+    uint64_t neg_q_mod_t = 0, neg_q_mod_t_shoup = 0;
+    DevBuf bfv_t_inv;      // [nQ][2]
+    DevBuf dec_mod_t, dec_mod_t_b;    // [nQ levels][nQ][2]
+    DevBuf dec_frac, dec_frac_b;      // [nQ levels][nQ] doubles
+    int q_msb = 0, t_msb = 0;
     // Galois
     std::vector<uint32_t> galois_elts;
     std::map<uint32_t, std::unique_ptr<DevBuf>> perms;

@@ -86,6 +86,14 @@ void secret_key_from_seed(const Context &c, const uint8_t *seed, uint64_t *s_ntt
 void kswitch_keygen_seeded(Context &c, uint32_t elt, const uint64_t *s_ntt, const uint8_t *seeds_a,
                            const uint8_t *seeds_e, uint64_t *key, uint64_t *scratch, cudaStream_t s);
 
+// BFV plaintexts (bfv_io.cu).
+void bfv_encode(const Context &c, const uint64_t *values, size_t count, uint64_t *pt, cudaStream_t s);
+void bfv_decode(const Context &c, const uint64_t *pt, uint64_t *values, uint64_t *scratch, cudaStream_t s);
+void bfv_encrypt_sk(const Context &c, const uint64_t *m, const uint64_t *s_ntt, const uint64_t *a, const int64_t *e,
+                    uint64_t *out, cudaStream_t s);
+void bfv_decrypt(const Context &c, const uint64_t *ct, int l, const uint64_t *s_ntt, uint64_t *pt, uint64_t *scratch,
+                 cudaStream_t s);
+
 // BFV (coefficient form).
 void bfv_keyswitch(const Context &c, const Workspace &w, uint64_t *ct, const uint64_t *c2, int l,
                    const uint64_t *const *evk, cudaStream_t s);

@@ -99,6 +99,10 @@ def _load():
     L.fhe_ckks_encrypt_symmetric.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]
     L.fhe_ckks_decrypt.argtypes = [_vp, _vp, _vp, _vp, _sz, _vp]
     L.fhe_kswitch_keygen.argtypes = [_vp, _vp, ctypes.c_uint32, _vp, _vp, _vp, _vp, _vp]
+    L.fhe_bfv_encode.argtypes = [_vp, _vp, _sz, _vp, _vp]
+    L.fhe_bfv_decode.argtypes = [_vp, _vp, _vp, _vp, _vp]
+    L.fhe_bfv_encrypt_symmetric.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _vp]
+    L.fhe_bfv_decrypt.argtypes = [_vp, _vp, _vp, _sz, _vp, _vp, _vp]
     L.fhe_sample_uniform.argtypes = [_vp, ctypes.c_char_p, _sz, _vp, _vp]
     L.fhe_sample_ternary.argtypes = [_vp, ctypes.c_char_p, _vp, _vp]
     L.fhe_sample_cbd.argtypes = [_vp, ctypes.c_char_p, _vp, _vp]
@@ -358,6 +362,23 @@ class Context:
         """galois_elt 0: relinearisation key (s^2); else the Galois key of that element."""
         _check(lib.fhe_kswitch_keygen(self._h, ws._h, galois_elt, _ptr(s_ntt), _ptr(a), _ptr(e), _ptr(key),
                                       _stream(stream)))
+
+    # --- BFV plaintexts
+    def bfv_encode(self, values, pt, count=None, stream=None):
+        """values: device int64 [count] slot values (negative taken plus t); pt: [N]."""
+        count = values.numel() if count is None else count
+        _check(lib.fhe_bfv_encode(self._h, _ptr(values), count, _ptr(pt), _stream(stream)))
+
+    def bfv_decode(self, ws, pt, values, stream=None):
+        _check(lib.fhe_bfv_decode(self._h, ws._h, _ptr(pt), _ptr(values), _stream(stream)))
+
+    def bfv_encrypt_symmetric(self, pt, s_ntt, a, e, out, stream=None):
+        """out [2][nQ][N] = BFV encryption of pt [N] under s with uniform a [nQ][N] and error e [N]."""
+        _check(lib.fhe_bfv_encrypt_symmetric(self._h, _ptr(pt), _ptr(s_ntt), _ptr(a), _ptr(e), _ptr(out),
+                                             _stream(stream)))
+
+    def bfv_decrypt(self, ws, ct, chain_index, s_ntt, pt, stream=None):
+        _check(lib.fhe_bfv_decrypt(self._h, ws._h, _ptr(ct), chain_index, _ptr(s_ntt), _ptr(pt), _stream(stream)))
 
     # --- the reference's samplers (64-byte seeds, bytes)
     @staticmethod

@@ -78,7 +78,7 @@ class Tables:
 class Kernels:
     def __init__(self):
         m = {s: R.Module(s) for s in ("fntt_2d", "intt_2d", "ntt_modup", "ntt_moddown", "rns_bconv",
-                                       "eval_key_switch", "rns", "polymath", "galois", "prng")}
+                                       "eval_key_switch", "rns", "polymath", "galois", "prng", "batchencoder")}
         self.m = m
         k = lambda stem, name: m[stem].kernel(name)  # noqa: E731
         self.f1, self.f2 = k("fntt_2d", "inplace_fnwt_radix8_phase1"), k("fntt_2d", "inplace_fnwt_radix8_phase2")
@@ -112,6 +112,14 @@ class Kernels:
         self.mul_poly = k("polymath", "multiply_rns_poly")
         self.mul_add_neg = k("polymath", "multiply_and_add_negate_rns_poly")
         self.temp_mod_add = k("polymath", "multiply_temp_mod_and_add_rns_poly")
+        self.encode_gpu = k("batchencoder", "encode_gpu")
+        self.decode_gpu = k("batchencoder", "decode_gpu")
+        self.add_neg = k("polymath", "add_and_negate_rns_poly")
+        self.add_timesq = k("polymath", "bfv_add_timesQ_overt_kernel")
+        self.mul_add = k("polymath", "multiply_and_add_rns_poly")
+        self.add_poly = k("polymath", "add_rns_poly")
+        self.dec = {v: k("rns", "hps_decrypt_scale_and_round_kernel_" + v)
+                    for v in ("small", "small_lazy", "large", "large_lazy")}
         self.galois = k("galois", "apply_galois_ntt_permutation")
 
     # nwt_2d_radix8_forward_inplace, src/ntt/fntt_2d.cu:620-653
@@ -574,6 +582,115 @@ def case_prng_keygen(K, log_n, bits, special, seed):
     return out
 
 
+def ref_bfv_decrypt(K, T, ct_d, sk, nq, t, q, n):
+    """PhantomSecretKey::bfv_decrypt (src/secretkey.cu:571-635) with
+    DRNSTool::hps_decrypt_scale_and_round (src/rns.cu:583-668 tables, 1634-1665 variant choice)."""
+    g = n * nq // BLOCK_GLB
+    temp = R.zeros(nq * n + n)
+    temp[: nq * n].copy_(ct_d[nq * n: 2 * nq * n])
+    K.ntt_fwd(T, temp, nq, 0)
+    inner = R.zeros(nq * n + n)
+    K.mul_add(g, BLOCK_GLB, 0, temp, sk, inner, T.mod, inner, n, nq)
+    K.ntt_inv(T, inner, nq, 0)
+    K.add_poly(g, BLOCK_GLB, 0, ct_d, inner, T.mod, inner, n, nq)
+    qmsb, tmsb, smsb = max(v.bit_length() for v in q), t.bit_length(), nq.bit_length()
+    big = 1
+    for v in q:
+        big *= v
+    mt, fr, mtb, frb = [], [], [], []
+    hf = qmsb >> 1
+    for v in q:
+        hinv = pow((big // v) % v, -1, v)
+        x = t * hinv
+        mt.append((x // v) % t)
+        fr.append(float(x % v) / float(v))
+        xb = t * ((hinv << hf) % v)
+        mtb.append((xb // v) % t)
+        frb.append(float(xb % v) / float(v))
+    mt_d, mts_d = pair(mt, [t] * nq)
+    mtb_d, mtbs_d = pair(mtb, [t] * nq)
+    fr_d, frb_d = R.dev(np.array(fr), 8), R.dev(np.array(frb), 8)
+    out = R.zeros(n + 8)
+    gd = n // BLOCK_GLB
+    if qmsb + smsb < 52:
+        if qmsb + tmsb + smsb < 52:
+            variant = "small_lazy"
+            K.dec[variant](gd, BLOCK_GLB, 0, out, inner, mt_d, fr_d, t, n, nq)
+        else:
+            variant = "small"
+            K.dec[variant](gd, BLOCK_GLB, 0, out, inner, mt_d, mts_d, fr_d, t, n, nq)
+    elif hf + tmsb + smsb < 52:
+        variant = "large_lazy"
+        K.dec[variant](gd, BLOCK_GLB, 0, out, inner, mt_d, fr_d, mtb_d, frb_d, t, n, nq, hf)
+    else:
+        variant = "large"
+        K.dec[variant](gd, BLOCK_GLB, 0, out, inner, mt_d, mts_d, fr_d, mtb_d, mtbs_d, frb_d, t, n, nq, hf)
+    return R.host(out, n), variant
+
+
+def case_bfv_io(K, log_n, bits, special, t, seed):
+    """PhantomBatchEncoder encode / decode (src/batchencoder.cu:51-118, index map :25-49),
+    BFV encrypt_symmetric (src/secretkey.cu:463-485 with encrypt_zero_symmetric :232-295 in
+    coefficient form and src/scalingvariant.cu:10-31) and bfv_decrypt, on seeded values."""
+    n = 1 << log_n
+    mods = O.create_coeff_modulus(n, bits)
+    nq, qp = len(bits) - special, len(bits)
+    q = mods[:nq]
+    T = Tables(log_n, mods)
+    Tt = Tables(log_n, [t])
+    rng = np.random.default_rng(seed)
+    values = rng.integers(0, t, size=n, dtype=np.uint64)
+    seed_s, seed_a, seed_e = (rng.bytes(64) for _ in range(3))
+    # index map (src/batchencoder.cu:25-49)
+    imap = np.zeros(n, dtype=np.uint64)
+    pos, m = 1, 2 * n
+    for i in range(n // 2):
+        imap[i] = int(format((pos - 1) >> 1, f"0{log_n}b")[::-1], 2)
+        imap[n // 2 + i] = int(format((m - pos - 1) >> 1, f"0{log_n}b")[::-1], 2)
+        pos = (pos * 5) & (m - 1)
+    imap_d = R.dev(imap, 8)
+    pt = R.zeros(n + 8)
+    gs = -(-n // BLOCK_GLB)
+    K.encode_gpu(gs, BLOCK_GLB, 0, pt, R.dev(values, 8), n, imap_d, t, n)
+    K.ntt_inv(Tt, pt, 1, 0)
+    out = {"log_n": log_n, "bits": bits, "special": special, "t": t, "seed": seed, "encode": sha(R.host(pt, n))}
+    cp = R.zeros(n + 8)
+    cp[:n].copy_(pt[:n])
+    K.ntt_fwd(Tt, cp, 1, 0)
+    dec = R.zeros(n + 8)
+    K.decode_gpu(gs, BLOCK_GLB, 0, dec, cp, imap_d, n)
+    assert np.array_equal(R.host(dec, n), values), "reference batch encoder round trip"
+    # secret key over QP (gen_secretkey), then encrypt at the first data level
+    g = n * qp // BLOCK_GLB
+    sk = R.zeros(qp * n + n)
+    K.s_ternary(g, BLOCK_GLB, 0, sk, seed_dev(seed_s), T.mod, n, qp)
+    K.ntt_fwd(T, sk, qp, 0)
+    gq = n * nq // BLOCK_GLB
+    ct = R.zeros(2 * nq * n + n)
+    u = R.zeros(nq * n + n)
+    K.s_error(gq, BLOCK_GLB, 0, u, seed_dev(seed_e), T.mod, n, nq)
+    K.s_uniform(gq, BLOCK_GLB, 0, R.Ptr(ct, nq * n), seed_dev(seed_a), T.mod, n, nq)
+    K.mul_poly(gq, BLOCK_GLB, 0, R.Ptr(ct, nq * n), sk, T.mod, ct, n, nq)
+    K.ntt_inv(T, ct, nq, 0)
+    K.add_neg(gq, BLOCK_GLB, 0, ct, u, T.mod, ct, n, nq)
+    K.ntt_inv(T, R.Ptr(ct, nq * n), nq, 0)
+    big = 1
+    for v in q:
+        big *= v
+    negq = (-big) % t
+    tinv, tinvs = pair([pow(t, -1, v) for v in q], q)
+    K.add_timesq(gq, BLOCK_GLB, 0, ct, pt, negq, (negq << 64) // t, tinv, tinvs, T.mod, t, n, nq)
+    out["encrypt"] = sha(R.host(ct, 2 * nq * n))
+    m_dec, variant = ref_bfv_decrypt(K, T, ct, sk, nq, t, q, n)
+    assert np.array_equal(m_dec, R.host(pt, n)), "reference decryption of its own encryption"
+    out["decrypt_variant"] = variant
+    rnd = R.dev(O.random_residues(rng, q, n, 2), n)
+    m_rnd, _ = ref_bfv_decrypt(K, T, rnd, sk, nq, t, q, n)
+    out["decrypt_random"] = sha(m_rnd)
+    out["seeds"] = {"secret": seed_s.hex(), "a": seed_a.hex(), "e": seed_e.hex()}
+    return out
+
+
 def graph_time(fn, inner, reps, scratch=()):
     """Device time (ms) per call of fn(i), a sequence of reference launches and device copies:
     one synchronous warm-up run (allocates scratch), then `inner` calls captured in one CUDA graph,
@@ -722,6 +839,11 @@ def main(path):
         "hps_n15": case_hps(K, 15, [50] * 16 + [60, 60], 2, 65537, 1501),
         "prng_keygen_n12": case_prng_keygen(K, 12, [60, 40, 40, 40, 60, 60], 2, 1208),
         "prng_keygen_n13_a3": case_prng_keygen(K, 13, [60] + [50] * 5 + [60] * 3, 3, 1304),
+        "bfvio_n12_4x50": case_bfv_io(K, 12, [50, 50, 50, 50, 60, 60], 2, 65537, 1209),
+        "bfvio_n13_6x40": case_bfv_io(K, 13, [40] * 6 + [60], 1, 786433, 1305),
+        "bfvio_n15_16x50": case_bfv_io(K, 15, [50] * 16 + [60, 60], 2, 65537, 1503),
+        "bfvio_n12_3x30": case_bfv_io(K, 12, [30, 30, 30, 60], 1, 65537, 1210),
+        "bfvio_n12_3x60": case_bfv_io(K, 12, [60, 60, 60, 60], 1, 786433, 1211),
         "bfv_n12_4x50": case_bfv(K, 12, [50, 50, 50, 50, 60, 60], 2, 65537, 1207),
         "bfv_n13_a3": case_bfv(K, 13, [50] * 6 + [60] * 3, 3, 65537, 1303),
         "bfv_n15_16x50": case_bfv(K, 15, [50] * 16 + [60, 60], 2, 65537, 1502),

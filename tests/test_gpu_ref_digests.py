@@ -174,3 +174,40 @@ def test_samplers_and_seeded_keygen_digests(pg, name):
                               b"".join(bytes.fromhex(h) for h in g["seeds"]["e"]), key)
     assert sha(key) == g["relin_key"]
     assert ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("name", [k for k in G if k.startswith("bfvio_")])
+def test_bfv_encode_encrypt_decrypt_digests(pg, name):
+    """Batch encoding, symmetric encryption (the reference's samplers) and HPS decryption give the
+    reference's words; the parameter sets cover its four decryption variants."""
+    g = G[name]
+    n = 1 << g["log_n"]
+    mods = pg.create_coeff_modulus(n, g["bits"])
+    nq, qp, t = len(g["bits"]) - g["special"], len(g["bits"]), g["t"]
+    ctx = pg.Context(n, mods, g["special"], scheme=pg.SCHEME_BFV, plain_modulus=t)
+    ws = ctx.workspace()
+    rng = np.random.default_rng(g["seed"])
+    values = rng.integers(0, t, size=n, dtype=np.uint64)
+    sd = dict(zip(("secret", "a", "e"), (rng.bytes(64) for _ in range(3))))  # the generator's draw order
+    assert all(sd[k] == bytes.fromhex(v) for k, v in g["seeds"].items())
+    pt = torch.empty(n, dtype=torch.int64, device="cuda")
+    ctx.bfv_encode(pg.to_device(values), pt)
+    assert sha(pt) == g["encode"]
+    back = torch.empty(n, dtype=torch.int64, device="cuda")
+    ctx.bfv_decode(ws, pt, back)
+    assert np.array_equal(back.cpu().numpy().view(np.uint64), values)
+    s = torch.empty((qp, n), dtype=torch.int64, device="cuda")
+    ctx.secret_key_from_seed(ws, sd["secret"], s)
+    a = torch.empty((nq, n), dtype=torch.int64, device="cuda")
+    ctx.sample_uniform(sd["a"], nq, a)
+    e = torch.empty(n, dtype=torch.int64, device="cuda")
+    ctx.sample_cbd(sd["e"], e)
+    ct = torch.empty((2, nq, n), dtype=torch.int64, device="cuda")
+    ctx.bfv_encrypt_symmetric(pt, s, a, e, ct)
+    assert sha(ct) == g["encrypt"]
+    m = torch.empty(n, dtype=torch.int64, device="cuda")
+    ctx.bfv_decrypt(ws, ct, 1, s, m)
+    assert torch.equal(m, pt), "decryption of the encryption"
+    rnd = pg.to_device(O.random_residues(rng, mods[:nq], n, 2))
+    ctx.bfv_decrypt(ws, rnd, 1, s, m)
+    assert sha(m) == g["decrypt_random"], f"decryption of random words ({g['decrypt_variant']} variant)"
