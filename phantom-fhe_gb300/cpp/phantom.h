@@ -418,6 +418,12 @@ public:
     [[nodiscard]] double scale() const noexcept { return scale_; }
     void set_scale(double s) noexcept { scale_ = s; }
     void set_chain_index(std::size_t c) noexcept { chain_index_ = c; }
+    // raw shape (BFV plaintexts: one limb of N coefficients modulo t, include/plaintext.h)
+    void resize(std::size_t coeff_modulus_size, std::size_t poly_modulus_degree) {
+        limbs_ = coeff_modulus_size;
+        n_ = poly_modulus_degree;
+        if (data_.size() != limbs_ * n_) data_.reset(limbs_ * n_);
+    }
 
 private:
     std::size_t chain_index_ = 0, limbs_ = 0, n_ = 0;
@@ -545,6 +551,53 @@ private:
 // Secret key (PhantomSecretKey, include/secretkey.h:276-330) for CKKS: uniform ternary s, the
 // reference's key and encryption formulas on the GPU, randomness from a host generator (uniform
 // a, centred binomial e: popcount of 21 bits minus popcount of 21 bits, as src/prng.cu:222-244).
+// PhantomBatchEncoder (include/batchencoder.h, src/batchencoder.cu): N slots modulo t <-> a BFV
+// plaintext, on the GPU (fhe_bfv_encode / fhe_bfv_decode).
+class PhantomBatchEncoder {
+public:
+    explicit PhantomBatchEncoder(const PhantomContext &context) : n_(context.poly_modulus_degree()) {
+        if (context.parms().scheme() != phantom::scheme_type::bfv)
+            throw std::invalid_argument("PhantomBatchEncoder only supports BFV/BGV scheme");
+    }
+    [[nodiscard]] std::size_t slot_count() const noexcept { return n_; }
+    void encode(const PhantomContext &context, const std::vector<std::uint64_t> &values_matrix,
+                PhantomPlaintext &destination) const {
+        if (values_matrix.size() > n_) throw std::logic_error("values_matrix size is too large");
+        destination.resize(1, n_);
+        destination.set_chain_index(0);
+        PhantomDeviceBuffer dv(values_matrix.empty() ? 1 : values_matrix.size());
+        phantom::detail::cuda_check(cudaMemcpyAsync(dv.get(), values_matrix.data(), values_matrix.size() * 8,
+                                                    cudaMemcpyHostToDevice, cudaStreamPerThread));
+        phantom::detail::check(fhe_bfv_encode(context.handle(), dv.get(), values_matrix.size(), destination.data(),
+                                              cudaStreamPerThread));
+        phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
+    }
+    [[nodiscard]] PhantomPlaintext encode(const PhantomContext &context,
+                                          const std::vector<std::uint64_t> &values_matrix) const {
+        PhantomPlaintext p;
+        encode(context, values_matrix, p);
+        return p;
+    }
+    void decode(const PhantomContext &context, const PhantomPlaintext &plain,
+                std::vector<std::uint64_t> &destination) const {
+        destination.resize(n_);
+        PhantomDeviceBuffer out(n_);
+        phantom::detail::check(fhe_bfv_decode(context.handle(), context.workspace(), plain.data(), out.get(),
+                                              cudaStreamPerThread));
+        phantom::detail::cuda_check(cudaMemcpyAsync(destination.data(), out.get(), n_ * 8, cudaMemcpyDeviceToHost,
+                                                    cudaStreamPerThread));
+        phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
+    }
+    [[nodiscard]] std::vector<std::uint64_t> decode(const PhantomContext &context, const PhantomPlaintext &plain) const {
+        std::vector<std::uint64_t> v;
+        decode(context, plain, v);
+        return v;
+    }
+
+private:
+    std::size_t n_;
+};
+
 class PhantomSecretKey {
 public:
     // The secret key and every later key or encryption draw their randomness through the
@@ -581,6 +634,7 @@ public:
 
     void encrypt_symmetric(const PhantomContext &context, const PhantomPlaintext &plain,
                            PhantomCiphertext &cipher) const {
+        if (context.parms().scheme() == phantom::scheme_type::bfv) return bfv_encrypt(context, plain, cipher);
         const std::size_t n = context.poly_modulus_degree(), l = plain.coeff_modulus_size();
         PhantomDeviceBuffer da(l * n), de(n);
         const auto sa = seed_bytes(), se = seed_bytes();
@@ -604,6 +658,15 @@ public:
 
     void decrypt(const PhantomContext &context, const PhantomCiphertext &cipher, PhantomPlaintext &plain) {
         if (cipher.size() != 2) throw std::invalid_argument("decrypt needs a size-2 ciphertext");
+        if (context.parms().scheme() == phantom::scheme_type::bfv) {
+            plain.resize(1, context.poly_modulus_degree());
+            plain.set_chain_index(0);
+            phantom::detail::check(fhe_bfv_decrypt(context.handle(), context.workspace(), cipher.data(),
+                                                   cipher.chain_index(), s_ntt_.get(), plain.data(),
+                                                   cudaStreamPerThread));
+            phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
+            return;
+        }
         plain.resize(context, cipher.chain_index());
         phantom::detail::check(fhe_ckks_decrypt(context.handle(), cipher.data(), s_ntt_.get(), plain.data(),
                                                 cipher.chain_index(), cudaStreamPerThread));
@@ -616,6 +679,22 @@ public:
     }
 
 private:
+    // BFV at the first data level (src/secretkey.cu:463-485): a and e from fresh seeds.
+    void bfv_encrypt(const PhantomContext &context, const PhantomPlaintext &plain, PhantomCiphertext &cipher) const {
+        const std::size_t n = context.poly_modulus_degree(), l = context.coeff_modulus_size(1);
+        PhantomDeviceBuffer da(l * n), de(n);
+        const auto sa = seed_bytes(), se = seed_bytes();
+        phantom::detail::check(fhe_sample_uniform(context.handle(), sa.data(), l, da.get(), cudaStreamPerThread));
+        phantom::detail::check(fhe_sample_cbd(context.handle(), se.data(), reinterpret_cast<std::int64_t *>(de.get()),
+                                              cudaStreamPerThread));
+        cipher.resize(context, 1, 2);
+        phantom::detail::check(fhe_bfv_encrypt_symmetric(context.handle(), plain.data(), s_ntt_.get(), da.get(),
+                                                         reinterpret_cast<const std::int64_t *>(de.get()),
+                                                         cipher.data(), cudaStreamPerThread));
+        phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
+        cipher.set_scale(1.0);
+        cipher.set_ntt_form(false);
+    }
     std::array<std::uint8_t, 64> seed_bytes() const {
         std::array<std::uint8_t, 64> b;
         for (std::size_t i = 0; i < 64; i += 8) {
