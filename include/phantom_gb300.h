@@ -101,6 +101,13 @@ int fhe_context_autotune(fhe_context *ctx, int *chosen_l1, float *best_us);
  * 16-per-thread kernels and so suit launches of a few waves; larger passes run 16 per thread.
  * -1 restores the default (512 tiles, measured on GB300); 0 disables the small
  * kernels.  Every setting gives the same words.  No counterpart in the reference. */
+/* Kernel chains of one call launched with programmatic dependent launch (on by default): a
+ * kernel may be scheduled while its predecessor drains its last wave and starts once that
+ * predecessor's writes are visible.  Every setting gives the same words.  No counterpart in the
+ * reference. */
+int fhe_context_launch_overlap(const fhe_context *ctx);
+int fhe_context_set_launch_overlap(fhe_context *ctx, int enable);
+
 int fhe_context_ntt_small_launch(const fhe_context *ctx);
 int fhe_context_set_ntt_small_launch(fhe_context *ctx, int tiles);
 

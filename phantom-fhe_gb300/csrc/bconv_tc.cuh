@@ -18,6 +18,7 @@
 #include <algorithm>
 
 #include "launch.cuh"
+#include "pdl.cuh"
 #include "tc.cuh"
 
 namespace pfg {
@@ -103,6 +104,8 @@ struct NoExtra {
 template <int KSTEPS, bool RESCALE, class Src>
 __global__ void __launch_bounds__(tc::kPipeThreads, 1)
         tc_bconv_kernel(Src src, int ngroups, const Mod *mods, const uint64_t *pinv, unsigned *status, int log_n) {
+    pdl_wait();
+    pdl_release();
     constexpr int KP = KSTEPS * 16, KC = KP / 8;
     constexpr uint32_t SBO = KC * 128;
     constexpr int ABYTES = tc::kRows * KP * 2, BBYTES = tc::kTmemCols * KP * 2;
@@ -313,7 +316,7 @@ void with_tc_ksteps(int kpad, F &&f) {
 // Launch over ngroups groups: one persistent CTA per SM (it owns all 512 tensor-memory columns).
 template <bool RESCALE, class Src>
 void tc_bconv_launch(int kpad, int num_sms, int log_n, const Src &src, int ngroups, const Mod *mods,
-                     const uint64_t *pinv, unsigned *status, cudaStream_t s) {
+                     const uint64_t *pinv, unsigned *status, cudaStream_t s, bool pdl = false) {
     const long long units = (long long)ngroups << (log_n - 7);
     const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>(num_sms, units));
     with_tc_ksteps(kpad, [&]<int KS>() {
@@ -324,8 +327,8 @@ void tc_bconv_launch(int kpad, int num_sms, int log_n, const Src &src, int ngrou
         }();
         (void)attr;
         count_launch();
-        tc_bconv_kernel<KS, RESCALE, Src><<<grid, tc::kPipeThreads, tc::kPipeSmemBytes, s>>>(src, ngroups, mods, pinv,
-                                                                                         status, log_n);
+        launch_pdl(pdl, tc_bconv_kernel<KS, RESCALE, Src>, dim3(grid), dim3(tc::kPipeThreads), tc::kPipeSmemBytes, s,
+                   src, ngroups, mods, pinv, status, log_n);
     });
 }
 

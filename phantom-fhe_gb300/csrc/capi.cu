@@ -158,6 +158,18 @@ int fhe_context_set_ntt_small_launch(fhe_context *ctx, int tiles) {
     }, false);
 }
 
+int fhe_context_launch_overlap(const fhe_context *ctx) {
+    if (!ctx || !ctx->c) return 0;
+    return ctx->c->pdl ? 1 : 0;
+}
+
+int fhe_context_set_launch_overlap(fhe_context *ctx, int enable) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        c.pdl = enable != 0;
+    }, false);
+}
+
 int fhe_context_autotune(fhe_context *ctx, int *chosen_l1, float *best_us) {
     return guarded([&] {
         pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));

@@ -123,6 +123,9 @@ struct Context {
     // NTT passes over at most this many 4096-coefficient tiles run 8 coefficients per thread
     // (NttShape<8>); larger ones 16.  -1: the default, kNttSmallLaunchTiles.
     int ntt_small_tiles = -1;
+    // kernel chains launched with programmatic dependent launch (pdl.cuh); any setting gives the
+    // same words
+    bool pdl = true;
     long long ntt_small_limit() const { return ntt_small_tiles >= 0 ? ntt_small_tiles : kNttSmallLaunchTiles; }
     int l1() const { return l1_sel ? l1_sel : log_n / 2; }
     int l2() const { return log_n - l1(); }

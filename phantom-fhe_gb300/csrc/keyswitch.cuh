@@ -34,6 +34,8 @@ template <class Own, bool OWN_IN_TM>
 __global__ void __launch_bounds__(256) ks_inner_product(uint64_t *cx, const uint64_t *tm, Own own,
                                                         const uint64_t *const *evk, const Mod *mods, int log_n,
                                                         int l, int nQ, int alpha, int beta, int qp) {
+    pdl_wait();
+    pdl_release();
     const int qlp = l + alpha;
     const size_t total = (size_t)qlp << log_n;
     const uint32_t nmask = (1u << log_n) - 1;

@@ -89,9 +89,9 @@ void col_pass_e(const Context &c, dim3 grid, Map m, Load ld, Store st, cudaStrea
     constexpr int NT = NttShape<E>::kThreads;
     const NttTables T = c.ntt();
     switch (c.l1()) {
-        case 6: ntt_col_pass<6, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
-        case 7: ntt_col_pass<7, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
-        case 8: ntt_col_pass<8, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
+        case 6: launch_pdl(c.pdl, ntt_col_pass<6, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
+        case 7: launch_pdl(c.pdl, ntt_col_pass<7, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
+        case 8: launch_pdl(c.pdl, ntt_col_pass<8, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
         default: break;
     }
 }
@@ -101,10 +101,10 @@ void row_pass_e(const Context &c, dim3 grid, Map m, Load ld, Store st, cudaStrea
     constexpr int NT = NttShape<E>::kThreads;
     const NttTables T = c.ntt();
     switch (c.l2()) {
-        case 6: ntt_row_pass<6, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
-        case 7: ntt_row_pass<7, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
-        case 8: ntt_row_pass<8, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
-        case 9: ntt_row_pass<9, FWD, LAST, Map, Load, Store, E><<<grid, NT, 0, s>>>(T, m, ld, st); break;
+        case 6: launch_pdl(c.pdl, ntt_row_pass<6, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
+        case 7: launch_pdl(c.pdl, ntt_row_pass<7, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
+        case 8: launch_pdl(c.pdl, ntt_row_pass<8, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
+        case 9: launch_pdl(c.pdl, ntt_row_pass<9, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
         default: break;
     }
 }

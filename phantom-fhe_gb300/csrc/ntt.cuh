@@ -20,6 +20,7 @@
 #include <cstdint>
 
 #include "modarith.cuh"
+#include "pdl.cuh"
 
 namespace pfg {
 
@@ -204,6 +205,8 @@ struct NttTables {
 template <int LM, bool FWD, bool LAST, class Map, class Load, class Store, int E = 16>
 __global__ void __launch_bounds__(NttShape<E>::kThreads, NttShape<E>::kMinBlocks)
         ntt_col_pass(NttTables T, Map map, Load ld, Store st) {
+    pdl_wait();
+    pdl_release();
     constexpr int M = 1 << LM;
     constexpr int V = kTileElems / M;
     constexpr int VP = M + M / 16 + 1;  // padded vector length (odd: column sweeps hit distinct banks)
@@ -248,6 +251,8 @@ __global__ void __launch_bounds__(NttShape<E>::kThreads, NttShape<E>::kMinBlocks
 template <int LM, bool FWD, bool LAST, class Map, class Load, class Store, int E = 16>
 __global__ void __launch_bounds__(NttShape<E>::kThreads, NttShape<E>::kMinBlocks)
         ntt_row_pass(NttTables T, Map map, Load ld, Store st) {
+    pdl_wait();
+    pdl_release();
     constexpr int M = 1 << LM;
     constexpr int TPV = M / E;
     constexpr int V = kTileElems / M;

@@ -156,7 +156,7 @@ static void pq_bconv_tc_launch(const Context &c, const LevelTables &lt, uint64_t
                     (RESCALE ? lt.tc_rescale_meta : lt.tc_moddown_meta).as<TcOutMeta>(), zc, zd,
                     RESCALE ? lt.tc_rescale_nn : lt.tc_moddown_nn, l, c.nP, c.log_n};
     tc_bconv_launch<RESCALE>(c.tc_kpad, c.num_sms, c.log_n, src, 2, c.d_mods.as<Mod>(), c.p_inv.as<uint64_t>(),
-                             c.d_status.as<unsigned>(), s);
+                             c.d_status.as<unsigned>(), s, c.pdl);
 }
 
 // tensor-core mod-up conversion of every digit
@@ -165,7 +165,7 @@ void modup_bconv_tc_launch(const Context &c, const LevelTables &lt, uint64_t *tm
     const ModupSrc src{y, tm, lt.tc_modup.as<uint16_t>(), lt.tc_modup_meta.as<TcOutMeta>(), lt.tc_modup_nn.as<int>(),
                        l, c.nP, c.log_n, c.tc_kpad};
     tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, lt.beta, c.d_mods.as<Mod>(), c.p_inv.as<uint64_t>(),
-                           c.d_status.as<unsigned>(), s);
+                           c.d_status.as<unsigned>(), s, c.pdl);
 }
 
 template <class C2Load>
@@ -198,9 +198,8 @@ static void inner_product(const Context &c, const KsBuffers &b, Own own, int l, 
     const int qlp = l + c.nP;
     const size_t work = ((size_t)qlp << c.log_n) / 2;
     count_launch();
-    ks_inner_product<Own, false><<<grid_for(work, 256), 256, 0, s>>>(b.cx, b.tm, own, evk, c.d_mods.as<Mod>(),
-                                                                      c.log_n, l, c.nQ, c.nP, c.beta(l),
-                                                                      c.nQ + c.nP);
+    launch_pdl(c.pdl, ks_inner_product<Own, false>, dim3(grid_for(work, 256)), dim3(256), 0, s, b.cx,
+               (const uint64_t *)b.tm, own, evk, c.d_mods.as<Mod>(), c.log_n, l, c.nQ, c.nP, c.beta(l), c.nQ + c.nP);
 }
 
 // Step 4: P limbs of both cx polynomials back to coefficients, times PHatInv.
@@ -220,6 +219,8 @@ __global__ void __launch_bounds__(256) moddown_combine(uint64_t *out0, uint64_t 
                                                        long long vps, const uint64_t *cx, long long cps,
                                                        const uint64_t *pinv, const Mod *mods, int log_n, int l,
                                                        Base base) {
+    pdl_wait();
+    pdl_release();
     const size_t half = (size_t)1 << (log_n - 1), per_poly = (size_t)l * half;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * per_poly;
          e += (size_t)gridDim.x * blockDim.x) {
@@ -259,8 +260,9 @@ static void moddown_ntt(const Context &c, const KsBuffers &b, uint64_t *mid, int
     PtrStore ms{mid, mps, c.log_n};
     ntt_fwd(c, 2 * l, QlpMap{l, 0, l, c.nQ}, PtrLoad{mid, mps, c.log_n}, ms, ms, s);
     count_launch();
-    moddown_combine<Base><<<grid_for((size_t)l << c.log_n, 256), 256, 0, s>>>(
-            out0, out1, mid, mps, b.cx, cps, c.p_inv.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, l, base);
+    launch_pdl(c.pdl, moddown_combine<Base>, dim3(grid_for((size_t)l << c.log_n, 256)), dim3(256), 0, s, out0, out1,
+               (const uint64_t *)mid, mps, (const uint64_t *)b.cx, cps, c.p_inv.as<uint64_t>(), c.d_mods.as<Mod>(),
+               c.log_n, l, base);
 }
 
 void ckks_keyswitch(const Context &c, const Workspace &w, uint64_t *ct, const uint64_t *c2, int l,
@@ -391,6 +393,8 @@ __global__ void __launch_bounds__(256) rescale_combine(uint64_t *out, const uint
                                                        long long cps, const uint64_t *a, const uint64_t *b,
                                                        long long lps, const uint64_t *pinv, const uint64_t *iq,
                                                        const Mod *mods, int log_n, int lm1) {
+    pdl_wait();
+    pdl_release();
     const size_t half = (size_t)1 << (log_n - 1), per_poly = (size_t)lm1 * half;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * per_poly;
          e += (size_t)gridDim.x * blockDim.x) {
@@ -455,9 +459,9 @@ void ckks_mul_relin_rescale(const Context &c, const Workspace &w, const uint64_t
     PtrLoad ld{b.tm, ops, c.log_n};
     ntt_fwd(c, 2 * (l - 1), QlpMap{l - 1, 0, l, c.nQ}, ld, ms, ms, s);
     count_launch();
-    rescale_combine<<<grid_for((size_t)(l - 1) << c.log_n, 256), 256, 0, s>>>(
-            out, b.tm, b.cx, cps, ct1, ct2, lps, c.p_inv.as<uint64_t>(), lt.inv_qlast.as<uint64_t>(), mods, c.log_n,
-            l - 1);
+    launch_pdl(c.pdl, rescale_combine, dim3(grid_for((size_t)(l - 1) << c.log_n, 256)), dim3(256), 0, s, out,
+               (const uint64_t *)b.tm, (const uint64_t *)b.cx, cps, ct1, ct2, lps, c.p_inv.as<uint64_t>(),
+               lt.inv_qlast.as<uint64_t>(), mods, c.log_n, l - 1);
 }
 
 void ckks_tensor(const Context &c, uint64_t *ct1, const uint64_t *ct2, int l, cudaStream_t s);

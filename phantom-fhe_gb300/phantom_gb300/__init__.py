@@ -62,6 +62,8 @@ def _load():
     L.fhe_context_status.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint)]
     L.fhe_context_ntt_split.argtypes = [_vp]
     L.fhe_context_set_ntt_split.argtypes = [_vp, ctypes.c_int]
+    L.fhe_context_launch_overlap.argtypes = [_vp]
+    L.fhe_context_set_launch_overlap.argtypes = [_vp, ctypes.c_int]
     L.fhe_context_ntt_small_launch.argtypes = [_vp]
     L.fhe_context_set_ntt_small_launch.argtypes = [_vp, ctypes.c_int]
     L.fhe_context_autotune.argtypes = [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)]
@@ -215,6 +217,15 @@ class Context:
     @ntt_split.setter
     def ntt_split(self, l1):
         _check(lib.fhe_context_set_ntt_split(self._h, int(l1)))
+
+    @property
+    def launch_overlap(self):
+        """Kernel chains launched with programmatic dependent launch (same words either way)."""
+        return bool(lib.fhe_context_launch_overlap(self._h))
+
+    @launch_overlap.setter
+    def launch_overlap(self, on):
+        _check(lib.fhe_context_set_launch_overlap(self._h, int(bool(on))))
 
     @property
     def ntt_small_launch(self):
