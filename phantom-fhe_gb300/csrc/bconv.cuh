@@ -9,6 +9,7 @@
 // and produces all output limbs with 128-bit accumulation and one Barrett reduction per output;
 // the conversion matrix rows are warp-uniform loads.  Outputs are in coefficient form.
 #pragma once
+#include "pdl.cuh"
 #include "modarith.cuh"
 
 namespace pfg {
@@ -29,6 +30,8 @@ template <int A, bool SCALE>
 __global__ void __launch_bounds__(256) modup_bconv(uint64_t *tm, const uint64_t *y, const uint64_t *phi,
                                                    const uint64_t *mat, const Mod *mods, int log_n, int l,
                                                    int nQ, int alpha) {
+    pdl_wait();
+    pdl_release();
     const int d = blockIdx.y, qlp = l + alpha;
     const int s0 = d * alpha, sz = min(alpha, l - s0);
     const size_t half = (size_t)1 << (log_n - 1);
@@ -77,6 +80,8 @@ template <int A>
 __global__ void __launch_bounds__(256) moddown_bconv(uint64_t *delta, long long dps, const uint64_t *cx,
                                                      long long cps, const uint64_t *pmat, const Mod *mods, int log_n,
                                                      int l, int nP) {
+    pdl_wait();
+    pdl_release();
     const int t = blockIdx.y;
     const size_t half = (size_t)1 << (log_n - 1);
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < half; e += (size_t)gridDim.x * blockDim.x) {
@@ -119,6 +124,8 @@ __global__ void __launch_bounds__(256) rescale_fused_bconv(uint64_t *w, long lon
                                                            long long cps, const uint64_t *zc, const uint64_t *zd,
                                                            const uint64_t *pmat, const uint64_t *pinv,
                                                            const Mod *mods, int log_n, int l, int nP) {
+    pdl_wait();
+    pdl_release();
     const int t = blockIdx.y;
     const size_t half = (size_t)1 << (log_n - 1);
     const Mod ml = mods[l - 1];

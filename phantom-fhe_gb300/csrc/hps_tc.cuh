@@ -19,6 +19,7 @@
 // issues ceil(K / 16) MMAs from one thread into 256 tensor-memory columns and runs the epilogue
 // with 8 warps (lane quarter x half of the outputs).  Bounded wait on the MMA barrier.
 #pragma once
+#include "pdl.cuh"
 #include "tc.cuh"
 
 namespace pfg {
@@ -45,6 +46,8 @@ struct HpsTcArgs {
 
 template <int MODE>
 __global__ void __launch_bounds__(256, 1) hps_tc_kernel(HpsTcArgs a) {
+    pdl_wait();
+    pdl_release();
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t tmem_slot, ok_flag;
     __shared__ __align__(8) uint64_t bar;

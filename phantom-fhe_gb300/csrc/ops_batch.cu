@@ -234,6 +234,8 @@ struct BLastStore {
 // (keyswitch_inplace's add_to_ct_kernel, src/rns_bconv.cu:763-769), two coefficients per thread.
 __global__ void __launch_bounds__(256) batch_keyswitch_combine(BItemsRef r, Prefix pre, const uint64_t *pinv,
                                                                const Mod *mods) {
+    pdl_wait();
+    pdl_release();
     const int c = pre.find(blockIdx.y), t = blockIdx.y - pre.p[c];
     const int lc = r.it.l[c], log_n = r.log_n;
     const size_t half = (size_t)1 << (log_n - 1), work = (size_t)lc * half;
@@ -256,6 +258,8 @@ __global__ void __launch_bounds__(256) batch_keyswitch_combine(BItemsRef r, Pref
 // with v the forward NTT of w (stored plainly in the item's scratch), two coefficients per thread.
 __global__ void __launch_bounds__(256) batch_rescale_combine(BItemsRef r, Prefix pre, const uint64_t *pinv,
                                                              const Mod *mods) {
+    pdl_wait();
+    pdl_release();
     const int c = pre.find(blockIdx.y), t = blockIdx.y - pre.p[c];
     const int lc = r.it.l[c], log_n = r.log_n;
     const size_t half = (size_t)1 << (log_n - 1), work = (size_t)(lc - 1) * half;
@@ -285,6 +289,8 @@ __global__ void __launch_bounds__(256) batch_rescale_combine(BItemsRef r, Prefix
 // Mod-up base conversion for (item, digit) = block row.
 template <int A>
 __global__ void __launch_bounds__(256) modup_bconv_batch(BItemsRef r, Prefix pre, const Mod *mods, int nQ) {
+    pdl_wait();
+    pdl_release();
     const int c = pre.find(blockIdx.y), d = blockIdx.y - pre.p[c];
     const int l = r.it.l[c], alpha = r.alpha, qlp = l + alpha, log_n = r.log_n;
     const int s0 = d * alpha, sz = min(alpha, l - s0);
@@ -327,6 +333,8 @@ __global__ void __launch_bounds__(256) modup_bconv_batch(BItemsRef r, Prefix pre
 // HBM for the first item and from cache for the others.
 __global__ void __launch_bounds__(256) ks_inner_product_batch(BItemsRef r, const uint64_t *const *evk,
                                                               const Mod *mods, int nQ, int qp) {
+    pdl_wait();
+    pdl_release();
     const int tk = blockIdx.y, alpha = r.alpha, log_n = r.log_n;
     const Mod m = mods[tk];
     const size_t half = (size_t)1 << (log_n - 1);
@@ -377,6 +385,8 @@ __global__ void __launch_bounds__(256) ks_inner_product_batch(BItemsRef r, const
 template <int A>
 __global__ void __launch_bounds__(256) rescale_bconv_batch(BItemsRef r, Prefix pre, const uint64_t *pmat,
                                                            const uint64_t *pinv, const Mod *mods) {
+    pdl_wait();
+    pdl_release();
     const int c = pre.find(blockIdx.y), t = blockIdx.y - pre.p[c];
     const int l = r.it.l[c], nP = r.alpha, log_n = r.log_n;
     uint64_t *ws = r.it.ws[c];
@@ -564,11 +574,11 @@ void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t it
                 src.log_n = c.log_n;
                 src.kpad = c.tc_kpad;
                 tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, pre.p[count], mods,
-                                       c.p_inv.as<uint64_t>(), c.d_status.as<unsigned>(), s);
+                                       c.p_inv.as<uint64_t>(), c.d_status.as<unsigned>(), s, c.pdl);
             } else {
                 with_digit_bound(alpha, [&]<int A>() {
                     count_launch();
-                    modup_bconv_batch<A><<<dim3(gx, pre.p[count]), 256, 0, s>>>(r, pre, mods, nQ);
+                    launch_pdl(c.pdl, modup_bconv_batch<A>, dim3(dim3(gx, pre.p[count])), dim3(256), 0, s, r, pre, mods, nQ);
                 });
             }
         }
@@ -581,7 +591,7 @@ void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t it
         }
         // 4. inner product, one block row per key limb
         count_launch();
-        ks_inner_product_batch<<<dim3(gx, (unsigned)(nQ + alpha)), 256, 0, s>>>(r, rlk, mods, nQ, nQ + alpha);
+        launch_pdl(c.pdl, ks_inner_product_batch, dim3(dim3(gx, (unsigned)(nQ + alpha))), dim3(256), 0, s, r, rlk, mods, nQ, nQ + alpha);
         // 5. inverse NTT of the P limbs (x PHatInv), cx limb l-1 and tensor limb l-1
         {
             BLastLimbMap lm{make_prefix(count, [&](int) { return 2 * (alpha + 2); }), {}, nQ, alpha};
@@ -607,13 +617,12 @@ void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t it
             src.alpha = alpha;
             src.log_n = c.log_n;
             tc_bconv_launch<true>(c.tc_kpad, c.num_sms, c.log_n, src, 2 * count, mods, c.p_inv.as<uint64_t>(),
-                                  c.d_status.as<unsigned>(), s);
+                                  c.d_status.as<unsigned>(), s, c.pdl);
         } else {
             Prefix pre = make_prefix(count, [&](int) { return 2; });
             with_digit_bound(alpha, [&]<int A>() {
                 count_launch();
-                rescale_bconv_batch<A><<<dim3(gx, pre.p[count]), 256, 0, s>>>(r, pre, c.p_mat.as<uint64_t>(),
-                                                                               c.p_inv.as<uint64_t>(), mods);
+                launch_pdl(c.pdl, rescale_bconv_batch<A>, dim3(dim3(gx, pre.p[count])), dim3(256), 0, s, r, pre, c.p_mat.as<uint64_t>(), c.p_inv.as<uint64_t>(), mods);
             });
         }
         // 7. forward NTT of w with the final combine
@@ -624,7 +633,7 @@ void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t it
             ntt_fwd2(c, fm.pre.p[count], fm, w, w, w, w, s);
             Prefix pre = make_prefix(count, [&](int) { return 2; });
             count_launch();
-            batch_rescale_combine<<<dim3(gx, pre.p[count]), 256, 0, s>>>(r, pre, c.p_inv.as<uint64_t>(), mods);
+            launch_pdl(c.pdl, batch_rescale_combine, dim3(dim3(gx, pre.p[count])), dim3(256), 0, s, r, pre, c.p_inv.as<uint64_t>(), mods);
         }
     }
 }
@@ -693,7 +702,7 @@ void ckks_keyswitch_batch(const Context &c, uint64_t *ws_base, size_t item_words
             src.log_n = c.log_n;
             src.kpad = c.tc_kpad;
             tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, pre.p[count], mods, c.p_inv.as<uint64_t>(),
-                                   c.d_status.as<unsigned>(), s);
+                                   c.d_status.as<unsigned>(), s, c.pdl);
         }
         {
             BModupMap mm{make_prefix(count, [&](int i) { return beta_of(i) * (lvl(i) + alpha); }), {}, nQ, alpha};
@@ -703,7 +712,7 @@ void ckks_keyswitch_batch(const Context &c, uint64_t *ws_base, size_t item_words
         }
         // 4. inner product, one block row per key limb
         count_launch();
-        ks_inner_product_batch<<<dim3(gx, (unsigned)(nQ + alpha)), 256, 0, s>>>(r, evk, mods, nQ, nQ + alpha);
+        launch_pdl(c.pdl, ks_inner_product_batch, dim3(dim3(gx, (unsigned)(nQ + alpha))), dim3(256), 0, s, r, evk, mods, nQ, nQ + alpha);
         // 5. inverse NTT of the P limbs of both cx polynomials, times PHatInv
         {
             BPMap pm{make_prefix(count, [&](int) { return 2 * alpha; }), alpha, nQ};
@@ -727,7 +736,7 @@ void ckks_keyswitch_batch(const Context &c, uint64_t *ws_base, size_t item_words
             src.alpha = alpha;
             src.log_n = c.log_n;
             tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, 2 * count, mods, c.p_inv.as<uint64_t>(),
-                                   c.d_status.as<unsigned>(), s);
+                                   c.d_status.as<unsigned>(), s, c.pdl);
         }
         // 7. forward NTT of delta, then ct += (cx - NTT(delta)) P^-1
         {
@@ -737,7 +746,7 @@ void ckks_keyswitch_batch(const Context &c, uint64_t *ws_base, size_t item_words
             ntt_fwd2(c, fm.pre.p[count], fm, w, w, w, w, s);
             Prefix pre = make_prefix(count, [&](int) { return 2; });
             count_launch();
-            batch_keyswitch_combine<<<dim3(gx, pre.p[count]), 256, 0, s>>>(r, pre, c.p_inv.as<uint64_t>(), mods);
+            launch_pdl(c.pdl, batch_keyswitch_combine, dim3(dim3(gx, pre.p[count])), dim3(256), 0, s, r, pre, c.p_inv.as<uint64_t>(), mods);
         }
     }
 }

@@ -43,6 +43,8 @@ __global__ void __launch_bounds__(256) hps_bconv(uint64_t *out, long long ops, c
                                                  const Mod *mods, int ib0, int ni, int ob0, int no,
                                                  const uint64_t *hat_inv, const double *inv, const uint64_t *mat,
                                                  const uint64_t *alpha_tab, int log_n) {
+    pdl_wait();
+    pdl_release();
     extern __shared__ uint64_t sh[];
     uint64_t *ys = sh;                                  // [ni][kHpsTile]
     long long *vs = reinterpret_cast<long long *>(sh + (size_t)ni * kHpsTile);  // [kHpsTile]
@@ -87,6 +89,8 @@ __global__ void __launch_bounds__(256) hps_scale_round_to_q(uint64_t *out, long 
                                                             const uint64_t *r_hat_inv, const double *r_inv,
                                                             const uint64_t *r2q, const uint64_t *r2q_alpha,
                                                             int log_n) {
+    pdl_wait();
+    pdl_release();
     extern __shared__ uint64_t sh[];
     const int nqr = nQ + nR;
     uint64_t *xs = sh;                                   // [nQ + nR][kHpsTile]
@@ -204,6 +208,8 @@ struct BfvCxStore {
 __global__ void bfv_moddown_combine(uint64_t *out, long long ops, const uint64_t *base, long long bps,
                                     const uint64_t *cx, long long cps, const uint64_t *pmat, const uint64_t *pinv,
                                     const Mod *mods, int l, int nP, int log_n) {
+    pdl_wait();
+    pdl_release();
     const size_t total = (size_t)2 * l << log_n;
     const uint32_t nmask = (1u << log_n) - 1;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
@@ -234,30 +240,24 @@ static void bfv_keyswitch_to(const Context &c, uint64_t *scratch, uint64_t *out,
         const BfvModupSrc src{c2, tm, lt.tc_modup.as<uint16_t>(), lt.tc_modup_meta.as<TcOutMeta>(),
                               lt.tc_modup_nn.as<int>(), lt.part_hat_inv.as<uint64_t>(), l, alpha, c.log_n, c.tc_kpad};
         tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, beta, c.d_mods.as<Mod>(), c.p_inv.as<uint64_t>(),
-                               c.d_status.as<unsigned>(), s);
+                               c.d_status.as<unsigned>(), s, c.pdl);
     } else {
         with_digit_bound(alpha, [&]<int A>() {
             count_launch();
-            modup_bconv<A, true><<<dim3((unsigned)std::max<uint64_t>(1, c.n / 512), beta), 256, 0, s>>>(
-                    tm, c2, lt.part_hat_inv.as<uint64_t>(), lt.modup_mat.as<uint64_t>(), c.d_mods.as<Mod>(),
-                    c.log_n, l, c.nQ, alpha);
+            launch_pdl(c.pdl, modup_bconv<A, true>, dim3(dim3((unsigned)std::max<uint64_t>(1, c.n / 512), beta)), dim3(256), 0, s, tm, c2, lt.part_hat_inv.as<uint64_t>(), lt.modup_mat.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, l, c.nQ, alpha);
         });
     }
     PtrStore ts{tm, tps, c.log_n};
     ntt_fwd(c, beta * qlp, ModupMap{qlp, l, c.nQ, alpha, false}, PtrLoad{tm, tps, c.log_n}, ts, ts, s);
     const size_t work = ((size_t)qlp << c.log_n) / 2;
     count_launch();
-    ks_inner_product<NoOwn, true><<<grid_for_bfv(work, 256), 256, 0, s>>>(cx, tm, NoOwn{}, evk, c.d_mods.as<Mod>(),
-                                                                          c.log_n, l, c.nQ, alpha, beta,
-                                                                          c.nQ + c.nP);
+    launch_pdl(c.pdl, ks_inner_product<NoOwn, true>, dim3(grid_for_bfv(work, 256)), dim3(256), 0, s, cx, tm, NoOwn{}, evk, c.d_mods.as<Mod>(), c.log_n, l, c.nQ, alpha, beta, c.nQ + c.nP);
     PtrStore cs{cx, tps, c.log_n};
     ntt_inv(c, 2 * qlp, QlpMap{qlp, 0, l, c.nQ}, PtrLoad{cx, tps, c.log_n}, cs,
             BfvCxStore{cx, tps, c.log_n, l, c.p_hat_inv.as<uint64_t>(), c.d_mods.as<Mod>()}, s);
     const long long lps = (long long)l << c.log_n;
     count_launch();
-    bfv_moddown_combine<<<grid_for_bfv((size_t)2 * lps, 256), 256, 0, s>>>(
-            out, lps, base, lps, cx, tps, c.p_mat.as<uint64_t>(), c.p_inv.as<uint64_t>(), c.d_mods.as<Mod>(), l,
-            c.nP, c.log_n);
+    launch_pdl(c.pdl, bfv_moddown_combine, dim3(grid_for_bfv((size_t)2 * lps, 256)), dim3(256), 0, s, out, lps, base, lps, cx, tps, c.p_mat.as<uint64_t>(), c.p_inv.as<uint64_t>(), c.d_mods.as<Mod>(), l, c.nP, c.log_n);
 }
 
 void bfv_keyswitch(const Context &c, const Workspace &w, uint64_t *ct, const uint64_t *c2, int l,
@@ -279,7 +279,7 @@ static void hps_tc_launch(const Context &c, const HpsTcArgs &a, cudaStream_t s) 
     const int per_sm = smem <= 100 * 1024 ? 2 : 1;  // 2 x 256 tensor-memory columns at most
     const int units = a.polys << (a.log_n - 7);
     count_launch();
-    hps_tc_kernel<MODE><<<std::min(units, per_sm * c.num_sms), 256, smem, s>>>(a);
+    launch_pdl(c.pdl, hps_tc_kernel<MODE>, dim3(std::min(units, per_sm * c.num_sms)), dim3(256), smem, s, a);
 }
 
 // Q -> R (or R -> Q) HPS conversion of `polys` polynomials on the tensor cores.
@@ -326,9 +326,7 @@ void bfv_mul_relin_hps(const Context &c, const Workspace &w, uint64_t *ct1, cons
         hps_conv_tc(c, true, ea + qps, qrps, ct1, qps, 2, s);
     } else {
         count_launch();
-        hps_bconv<<<g, 256, sm_q, s>>>(ea + qps, qrps, ct1, qps, mods, 0, nQ, rbase, nR,
-                                       c.hps_q_hat_inv.as<uint64_t>(), c.hps_q_inv.as<double>(),
-                                       c.hps_q2r_mat.as<uint64_t>(), c.hps_q2r_alpha.as<uint64_t>(), c.log_n);
+        launch_pdl(c.pdl, hps_bconv, dim3(g), dim3(256), sm_q, s, ea + qps, qrps, ct1, qps, mods, 0, nQ, rbase, nR, c.hps_q_hat_inv.as<uint64_t>(), c.hps_q_inv.as<double>(), c.hps_q2r_mat.as<uint64_t>(), c.hps_q2r_alpha.as<uint64_t>(), c.log_n);
     }
     const uint64_t *ebp = ea;
     if (!square) {
@@ -337,9 +335,7 @@ void bfv_mul_relin_hps(const Context &c, const Workspace &w, uint64_t *ct1, cons
             hps_conv_tc(c, true, eb + qps, qrps, ct2, qps, 2, s);
         } else {
             count_launch();
-            hps_bconv<<<g, 256, sm_q, s>>>(eb + qps, qrps, ct2, qps, mods, 0, nQ, rbase, nR,
-                                           c.hps_q_hat_inv.as<uint64_t>(), c.hps_q_inv.as<double>(),
-                                           c.hps_q2r_mat.as<uint64_t>(), c.hps_q2r_alpha.as<uint64_t>(), c.log_n);
+            launch_pdl(c.pdl, hps_bconv, dim3(g), dim3(256), sm_q, s, eb + qps, qrps, ct2, qps, mods, 0, nQ, rbase, nR, c.hps_q_hat_inv.as<uint64_t>(), c.hps_q_inv.as<double>(), c.hps_q2r_mat.as<uint64_t>(), c.hps_q2r_alpha.as<uint64_t>(), c.log_n);
         }
         ebp = eb;
     }
@@ -376,10 +372,7 @@ void bfv_mul_relin_hps(const Context &c, const Workspace &w, uint64_t *ct1, cons
     } else {
         dim3 g3((unsigned)(n / kHpsTile), 3);
         count_launch();
-        hps_scale_round_to_q<<<g3, 256, sm_r, s>>>(o3, qps, t3, qrps, mods, nQ, rbase, nR, c.hps_frac.as<double>(),
-                                                    c.hps_modr.as<uint64_t>(), c.hps_r_hat_inv.as<uint64_t>(),
-                                                    c.hps_r_inv.as<double>(), c.hps_r2q_mat.as<uint64_t>(),
-                                                    c.hps_r2q_alpha.as<uint64_t>(), c.log_n);
+        launch_pdl(c.pdl, hps_scale_round_to_q, dim3(g3), dim3(256), sm_r, s, o3, qps, t3, qrps, mods, nQ, rbase, nR, c.hps_frac.as<double>(), c.hps_modr.as<uint64_t>(), c.hps_r_hat_inv.as<uint64_t>(), c.hps_r_inv.as<double>(), c.hps_r2q_mat.as<uint64_t>(), c.hps_r2q_alpha.as<uint64_t>(), c.log_n);
     }
     // 4. relinearise c2 into (c0, c1), written to ct1
     bfv_keyswitch_to(c, ks, ct1, o3, o3 + 2 * qps, nQ, rlk, s);
@@ -387,6 +380,8 @@ void bfv_mul_relin_hps(const Context &c, const Workspace &w, uint64_t *ct1, cons
 
 __global__ void divide_round_q_last(uint64_t *out, const uint64_t *in, const uint64_t *iq, const Mod *mods, int l,
                                     int log_n, size_t total) {
+    pdl_wait();
+    pdl_release();
     const uint32_t nmask = (1u << log_n) - 1;
     const size_t lo = (size_t)(l - 1) << log_n;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
@@ -403,8 +398,7 @@ __global__ void divide_round_q_last(uint64_t *out, const uint64_t *in, const uin
 void bfv_divide_round_q_last(const Context &c, const uint64_t *in, uint64_t *out, int size, int l, cudaStream_t s) {
     const size_t total = (size_t)size * ((size_t)(l - 1) << c.log_n);
     count_launch();
-    divide_round_q_last<<<grid_for_bfv(total, 256), 256, 0, s>>>(out, in, c.levels[l]->inv_qlast.as<uint64_t>(),
-                                                                  c.d_mods.as<Mod>(), l, c.log_n, total);
+    launch_pdl(c.pdl, divide_round_q_last, dim3(grid_for_bfv(total, 256)), dim3(256), 0, s, out, in, c.levels[l]->inv_qlast.as<uint64_t>(), c.d_mods.as<Mod>(), l, c.log_n, total);
 }
 
 }  // namespace pfg

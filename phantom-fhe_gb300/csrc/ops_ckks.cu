@@ -183,8 +183,7 @@ static void modup_ckks(const Context &c, const KsBuffers &b, C2Load c2ld, int l,
         dim3 g(bconv_blocks(c), beta);
         with_digit_bound(alpha, [&]<int A>() {
             count_launch();
-            modup_bconv<A, false><<<g, 256, 0, s>>>(b.tm, b.y, nullptr, lt.modup_mat.as<uint64_t>(),
-                                                     c.d_mods.as<Mod>(), c.log_n, l, c.nQ, alpha);
+            launch_pdl(c.pdl, modup_bconv<A, false>, dim3(g), dim3(256), 0, s, b.tm, b.y, nullptr, lt.modup_mat.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, l, c.nQ, alpha);
         });
     }
     PtrStore ts{b.tm, tps, c.log_n};
@@ -253,8 +252,7 @@ static void moddown_ntt(const Context &c, const KsBuffers &b, uint64_t *mid, int
     } else {
         with_digit_bound(c.nP, [&]<int A>() {
             count_launch();
-            moddown_bconv<A><<<dim3(bconv_blocks(c), 2), 256, 0, s>>>(mid, mps, b.cx, cps, c.p_mat.as<uint64_t>(),
-                                                                       c.d_mods.as<Mod>(), c.log_n, l, c.nP);
+            launch_pdl(c.pdl, moddown_bconv<A>, dim3(dim3(bconv_blocks(c), 2)), dim3(256), 0, s, mid, mps, b.cx, cps, c.p_mat.as<uint64_t>(), c.d_mods.as<Mod>(), c.log_n, l, c.nP);
         });
     }
     PtrStore ms{mid, mps, c.log_n};
@@ -449,10 +447,7 @@ void ckks_mul_relin_rescale(const Context &c, const Workspace &w, const uint64_t
     } else {
         with_digit_bound(alpha, [&]<int A>() {
             count_launch();
-            rescale_fused_bconv<A><<<dim3(bconv_blocks(c), 2), 256, 0, s>>>(b.tm, ops, b.cx, cps, zc, zd,
-                                                                             c.p_mat.as<uint64_t>(),
-                                                                             c.p_inv.as<uint64_t>(), mods, c.log_n,
-                                                                             l, c.nP);
+            launch_pdl(c.pdl, rescale_fused_bconv<A>, dim3(dim3(bconv_blocks(c), 2)), dim3(256), 0, s, b.tm, ops, b.cx, cps, zc, zd, c.p_mat.as<uint64_t>(), c.p_inv.as<uint64_t>(), mods, c.log_n, l, c.nP);
         });
     }
     PtrStore ms{b.tm, ops, c.log_n};
@@ -470,6 +465,8 @@ void ckks_tensor(const Context &c, uint64_t *ct1, const uint64_t *ct2, int l, cu
 
 // g[p][k][i] = src[p][k][perm[i]] for 2 polynomials of l limbs
 __global__ void galois_permute(uint64_t *dst, const uint64_t *src, const uint32_t *perm, int log_n, size_t total) {
+    pdl_wait();
+    pdl_release();
     const uint32_t nmask = (1u << log_n) - 1;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const uint32_t idx = (uint32_t)e & nmask;
@@ -483,7 +480,7 @@ void ckks_apply_galois(const Context &c, const Workspace &w, uint64_t *ct, int l
     const long long lps = (long long)l << c.log_n;
     const size_t total = 2 * (size_t)lps;
     count_launch();
-    galois_permute<<<grid_for(total, 256), 256, 0, s>>>(b.g, ct, perm, c.log_n, total);
+    launch_pdl(c.pdl, galois_permute, dim3(grid_for(total, 256)), dim3(256), 0, s, b.g, ct, perm, c.log_n, total);
     const uint64_t *g1 = b.g + lps;
     modup_ckks(c, b, PtrLoad{g1, lps, c.log_n}, l, s);
     inner_product(c, b, PlainOwn{g1, c.log_n}, l, gk, s);
@@ -505,6 +502,8 @@ __global__ void __launch_bounds__(256) ks_inner_product_hoisted(uint64_t *cx, co
                                                                 const uint64_t *c1, HoistSteps steps,
                                                                 const Mod *mods, int log_n, int l, int nQ,
                                                                 int alpha, int beta, int qp, bool accumulate) {
+    pdl_wait();
+    pdl_release();
     const int qlp = l + alpha;
     const size_t total = (size_t)qlp << log_n;
     const uint32_t nmask = (1u << log_n) - 1;
@@ -543,6 +542,8 @@ __global__ void __launch_bounds__(256) ks_inner_product_hoisted(uint64_t *cx, co
 // acc0[i] = sum_s c0[perm_s[i]]
 __global__ void galois_sum(uint64_t *dst, const uint64_t *src, HoistSteps steps, const Mod *mods, int log_n,
                            size_t total, bool accumulate) {
+    pdl_wait();
+    pdl_release();
     const uint32_t nmask = (1u << log_n) - 1;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const uint32_t idx = (uint32_t)e & nmask;
@@ -571,11 +572,9 @@ void ckks_hoisting(const Context &c, const Workspace &w, uint64_t *ct, int l, co
         }
         const bool acc = s0 > 0;
         count_launch();
-        galois_sum<<<grid_for((size_t)lps, 256), 256, 0, s>>>(acc0, ct, hs, c.d_mods.as<Mod>(), c.log_n,
-                                                              (size_t)lps, acc);
+        launch_pdl(c.pdl, galois_sum, dim3(grid_for((size_t)lps, 256)), dim3(256), 0, s, acc0, ct, hs, c.d_mods.as<Mod>(), c.log_n, (size_t)lps, acc);
         count_launch();
-        ks_inner_product_hoisted<<<grid_for((size_t)qlp << c.log_n, 256), 256, 0, s>>>(
-                b.cx, b.tm, c1, hs, c.d_mods.as<Mod>(), c.log_n, l, c.nQ, c.nP, c.beta(l), c.nQ + c.nP, acc);
+        launch_pdl(c.pdl, ks_inner_product_hoisted, dim3(grid_for((size_t)qlp << c.log_n, 256)), dim3(256), 0, s, b.cx, b.tm, c1, hs, c.d_mods.as<Mod>(), c.log_n, l, c.nQ, c.nP, c.beta(l), c.nQ + c.nP, acc);
     }
     moddown_intt_p(c, b, l, s);
     moddown_ntt(c, b, b.tm, l, ct, ct + lps, FirstPolyBase{acc0, c.log_n}, s);
@@ -595,14 +594,13 @@ void ckks_rotations_hoisted(const Context &c, const Workspace &w, const uint64_t
     const int qlp = l + c.nP;
     for (size_t i = 0; i < steps.size(); i++) {
         count_launch();
-        galois_permute<<<grid_for((size_t)lps, 256), 256, 0, s>>>(b.g, ct, steps[i].perm, c.log_n, (size_t)lps);
+        launch_pdl(c.pdl, galois_permute, dim3(grid_for((size_t)lps, 256)), dim3(256), 0, s, b.g, ct, steps[i].perm, c.log_n, (size_t)lps);
         HoistSteps hs{};
         hs.count = 1;
         hs.perm[0] = steps[i].perm;
         hs.key[0] = steps[i].key;
         count_launch();
-        ks_inner_product_hoisted<<<grid_for((size_t)qlp << c.log_n, 256), 256, 0, s>>>(
-                b.cx, b.tm, c1, hs, c.d_mods.as<Mod>(), c.log_n, l, c.nQ, c.nP, c.beta(l), c.nQ + c.nP, false);
+        launch_pdl(c.pdl, ks_inner_product_hoisted, dim3(grid_for((size_t)qlp << c.log_n, 256)), dim3(256), 0, s, b.cx, b.tm, c1, hs, c.d_mods.as<Mod>(), c.log_n, l, c.nQ, c.nP, c.beta(l), c.nQ + c.nP, false);
         moddown_intt_p(c, b, l, s);
         // the mod-down's scratch must not be tm (it still holds the shared mod-up)
         moddown_ntt(c, b, b.h, l, outs[i], outs[i] + lps, FirstPolyBase{b.g, c.log_n}, s);
@@ -612,6 +610,8 @@ void ckks_rotations_hoisted(const Context &c, const Workspace &w, const uint64_t
 // ------------------------------------------------------------------ tensor (standalone)
 
 __global__ void tensor_2x2(uint64_t *ct1, const uint64_t *ct2, const Mod *mods, int log_n, size_t lps, bool square) {
+    pdl_wait();
+    pdl_release();
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < lps; e += (size_t)gridDim.x * blockDim.x) {
         const Mod m = mods[e >> log_n];
         const uint64_t a0 = ct1[e], a1 = ct1[lps + e];
@@ -627,7 +627,7 @@ __global__ void tensor_2x2(uint64_t *ct1, const uint64_t *ct2, const Mod *mods, 
 void ckks_tensor(const Context &c, uint64_t *ct1, const uint64_t *ct2, int l, cudaStream_t s) {
     const size_t lps = (size_t)l << c.log_n;
     count_launch();
-    tensor_2x2<<<grid_for(lps, 256), 256, 0, s>>>(ct1, ct2, c.d_mods.as<Mod>(), c.log_n, lps, ct1 == ct2);
+    launch_pdl(c.pdl, tensor_2x2, dim3(grid_for(lps, 256)), dim3(256), 0, s, ct1, ct2, c.d_mods.as<Mod>(), c.log_n, lps, ct1 == ct2);
 }
 
 }  // namespace pfg
