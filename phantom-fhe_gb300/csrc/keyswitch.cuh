@@ -59,10 +59,12 @@ __global__ void __launch_bounds__(256) ks_inner_product(uint64_t *cx, const uint
                 x0 = v.x;
                 x1 = v.y;
             }
+            // the key is read once per call: streaming loads (evict first) keep the mod-up output,
+            // written just before and read once here, in L2
             const uint64_t *key = evk[d];
-            const ulonglong2 k0 = __ldg(reinterpret_cast<const ulonglong2 *>(key + ((size_t)tbl << log_n) + idx));
+            const ulonglong2 k0 = __ldcs(reinterpret_cast<const ulonglong2 *>(key + ((size_t)tbl << log_n) + idx));
             const ulonglong2 k1 =
-                    __ldg(reinterpret_cast<const ulonglong2 *>(key + ((size_t)(qp + tbl) << log_n) + idx));
+                    __ldcs(reinterpret_cast<const ulonglong2 *>(key + ((size_t)(qp + tbl) << log_n) + idx));
             if (terms == 7) {  // keep the sum below q * 2^64 (reduce128's precondition)
                 a0 = u128{reduce128(a0, m), 0};
                 a1 = u128{reduce128(a1, m), 0};

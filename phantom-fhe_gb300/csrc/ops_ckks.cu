@@ -393,36 +393,36 @@ __global__ void __launch_bounds__(256) rescale_combine(uint64_t *out, const uint
                                                        const Mod *mods, int log_n, int lm1) {
     pdl_wait();
     pdl_release();
+    // one thread per coefficient pair of both output polynomials: every input word is read once
+    // (streaming loads: nothing here is read again by this call), the outputs stored streaming
     const size_t half = (size_t)1 << (log_n - 1), per_poly = (size_t)lm1 * half;
-    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * per_poly;
-         e += (size_t)gridDim.x * blockDim.x) {
-        const int t = e >= per_poly;
-        const size_t r = e - t * per_poly;
+    const size_t lm1n = (size_t)lm1 << log_n;
+    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < per_poly; r += (size_t)gridDim.x * blockDim.x) {
         const int j = (int)(r >> (log_n - 1));
         const size_t o = ((size_t)j << log_n) + 2 * (r & (half - 1));
         const Mod m = mods[j];
         const uint64_t pj = pinv[2 * j], pjs = pinv[2 * j + 1], qj = iq[2 * j], qjs = iq[2 * j + 1];
-        const ulonglong2 vv = *reinterpret_cast<const ulonglong2 *>(v + (size_t)t * (lm1 << log_n) + o);
-        const ulonglong2 cc = *reinterpret_cast<const ulonglong2 *>(cx + t * cps + o);
-        const ulonglong2 a0 = *reinterpret_cast<const ulonglong2 *>(a + o);
-        const ulonglong2 b0 = *reinterpret_cast<const ulonglong2 *>(b + o);
-        uint64_t d0, d1;
-        if (t == 0) {
-            d0 = mul_mod(a0.x, b0.x, m);
-            d1 = mul_mod(a0.y, b0.y, m);
-        } else {
-            const ulonglong2 a1 = *reinterpret_cast<const ulonglong2 *>(a + lps + o);
-            const ulonglong2 b1 = *reinterpret_cast<const ulonglong2 *>(b + lps + o);
-            u128 s0 = mul_wide(a0.x, b1.x), s1 = mul_wide(a0.y, b1.y);
-            mac(s0, a1.x, b0.x);
-            mac(s1, a1.y, b0.y);
-            d0 = reduce128(s0, m);
-            d1 = reduce128(s1, m);
+        const ulonglong2 a0 = __ldcs(reinterpret_cast<const ulonglong2 *>(a + o));
+        const ulonglong2 b0 = __ldcs(reinterpret_cast<const ulonglong2 *>(b + o));
+        const ulonglong2 a1 = __ldcs(reinterpret_cast<const ulonglong2 *>(a + lps + o));
+        const ulonglong2 b1 = __ldcs(reinterpret_cast<const ulonglong2 *>(b + lps + o));
+        uint64_t d[2][2];
+        d[0][0] = mul_mod(a0.x, b0.x, m);
+        d[0][1] = mul_mod(a0.y, b0.y, m);
+        u128 s0 = mul_wide(a0.x, b1.x), s1 = mul_wide(a0.y, b1.y);
+        mac(s0, a1.x, b0.x);
+        mac(s1, a1.y, b0.y);
+        d[1][0] = reduce128(s0, m);
+        d[1][1] = reduce128(s1, m);
+#pragma unroll
+        for (int t = 0; t < 2; t++) {
+            const ulonglong2 vv = __ldcs(reinterpret_cast<const ulonglong2 *>(v + (size_t)t * lm1n + o));
+            const ulonglong2 cc = __ldcs(reinterpret_cast<const ulonglong2 *>(cx + t * cps + o));
+            const uint64_t x0 = sub_mod(add_mod(d[t][0], mul_shoup(cc.x, pj, pjs, m.q), m.q), vv.x, m.q);
+            const uint64_t x1 = sub_mod(add_mod(d[t][1], mul_shoup(cc.y, pj, pjs, m.q), m.q), vv.y, m.q);
+            __stcs(reinterpret_cast<ulonglong2 *>(out + (size_t)t * lm1n + o),
+                   make_ulonglong2(mul_shoup(x0, qj, qjs, m.q), mul_shoup(x1, qj, qjs, m.q)));
         }
-        const uint64_t x0 = sub_mod(add_mod(d0, mul_shoup(cc.x, pj, pjs, m.q), m.q), vv.x, m.q);
-        const uint64_t x1 = sub_mod(add_mod(d1, mul_shoup(cc.y, pj, pjs, m.q), m.q), vv.y, m.q);
-        *reinterpret_cast<ulonglong2 *>(out + (size_t)t * (lm1 << log_n) + o) =
-                make_ulonglong2(mul_shoup(x0, qj, qjs, m.q), mul_shoup(x1, qj, qjs, m.q));
     }
 }
 
@@ -454,7 +454,7 @@ void ckks_mul_relin_rescale(const Context &c, const Workspace &w, const uint64_t
     PtrLoad ld{b.tm, ops, c.log_n};
     ntt_fwd(c, 2 * (l - 1), QlpMap{l - 1, 0, l, c.nQ}, ld, ms, ms, s);
     count_launch();
-    launch_pdl(c.pdl, rescale_combine, dim3(grid_for((size_t)(l - 1) << c.log_n, 256)), dim3(256), 0, s, out,
+    launch_pdl(c.pdl, rescale_combine, dim3(grid_for((size_t)(l - 1) << (c.log_n - 1), 256)), dim3(256), 0, s, out,
                (const uint64_t *)b.tm, (const uint64_t *)b.cx, cps, ct1, ct2, lps, c.p_inv.as<uint64_t>(),
                lt.inv_qlast.as<uint64_t>(), mods, c.log_n, l - 1);
 }
