@@ -54,8 +54,8 @@ __global__ void __launch_bounds__(256) ks_inner_product(uint64_t *cx, const uint
                 x0 = own(jj, m, idx);
                 x1 = own(jj, m, idx + 1);
             } else {
-                const ulonglong2 v =
-                        *reinterpret_cast<const ulonglong2 *>(tm + (((size_t)d * qlp + jj) << log_n) + idx);
+                const ulonglong2 v =  // the mod-up output is dead after this read
+                        __ldcs(reinterpret_cast<const ulonglong2 *>(tm + (((size_t)d * qlp + jj) << log_n) + idx));
                 x0 = v.x;
                 x1 = v.y;
             }

@@ -230,8 +230,8 @@ __global__ void __launch_bounds__(256) moddown_combine(uint64_t *out0, uint64_t 
         const size_t o = ((size_t)j << log_n) + idx;
         const Mod m = mods[j];
         const uint64_t pj = pinv[2 * j], pjs = pinv[2 * j + 1];
-        const ulonglong2 vv = *reinterpret_cast<const ulonglong2 *>(v + t * vps + o);
-        const ulonglong2 cc = *reinterpret_cast<const ulonglong2 *>(cx + t * cps + o);
+        const ulonglong2 vv = __ldcs(reinterpret_cast<const ulonglong2 *>(v + t * vps + o));  // read once
+        const ulonglong2 cc = __ldcs(reinterpret_cast<const ulonglong2 *>(cx + t * cps + o));
         const uint64_t y0 = add_mod(base(t, j, m, idx), mul_shoup(sub_mod(cc.x, vv.x, m.q), pj, pjs, m.q), m.q);
         const uint64_t y1 = add_mod(base(t, j, m, idx + 1), mul_shoup(sub_mod(cc.y, vv.y, m.q), pj, pjs, m.q), m.q);
         *reinterpret_cast<ulonglong2 *>((t == 0 ? out0 : out1) + o) = make_ulonglong2(y0, y1);
