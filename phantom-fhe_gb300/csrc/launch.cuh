@@ -51,12 +51,14 @@ struct ModupMap {
 
 // ---------------------------------------------------------------- generic functors
 
-struct PtrLoad {  // base[poly * ps + k * N + idx]
+// base[poly * ps + k * N + idx]; a streaming load: every NTT pass overwrites or abandons what it
+// reads, so the line need not stay in L2
+struct PtrLoad {
     const uint64_t *base;
     long long ps;
     int log_n;
     __device__ __forceinline__ uint64_t operator()(int poly, int k, int, uint32_t idx) const {
-        return base[poly * ps + ((long long)k << log_n) + idx];
+        return __ldcs(base + poly * ps + ((long long)k << log_n) + idx);
     }
 };
 
