@@ -833,6 +833,9 @@ def main(path):
         "ks_ckks_n16_a5_l7": case_keyswitch(K, 16, [60] + [40] * 9 + [60] * 5, 5, [7], 1602),
         "hmult_ckks_n12_a2": case_hmult(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, 1206),
         "hmult_ckks_n16_l30": case_hmult(K, 16, [60] + [40] * 29 + [60] * 5, 5, 30, 1606),
+        "hmult_ckks_n17_l8": case_hmult(K, 17, [60] + [50] * 7 + [60] * 4, 4, 8, 1701),
+        "ks_ckks_n17_a4": case_keyswitch(K, 17, [60] + [50] * 7 + [60] * 4, 4, [8, 3], 1702),
+        "ntt_n17_3": case_ntt(K, 17, [60, 50, 60], 1703),
         "rescale_n12": case_rescale(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, 1203),
         "tensor_galois_n12": case_tensor_galois(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, [1, -3, 7], 1204),
         "hps_n12": case_hps(K, 12, [50, 50, 50, 50, 60, 60], 2, 65537, 1205),
