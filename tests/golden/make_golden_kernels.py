@@ -328,6 +328,31 @@ def case_hmult(K, log_n, bits, special, l, seed):
             "multiply_and_relin": sha(relin), "rescaled": sha(R.host(out, 2 * (l - 1) * n))}
 
 
+def case_rotate(K, log_n, bits, special, l, step, seed):
+    """apply_galois_inplace for CKKS (src/evaluate.cu:1567-1630), as rotate_inplace calls it for a
+    step with a Galois key: permute c0 into temp and copy it back, permute c1 into temp, zero c1,
+    key-switch temp into (c0, c1).  The permutation table is this oracle's (the reference builds it
+    on the host, include/galois.cuh:98-113; it is fixed by the NTT order, which is pinned)."""
+    n = 1 << log_n
+    mods = O.create_coeff_modulus(n, bits)
+    nq = len(bits) - special
+    oc = O.Context(log_n, mods, nq, special)
+    T = Tables(log_n, mods)
+    rng = np.random.default_rng(seed)
+    evk_t, evk_ptrs = key_setup(rng, mods, n, nq, special)
+    ct = R.dev(O.random_residues(rng, mods[:l], n, 2), n)
+    elt = O.elt_from_step(step, n)
+    perm = torch.from_numpy(O.galois_perm(log_n, elt).view(np.int32).copy()).cuda()
+    temp = R.zeros(l * n + n)
+    K.galois(l * n // BLOCK_GLB, BLOCK_GLB, 0, temp, ct, perm, n, l)
+    ct[: l * n].copy_(temp[: l * n])
+    K.galois(l * n // BLOCK_GLB, BLOCK_GLB, 0, temp, R.Ptr(ct, l * n), perm, n, l)
+    ct[l * n: 2 * l * n].zero_()
+    ref_keyswitch(K, T, oc, KsLevel(oc, T, l), ct, temp, evk_ptrs)
+    return {"log_n": log_n, "bits": bits, "special": special, "l": l, "step": step, "elt": elt, "seed": seed,
+            "rotate": sha(R.host(ct, 2 * l * n))}
+
+
 def case_rescale(K, log_n, bits, special, l, seed):
     """DRNSTool::divide_and_round_q_last_ntt, src/rns.cu:1160-1184, on a size-2 ciphertext."""
     n = 1 << log_n
@@ -836,6 +861,8 @@ def main(path):
         "hmult_ckks_n17_l8": case_hmult(K, 17, [60] + [50] * 7 + [60] * 4, 4, 8, 1701),
         "ks_ckks_n17_a4": case_keyswitch(K, 17, [60] + [50] * 7 + [60] * 4, 4, [8, 3], 1702),
         "ntt_n17_3": case_ntt(K, 17, [60, 50, 60], 1703),
+        "rotate_ckks_n16_l30": case_rotate(K, 16, [60] + [40] * 29 + [60] * 5, 5, 30, 1, 1607),
+        "rotate_ckks_n12_a2": case_rotate(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, -3, 1212),
         "rescale_n12": case_rescale(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, 1203),
         "tensor_galois_n12": case_tensor_galois(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, [1, -3, 7], 1204),
         "hps_n12": case_hps(K, 12, [50, 50, 50, 50, 60, 60], 2, 65537, 1205),

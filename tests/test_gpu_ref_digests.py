@@ -211,3 +211,24 @@ def test_bfv_encode_encrypt_decrypt_digests(pg, name):
     rnd = pg.to_device(O.random_residues(rng, mods[:nq], n, 2))
     ctx.bfv_decrypt(ws, rnd, 1, s, m)
     assert sha(m) == g["decrypt_random"], f"decryption of random words ({g['decrypt_variant']} variant)"
+
+
+@pytest.mark.parametrize("name", [k for k in G if k.startswith("rotate_")])
+def test_rotate_digests(pg, name):
+    """HRotate (apply_galois_inplace with the step's Galois key) gives the reference's words."""
+    g = G[name]
+    n, l = 1 << g["log_n"], g["l"]
+    mods = pg.create_coeff_modulus(n, g["bits"])
+    nq = len(g["bits"]) - g["special"]
+    ctx = pg.Context(n, mods, g["special"], galois_elts=[g["elt"]])
+    ws = ctx.workspace()
+    rng = np.random.default_rng(g["seed"])
+    gk = O.random_residues(rng, mods, n, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), n)
+    key = pg.KeySwitchKey(pg.to_device(gk))
+    ct = O.random_residues(rng, mods[:l], n, 2)
+    for tc in (True, False):
+        ctx.tensor_cores = tc
+        t = pg.to_device(ct)
+        ctx.apply_galois(ws, t, nq - l + 1, g["elt"], key)
+        assert sha(t) == g["rotate"], f"tensor_cores={tc}"
+    assert ctx.device_status() == 0

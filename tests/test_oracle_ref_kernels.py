@@ -167,3 +167,18 @@ def test_samplers_and_seeded_keygen_match_reference_kernels(golden, name):
     a = np.stack([oc.sample_uniform(bytes.fromhex(h), qp) for h in g["seeds"]["a"]])
     e = np.stack([oc.ntt_fwd(_residues(oc.sample_small(bytes.fromhex(h), 1), mods, n)) for h in g["seeds"]["e"]])
     assert sha(oc.kswitch_key_combine(s, s2, a, e)) == g["relin_key"]
+
+
+@pytest.mark.parametrize("name", _cases("rotate_"))
+def test_rotate_matches_reference_kernels(golden, name):
+    g = golden[name]
+    n, l = 1 << g["log_n"], g["l"]
+    mods = O.create_coeff_modulus(n, g["bits"])
+    nq = len(g["bits"]) - g["special"]
+    oc = O.Context(g["log_n"], mods, nq, g["special"])
+    rng = np.random.default_rng(g["seed"])
+    dnum = -(-nq // g["special"])
+    gk = O.random_residues(rng, mods, n, 2 * dnum).reshape(dnum, 2, len(mods), n)
+    ct = O.random_residues(rng, mods[:l], n, 2)
+    assert O.elt_from_step(g["step"], n) == g["elt"]
+    assert sha(oc.ckks_apply_galois(l, ct, g["elt"], gk)) == g["rotate"]
