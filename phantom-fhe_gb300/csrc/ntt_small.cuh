@@ -49,11 +49,15 @@ __global__ void __cluster_dims__(kSmallCluster, 1, 1) __launch_bounds__(kSmallTh
     uint64_t *x = data + poly * ps + ((size_t)k << kSmallLogN) + (size_t)c * kSmallChunk;
     const uint64_t q = T.mods[tbl].q;
     const TwPair *gtw = (FWD ? T.tw : T.itw) + ((size_t)tbl << kSmallLogN);
-    for (int i = tid; i < kSmallChunk; i += kSmallThreads) sm[pad_idx(i)] = x[i];
+    // the twiddles come from the context's read-only tables: staged before waiting for the
+    // previous kernel (launch overlap), the data only after
     for (int i = tid; i < kSmallChunk - 1; i += kSmallThreads) {  // i = 2^(s-3) - 1 + g, s = 3..11
         const int s = 3 + (31 - __clz(i + 1)), g = i + 1 - (1 << (s - 3));
         ltw[i] = ld_tw(gtw, (1u << s) + (uint32_t)(c << (s - 3)) + g);
     }
+    pdl_wait();
+    pdl_release();
+    for (int i = tid; i < kSmallChunk; i += kSmallThreads) sm[pad_idx(i)] = x[i];
     const TwPair t0 = ld_tw(gtw, 1);
     auto local_tw = [&](int s, int e) { return ltw[(1 << (s - 3)) - 1 + (e >> (12 - s))]; };
     // cross-CTA radix-8 over stages 0..2 (CT forward order or GS inverse order)

@@ -57,8 +57,8 @@ size_t workspace_words(const Context &c) {
 template <bool FWD>
 static void ntt_n12_launch(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s) {
     count_launch();
-    ntt_n12<FWD><<<(unsigned)(polys * limbs * kSmallCluster), kSmallThreads, 0, s>>>(
-            data, (long long)limbs << c.log_n, limbs, start, c.ntt());
+    launch_pdl(c.pdl, ntt_n12<FWD>, dim3((unsigned)(polys * limbs * kSmallCluster)), dim3(kSmallThreads), 0, s, data,
+               (long long)limbs << c.log_n, limbs, start, c.ntt());
 }
 
 void ntt_forward(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s) {
