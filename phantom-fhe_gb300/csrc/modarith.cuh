@@ -32,6 +32,22 @@ __device__ __forceinline__ uint64_t mul_shoup_lazy(uint64_t x, uint64_t w, uint6
     return x * w - mulhi(x, ws) * q;
 }
 
+// floor(x * y / 2^64) - e with e in {0, 1, 2}: of the four 32 x 32-bit partial products the
+// low one is dropped and the middle ones contribute their high words only.  The dropped terms
+// are 2^32 (lo(xh yl) + lo(xl yh)) + xl yl < 3 * 2^64, so they carry at most 2 into the result.
+__device__ __forceinline__ uint64_t mulhi_trunc(uint64_t x, uint64_t y) {
+    const uint32_t xl = (uint32_t)x, xh = (uint32_t)(x >> 32), yl = (uint32_t)y, yh = (uint32_t)(y >> 32);
+    return (uint64_t)xh * yh + __umulhi(xh, yl) + __umulhi(xl, yh);
+}
+
+// x * w mod q in [0, 4q), any x < 2^64, w < q < 2^62, ws = floor(w * 2^64 / q): Shoup's product
+// with the truncated quotient (short by at most 2, so at most 2q above Shoup's [0, 2q)).  Two
+// 32-bit multiplies cheaper than mul_shoup_lazy; the NTT butterflies use it with lazy ranges
+// widened to match.
+__device__ __forceinline__ uint64_t mul_shoup_lazy4(uint64_t x, uint64_t w, uint64_t ws, uint64_t q) {
+    return x * w - mulhi_trunc(x, ws) * q;
+}
+
 __device__ __forceinline__ uint64_t mul_shoup(uint64_t x, uint64_t w, uint64_t ws, uint64_t q) {
     return csub(mul_shoup_lazy(x, w, ws, q), q);
 }

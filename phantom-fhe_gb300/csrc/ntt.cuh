@@ -65,15 +65,17 @@ __device__ __forceinline__ int grp_elem(int u, int gg, int j) {
     return ((g / TMIN) * (1 << K) + j) * TMIN + (g % TMIN);
 }
 
-// Forward (Cooley-Tukey, Harvey lazy: inputs < 4q, outputs < 4q) stages [SA, SA+K) on the
-// E registers of thread u.  Twiddle for local stage s of vector `row`:
+// Forward (Cooley-Tukey) stages [SA, SA+K) on the E registers of thread u, Harvey-style lazy
+// with the truncated-quotient product: inputs and outputs in [0, 8q) (8q < 2^64: every prime is
+// below 2^61).  Butterfly: a = csub(x, 4q) < 4q, b = y * w in [0, 4q) (mul_shoup_lazy4), outputs
+// a + b and a - b + 4q.  Twiddle for local stage s of vector `row`:
 // tw[(1 << (loff + s)) + (row << s) + (element >> (LM - s))].  All of a group's twiddle pairs
 // are fetched before its butterflies so their latency overlaps.
 template <int LM, int K, int SA, int E>
 __device__ __forceinline__ void fwd_regs(uint64_t (&x)[E], int u, const TwPair *tw, int loff, uint32_t row,
                                          uint64_t q) {
     constexpr int M = 1 << LM, TPV = M / E, G = E >> K, GS = 1 << K, TMIN = M >> (SA + K);
-    const uint64_t q2 = 2 * q;
+    const uint64_t q4 = 4 * q;
 #pragma unroll
     for (int gg = 0; gg < G; gg++) {
         const uint32_t hi = (uint32_t)((u + gg * TPV) / TMIN);
@@ -91,23 +93,24 @@ __device__ __forceinline__ void fwd_regs(uint64_t (&x)[E], int u, const TwPair *
             for (int j = 0; j < GS; j++) {
                 if (j & h) continue;
                 const TwPair t = w[(1 << k) - 1 + (j >> (K - k))];
-                const uint64_t a = csub(y[j], q2);
-                const uint64_t b = mul_shoup_lazy(y[j + h], t.w, t.ws, q);
+                const uint64_t a = csub(y[j], q4);
+                const uint64_t b = mul_shoup_lazy4(y[j + h], t.w, t.ws, q);
                 y[j] = a + b;
-                y[j + h] = a - b + q2;
+                y[j + h] = a - b + q4;
             }
         }
     }
 }
 
-// Inverse (Gentleman-Sande, inputs < 2q, outputs < 2q) stages SA+K-1 .. SA.  The global
-// stage-0 butterfly (loff == 0, local stage 0) scales its sum by n^-1; its difference twiddle
-// already carries n^-1 (src/host/ntt.cu:53-55).
+// Inverse (Gentleman-Sande) stages SA+K-1 .. SA, inputs and outputs in [0, 4q): sum a + b < 8q
+// reduced by csub(., 4q), difference (a - b + 4q) * w in [0, 4q) (mul_shoup_lazy4).  The global
+// stage-0 butterfly (loff == 0, local stage 0) scales its sum by n^-1 instead; its difference
+// twiddle already carries n^-1 (src/host/ntt.cu:53-55).
 template <int LM, int K, int SA, int E>
 __device__ __forceinline__ void inv_regs(uint64_t (&x)[E], int u, const TwPair *itw, int loff, uint32_t row,
                                          uint64_t q, uint64_t ninv, uint64_t ninv_s) {
     constexpr int M = 1 << LM, TPV = M / E, G = E >> K, GS = 1 << K, TMIN = M >> (SA + K);
-    const uint64_t q2 = 2 * q;
+    const uint64_t q4 = 4 * q;
 #pragma unroll
     for (int gg = 0; gg < G; gg++) {
         const uint32_t hi = (uint32_t)((u + gg * TPV) / TMIN);
@@ -128,8 +131,8 @@ __device__ __forceinline__ void inv_regs(uint64_t (&x)[E], int u, const TwPair *
                 const TwPair t = w[(1 << k) - 1 + (j >> (K - k))];
                 const uint64_t a = y[j], b = y[j + h];
                 const uint64_t s = a + b;
-                y[j] = first_stage ? mul_shoup_lazy(s, ninv, ninv_s, q) : csub(s, q2);
-                y[j + h] = mul_shoup_lazy(a - b + q2, t.w, t.ws, q);
+                y[j] = first_stage ? mul_shoup_lazy4(s, ninv, ninv_s, q) : csub(s, q4);
+                y[j + h] = mul_shoup_lazy4(a - b + q4, t.w, t.ws, q);
             }
         }
     }
@@ -196,7 +199,7 @@ struct NttTables {
 //   Load:  uint64_t operator()(int poly, int limb, int tbl, uint32_t idx) const
 //   Store: void operator()(int poly, int limb, int tbl, uint32_t idx, uint64_t v) const
 // `idx` is the coefficient index within the limb (row * N2 + column).  A pass that is not
-// the last of its transform stores lazy values ([0, 4q) forward, [0, 2q) inverse); the last
+// the last of its transform stores lazy values ([0, 8q) forward, [0, 4q) inverse); the last
 // pass hands canonical values to its Store functor.
 
 // Column pass: vectors are V consecutive columns, each of M = N1 elements (stride N2).  Thread
@@ -238,8 +241,8 @@ __global__ void __launch_bounds__(NttShape<E>::kThreads, NttShape<E>::kMinBlocks
         for (int j = 0; j < (1 << L::K); j++) {
             uint64_t y = x[gg * (1 << L::K) + j];
             if (LAST) {
-                if (FWD) y = csub(y, 2 * q);
-                y = csub(y, q);
+                if (FWD) y = csub(y, 4 * q);
+                y = csub(csub(y, 2 * q), q);
             }
             st(poly, k, tbl, (uint32_t)grp_elem<LM, L::K, L::SA, E>(u, gg, j) * n2 + col, y);
         }
@@ -293,7 +296,7 @@ __global__ void __launch_bounds__(NttShape<E>::kThreads, NttShape<E>::kMinBlocks
 #pragma unroll 4
         for (int i = threadIdx.x; i < V * M; i += NT) {
             uint64_t y = sm[(i / M) * VP + pad_idx(i % M)];
-            if (LAST) y = csub(csub(y, 2 * q), q);
+            if (LAST) y = csub(csub(csub(y, 4 * q), 2 * q), q);
             st(poly, k, tbl, base + i, y);
         }
     } else {
@@ -302,7 +305,7 @@ __global__ void __launch_bounds__(NttShape<E>::kThreads, NttShape<E>::kMinBlocks
 #pragma unroll
             for (int j = 0; j < (1 << L::K); j++) {
                 uint64_t y = x[gg * (1 << L::K) + j];
-                if (LAST) y = csub(y, q);
+                if (LAST) y = csub(csub(y, 2 * q), q);
                 st(poly, k, tbl, base + vv * M + grp_elem<LM, L::K, L::SA, E>(u, gg, j), y);
             }
     }
