@@ -75,6 +75,60 @@ def test_ntt_start_index_and_constant_inputs(small, pg):
         _eq(t, a, "round trip")
 
 
+def _primes_below_2_61(n, count):
+    """The largest primes q = 1 mod 2n below 2^61 (deterministic Miller-Rabin for 64 bits)."""
+    def is_prime(q):
+        d, s = q - 1, 0
+        while d % 2 == 0:
+            d, s = d // 2, s + 1
+        for a in (2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37):
+            x = pow(a, d, q)
+            if x in (1, q - 1):
+                continue
+            for _ in range(s - 1):
+                x = x * x % q
+                if x == q - 1:
+                    break
+            else:
+                return False
+        return True
+    out, q = [], ((1 << 61) - 1) // (2 * n) * (2 * n) + 1
+    while len(out) < count:
+        if q < (1 << 61) and is_prime(q):
+            out.append(q)
+        q -= 2 * n
+    return out
+
+
+@pytest.mark.parametrize("small_launch", [-1, 0])
+def test_ntt_lazy_inputs_at_range_limits(pg, small_launch):
+    """Inside a transform the butterflies keep values in [0, 8q) (forward) and [0, 4q) (inverse)
+    with a truncated-quotient Shoup product; producers fused into the passes hand over values in
+    those ranges.  Primes just below 2^61 (the context's limit) and inputs up to 8q - 1 / 4q - 1
+    put every bound at its edge; the outputs must still be the canonical transform."""
+    n = 1 << 14
+    mods = _primes_below_2_61(n, 3)
+    ctx = pg.Context(n, mods, 1)
+    ctx.ntt_small_launch = small_launch  # both the 8- and the 16-coefficient-per-thread passes
+    oc = O.Context(14, mods, 2, 1)
+    rng = np.random.default_rng(61)
+    a = O.random_residues(rng, mods, n, 2)
+    q = np.array(mods, dtype=np.uint64).reshape(1, 3, 1)
+    k = rng.integers(0, 8, size=a.shape, dtype=np.uint64)
+    k[..., :64] = 7  # the top of the range
+    lazy = a + k * q
+    assert int(lazy.max()) < (1 << 64)
+    t = pg.to_device(lazy)
+    ctx.ntt_forward(t, 2, 3, 0)
+    want = np.stack([oc.ntt_fwd(a[p]) for p in range(2)])
+    _eq(t, want, "forward NTT of inputs in [0, 8q)")
+    k4 = rng.integers(0, 4, size=a.shape, dtype=np.uint64)
+    k4[..., :64] = 3
+    b = pg.to_device(want + k4 * q)
+    ctx.ntt_inverse(b, 2, 3, 0)
+    _eq(b, a, "inverse NTT of inputs in [0, 4q)")
+
+
 def test_tensor(small, pg):
     ctx, oc, mods, nq, ws = small
     rng = np.random.default_rng(1)
