@@ -48,6 +48,12 @@ __device__ __forceinline__ uint64_t mul_shoup_lazy4(uint64_t x, uint64_t w, uint
     return x * w - mulhi_trunc(x, ws) * q;
 }
 
+// The same with nq = 2^64 - q given: x w + Q nq = x w - Q q (mod 2^64), and as a sum of products
+// the final 64-bit addition folds into the multiply-add chain instead of taking two integer adds.
+__device__ __forceinline__ uint64_t mul_shoup_lazy4n(uint64_t x, uint64_t w, uint64_t ws, uint64_t nq) {
+    return x * w + mulhi_trunc(x, ws) * nq;
+}
+
 __device__ __forceinline__ uint64_t mul_shoup(uint64_t x, uint64_t w, uint64_t ws, uint64_t q) {
     return csub(mul_shoup_lazy(x, w, ws, q), q);
 }

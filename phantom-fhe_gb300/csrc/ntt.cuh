@@ -75,7 +75,7 @@ template <int LM, int K, int SA, int E>
 __device__ __forceinline__ void fwd_regs(uint64_t (&x)[E], int u, const TwPair *tw, int loff, uint32_t row,
                                          uint64_t q) {
     constexpr int M = 1 << LM, TPV = M / E, G = E >> K, GS = 1 << K, TMIN = M >> (SA + K);
-    const uint64_t q4 = 4 * q;
+    const uint64_t q4 = 4 * q, nq = 0 - q;
 #pragma unroll
     for (int gg = 0; gg < G; gg++) {
         const uint32_t hi = (uint32_t)((u + gg * TPV) / TMIN);
@@ -94,7 +94,7 @@ __device__ __forceinline__ void fwd_regs(uint64_t (&x)[E], int u, const TwPair *
                 if (j & h) continue;
                 const TwPair t = w[(1 << k) - 1 + (j >> (K - k))];
                 const uint64_t a = csub(y[j], q4);
-                const uint64_t b = mul_shoup_lazy4(y[j + h], t.w, t.ws, q);
+                const uint64_t b = mul_shoup_lazy4n(y[j + h], t.w, t.ws, nq);
                 y[j] = a + b;
                 y[j + h] = a - b + q4;
             }
@@ -110,7 +110,7 @@ template <int LM, int K, int SA, int E>
 __device__ __forceinline__ void inv_regs(uint64_t (&x)[E], int u, const TwPair *itw, int loff, uint32_t row,
                                          uint64_t q, uint64_t ninv, uint64_t ninv_s) {
     constexpr int M = 1 << LM, TPV = M / E, G = E >> K, GS = 1 << K, TMIN = M >> (SA + K);
-    const uint64_t q4 = 4 * q;
+    const uint64_t q4 = 4 * q, nq = 0 - q;
 #pragma unroll
     for (int gg = 0; gg < G; gg++) {
         const uint32_t hi = (uint32_t)((u + gg * TPV) / TMIN);
@@ -131,8 +131,8 @@ __device__ __forceinline__ void inv_regs(uint64_t (&x)[E], int u, const TwPair *
                 const TwPair t = w[(1 << k) - 1 + (j >> (K - k))];
                 const uint64_t a = y[j], b = y[j + h];
                 const uint64_t s = a + b;
-                y[j] = first_stage ? mul_shoup_lazy4(s, ninv, ninv_s, q) : csub(s, q4);
-                y[j + h] = mul_shoup_lazy4(a - b + q4, t.w, t.ws, q);
+                y[j] = first_stage ? mul_shoup_lazy4n(s, ninv, ninv_s, nq) : csub(s, q4);
+                y[j + h] = mul_shoup_lazy4n(a - b + q4, t.w, t.ws, nq);
             }
         }
     }
