@@ -523,7 +523,9 @@ def run_ours(args):
         got = butterflies * wipb / t_ntt
         top = torch.cuda.get_device_properties(local).multi_processor_count * 4 * ck["sm_mhz"] * 1e6
         issue = {"warp_inst_per_butterfly": wipb, "achieved": got, "peak": top, "unit": "warp inst/s",
-                 "frac": got / top, "source": "ncu smsp__inst_executed.sum per butterfly; peak at the median SM clock"}
+                 "frac": got / top, "source": "ncu smsp__inst_executed.sum per butterfly; peak at the median SM clock",
+                 "busiest_pipe_ncu": {"pipe": "fmaheavy (IMAD)",
+                                      **prof.get("ntt_forward_fmaheavy_pipe_frac", {})}}
     line = {"metric": METRIC, "value": value, "unit": "ops/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": 1000 * t / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",

@@ -196,3 +196,46 @@ def test_small_launch_kernels_give_the_same_words(pg, log_n):
     assert ctx.ntt_small_launch == 512
     with pytest.raises(pg.InvalidArgument):
         ctx.ntt_small_launch = -2
+
+
+@pytest.mark.parametrize("log_n", [12, 14])
+def test_launch_overlap_off_gives_the_same_words(pg, log_n):
+    """Programmatic dependent launch changes only when a kernel may be scheduled: with it switched
+    off (plain stream order) the NTT (the cluster kernel at 2^12), a key switch, a rotation and
+    HMult + relin + rescale give the oracle's words, as they do with it on."""
+    n = 1 << log_n
+    bits = [60] + [40] * 5 + [60, 60]
+    mods = pg.create_coeff_modulus(n, bits)
+    elt = pg.elt_from_step(1, n)
+    ctx = pg.Context(n, mods, 2, galois_elts=[elt])
+    oc = O.Context(log_n, mods, 6, 2)
+    ws = ctx.workspace()
+    rng = np.random.default_rng(300 + log_n)
+    x = O.random_residues(rng, mods[:3], n, 1)
+    key = O.random_residues(rng, mods, n, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), n)
+    k = pg.KeySwitchKey(pg.to_device(key))
+    ct = O.random_residues(rng, mods[:6], n, 2)
+    c2 = O.random_residues(rng, mods[:6], n, 1)[0]
+    a = O.random_residues(rng, mods[:6], n, 2)
+    b = O.random_residues(rng, mods[:6], n, 2)
+    want_ntt = oc.ntt_fwd(x[0], [0, 1, 2])
+    want_ks = oc.keyswitch(6, ct, c2, key)
+    want_rot = oc.ckks_apply_galois(6, ct, elt, key)
+    want_hm = oc.rescale(6, oc.ckks_mul_relin(6, a, b, key))
+    for on in (False, True):
+        ctx.launch_overlap = on
+        assert ctx.launch_overlap == on
+        t = pg.to_device(x)
+        ctx.ntt_forward(t, 1, 3)
+        _eq(t, want_ntt, f"forward NTT, overlap {on}")
+        ctx.ntt_inverse(t, 1, 3)
+        _eq(t, x, f"round trip, overlap {on}")
+        tk = pg.to_device(ct)
+        ctx.keyswitch(ws, tk, pg.to_device(c2), 1, k)
+        _eq(tk, want_ks, f"keyswitch, overlap {on}")
+        tr = pg.to_device(ct)
+        ctx.rotate(ws, tr, 1, 1, [k])
+        _eq(tr, want_rot, f"rotate, overlap {on}")
+        out = torch.empty((2, 5, n), dtype=torch.int64, device="cuda")
+        ctx.multiply_relin_rescale(ws, pg.to_device(a), pg.to_device(b), out, 1, k)
+        _eq(out, want_hm, f"HMult, overlap {on}")
