@@ -26,7 +26,7 @@
 
 namespace pfg {
 
-static int grid_of(size_t work) { return (int)std::min<size_t>((work + 255) / 256, 152 * 16); }
+static int grid_of(size_t work) { return (int)std::min<size_t>((work + 255) / 256, kGridStrideBlocks); }
 
 __global__ void bfv_encode_scatter(uint64_t *out, const uint64_t *in, size_t count, const uint32_t *map, uint64_t t,
                                    size_t n) {

@@ -26,6 +26,10 @@ namespace pfg {
 // faster end to end with 8 per thread; passes of 528 tiles and more are faster with 16.
 constexpr int kNttSmallLaunchTiles = 512;
 
+// Block cap of the grid-stride element-wise kernels: 16 blocks of 256 threads per SM of GB300's
+// 152 SMs (8 resident per SM, two waves); a larger grid only adds block scheduling.
+constexpr int kGridStrideBlocks = 152 * 16;
+
 // values of phantom::scheme_type (include/host/encryptionparams.h)
 enum Scheme { kSchemeNone = 0, kSchemeBGV = 1, kSchemeBFV = 2, kSchemeCKKS = 3 };
 enum MulTech { kMulNone = 0, kMulBEHZ = 1, kMulHPS = 2, kMulHPSOverQ = 3, kMulHPSOverQLeveled = 4 };

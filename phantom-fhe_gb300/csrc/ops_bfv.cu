@@ -26,7 +26,7 @@ namespace pfg {
 
 static int grid_for_bfv(size_t work, int per_block) {
     size_t b = (work + per_block - 1) / per_block;
-    return (int)std::min<size_t>(b, 152 * 32);
+    return (int)std::min<size_t>(b, 2 * kGridStrideBlocks);
 }
 
 // ------------------------------------------------------------------ HPS base conversion

@@ -122,7 +122,7 @@ struct FirstPolyBase {  // t = 0: g0, t = 1: 0 (Galois: c1 is wiped before the k
 
 static int grid_for(size_t work, int per_block) {
     size_t b = (work + per_block - 1) / per_block;
-    return (int)std::min<size_t>(b, 152 * 16);
+    return (int)std::min<size_t>(b, kGridStrideBlocks);
 }
 
 // ------------------------------------------------------------------ pipeline pieces

@@ -17,7 +17,7 @@
 
 namespace pfg {
 
-static int grid_lin(size_t work) { return (int)std::min<size_t>((work + 255) / 256, 152 * 16); }
+static int grid_lin(size_t work) { return (int)std::min<size_t>((work + 255) / 256, kGridStrideBlocks); }
 
 // out[p][e] = ct[p][e] * pt[e]  (p = 0, 1; e over l limbs x N)
 __global__ void mul_plain_kernel(uint64_t *out, const uint64_t *ct, const uint64_t *pt, const Mod *mods, int log_n,

@@ -121,7 +121,7 @@ static PrngKey key_of(const uint8_t *seed) {
     return k;
 }
 
-static int grid_for(size_t work) { return (int)std::min<size_t>((work + 255) / 256, 152 * 16); }
+static int grid_for(size_t work) { return (int)std::min<size_t>((work + 255) / 256, kGridStrideBlocks); }
 
 void sample_uniform(const Context &c, const uint8_t *seed, int limbs, uint64_t *out, cudaStream_t s) {
     count_launch();
