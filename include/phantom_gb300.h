@@ -187,7 +187,8 @@ int fhe_bfv_mod_switch_to_next(const fhe_context *ctx, const uint64_t *in, uint6
 
 /* HMult + relinearise + rescale as one call (multiply_and_relin_inplace followed by
  * rescale_to_next_inplace, src/evaluate.cu:1061-1104 and 1545-1565): out (2 polys at
- * chain_index + 1) = Rescale(Relin(ct1 * ct2)).  Bit-identical to the two-call sequence. */
+ * chain_index + 1) = Rescale(Relin(ct1 * ct2)).  Bit-identical to the two-call sequence.
+ * ct1 and ct2 may be the same ciphertext (squaring); out must not overlap either input. */
 int fhe_ckks_multiply_relin_rescale(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *ct1,
                                     const uint64_t *ct2, uint64_t *out, size_t chain_index,
                                     const uint64_t *const *rlk, void *stream);

@@ -211,6 +211,23 @@ def test_multiply_relin_rescale_fused_equals_sequence(small, pg):
         assert torch.equal(out, out2)
 
 
+def test_multiply_relin_rescale_squaring(small, pg):
+    """ct1 and ct2 the same buffer (the reference's multiply_and_relin_inplace(ct, ct)), down to
+    the lowest level that can still rescale (l = 2 -> 1)."""
+    ctx, oc, mods, nq, ws = small
+    rng = np.random.default_rng(41)
+    key = _key(rng, mods, ctx.dnum, ctx.n)
+    k = pg.KeySwitchKey(pg.to_device(key))
+    for chain in (1, nq - 1):
+        l = ctx.level(chain)
+        a = O.random_residues(rng, mods[:l], ctx.n, 2)
+        ta = pg.to_device(a)
+        out = torch.empty((2, l - 1, ctx.n), dtype=torch.int64, device="cuda")
+        ctx.multiply_relin_rescale(ws, ta, ta, out, chain, k)
+        _eq(out, oc.rescale(l, oc.ckks_mul_relin(l, a, a, key)), f"fused square chain {chain}")
+        _eq(ta, a, "inputs untouched")
+
+
 def test_apply_galois_rotate_and_naf(small, pg):
     ctx, oc, mods, nq, ws = small
     rng = np.random.default_rng(50)
