@@ -111,6 +111,12 @@ int fhe_context_set_launch_overlap(fhe_context *ctx, int enable);
 int fhe_context_ntt_small_launch(const fhe_context *ctx);
 int fhe_context_set_ntt_small_launch(fhe_context *ctx, int tiles);
 
+/* Coefficients per CTA of those small-launch passes: 2048 (the default: twice the CTAs, so a
+ * launch of a few hundred tiles spreads evenly over the SMs) or 4096.  Every setting gives the
+ * same words.  No counterpart in the reference. */
+int fhe_context_ntt_small_tile(const fhe_context *ctx);
+int fhe_context_set_ntt_small_tile(fhe_context *ctx, int coefficients);
+
 /* Reads and clears the context's device status word (synchronises the device).  Non-zero
  * means a bounded wait inside a tensor-core kernel gave up and that call's output is invalid.
  * No counterpart in the reference. */

@@ -158,6 +158,20 @@ int fhe_context_set_ntt_small_launch(fhe_context *ctx, int tiles) {
     }, false);
 }
 
+int fhe_context_ntt_small_tile(const fhe_context *ctx) {
+    if (!ctx || !ctx->c) return 0;
+    return ctx->c->ntt_small_tile;
+}
+
+int fhe_context_set_ntt_small_tile(fhe_context *ctx, int coefficients) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        if (coefficients != pfg::kTileElems && coefficients != pfg::kTileElems / 2)
+            throw std::invalid_argument("small-launch tile must be 2048 or 4096 coefficients");
+        c.ntt_small_tile = coefficients;
+    }, false);
+}
+
 int fhe_context_launch_overlap(const fhe_context *ctx) {
     if (!ctx || !ctx->c) return 0;
     return ctx->c->pdl ? 1 : 0;

@@ -127,6 +127,9 @@ struct Context {
     // NTT passes over at most this many 4096-coefficient tiles run 8 coefficients per thread
     // (NttShape<8>); larger ones 16.  -1: the default, kNttSmallLaunchTiles.
     int ntt_small_tiles = -1;
+    // coefficients per CTA of those small passes: 2048 (twice the CTAs) or 4096; any setting
+    // gives the same words
+    int ntt_small_tile = kTileElems / 2;
     // kernel chains launched with programmatic dependent launch (pdl.cuh); any setting gives the
     // same words
     bool pdl = true;

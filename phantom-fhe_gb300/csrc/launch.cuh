@@ -86,51 +86,58 @@ struct ScaleStore {
 
 // ---------------------------------------------------------------- pass launchers
 
-template <bool FWD, bool LAST, int E, class Map, class Load, class Store>
+template <bool FWD, bool LAST, int E, int TILE, class Map, class Load, class Store>
 void col_pass_e(const Context &c, dim3 grid, Map m, Load ld, Store st, cudaStream_t s) {
-    constexpr int NT = NttShape<E>::kThreads;
+    constexpr int NT = NttShape<E, TILE>::kThreads;
     const NttTables T = c.ntt();
     switch (c.l1()) {
-        case 6: launch_pdl(c.pdl, ntt_col_pass<6, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
-        case 7: launch_pdl(c.pdl, ntt_col_pass<7, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
-        case 8: launch_pdl(c.pdl, ntt_col_pass<8, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
+        case 6: launch_pdl(c.pdl, ntt_col_pass<6, FWD, LAST, Map, Load, Store, E, TILE>, grid, dim3(NT), 0, s, T, m, ld, st); break;
+        case 7: launch_pdl(c.pdl, ntt_col_pass<7, FWD, LAST, Map, Load, Store, E, TILE>, grid, dim3(NT), 0, s, T, m, ld, st); break;
+        case 8: launch_pdl(c.pdl, ntt_col_pass<8, FWD, LAST, Map, Load, Store, E, TILE>, grid, dim3(NT), 0, s, T, m, ld, st); break;
         default: break;
     }
 }
 
-template <bool FWD, bool LAST, int E, class Map, class Load, class Store>
+template <bool FWD, bool LAST, int E, int TILE, class Map, class Load, class Store>
 void row_pass_e(const Context &c, dim3 grid, Map m, Load ld, Store st, cudaStream_t s) {
-    constexpr int NT = NttShape<E>::kThreads;
+    constexpr int NT = NttShape<E, TILE>::kThreads;
     const NttTables T = c.ntt();
     switch (c.l2()) {
-        case 6: launch_pdl(c.pdl, ntt_row_pass<6, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
-        case 7: launch_pdl(c.pdl, ntt_row_pass<7, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
-        case 8: launch_pdl(c.pdl, ntt_row_pass<8, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
-        case 9: launch_pdl(c.pdl, ntt_row_pass<9, FWD, LAST, Map, Load, Store, E>, grid, dim3(NT), 0, s, T, m, ld, st); break;
+        case 6: launch_pdl(c.pdl, ntt_row_pass<6, FWD, LAST, Map, Load, Store, E, TILE>, grid, dim3(NT), 0, s, T, m, ld, st); break;
+        case 7: launch_pdl(c.pdl, ntt_row_pass<7, FWD, LAST, Map, Load, Store, E, TILE>, grid, dim3(NT), 0, s, T, m, ld, st); break;
+        case 8: launch_pdl(c.pdl, ntt_row_pass<8, FWD, LAST, Map, Load, Store, E, TILE>, grid, dim3(NT), 0, s, T, m, ld, st); break;
+        case 9: launch_pdl(c.pdl, ntt_row_pass<9, FWD, LAST, Map, Load, Store, E, TILE>, grid, dim3(NT), 0, s, T, m, ld, st); break;
         default: break;
     }
 }
 
-// One pass over `blocks` limbs (blockIdx.y) of N / 4096 tiles each (blockIdx.x); launches of at
-// most c.ntt_small_limit() tiles take the 8-coefficients-per-thread kernels.
+// One pass over `blocks` limbs (blockIdx.y) of N / TILE tiles each (blockIdx.x).  Launches of
+// at most c.ntt_small_limit() 4096-coefficient tiles take the 8-coefficients-per-thread kernels,
+// on tiles of c.ntt_small_tile coefficients; larger ones 16 per thread on 4096.
 template <bool FWD, bool LAST, class Map, class Load, class Store>
 void col_pass(const Context &c, int blocks, Map m, Load ld, Store st, cudaStream_t s) {
-    const dim3 grid((unsigned)(c.n / kTileElems), (unsigned)blocks);
+    const long long tiles = (long long)(c.n / kTileElems) * blocks;
     count_launch();
-    if ((long long)grid.x * grid.y <= c.ntt_small_limit())
-        col_pass_e<FWD, LAST, 8>(c, grid, m, ld, st, s);
+    if (tiles > c.ntt_small_limit())
+        col_pass_e<FWD, LAST, 16, kTileElems>(c, dim3((unsigned)(c.n / kTileElems), (unsigned)blocks), m, ld, st, s);
+    else if (c.ntt_small_tile == kTileElems / 2)
+        col_pass_e<FWD, LAST, 8, kTileElems / 2>(c, dim3((unsigned)(c.n / (kTileElems / 2)), (unsigned)blocks), m, ld,
+                                                 st, s);
     else
-        col_pass_e<FWD, LAST, 16>(c, grid, m, ld, st, s);
+        col_pass_e<FWD, LAST, 8, kTileElems>(c, dim3((unsigned)(c.n / kTileElems), (unsigned)blocks), m, ld, st, s);
 }
 
 template <bool FWD, bool LAST, class Map, class Load, class Store>
 void row_pass(const Context &c, int blocks, Map m, Load ld, Store st, cudaStream_t s) {
-    const dim3 grid((unsigned)(c.n / kTileElems), (unsigned)blocks);
+    const long long tiles = (long long)(c.n / kTileElems) * blocks;
     count_launch();
-    if ((long long)grid.x * grid.y <= c.ntt_small_limit())
-        row_pass_e<FWD, LAST, 8>(c, grid, m, ld, st, s);
+    if (tiles > c.ntt_small_limit())
+        row_pass_e<FWD, LAST, 16, kTileElems>(c, dim3((unsigned)(c.n / kTileElems), (unsigned)blocks), m, ld, st, s);
+    else if (c.ntt_small_tile == kTileElems / 2)
+        row_pass_e<FWD, LAST, 8, kTileElems / 2>(c, dim3((unsigned)(c.n / (kTileElems / 2)), (unsigned)blocks), m, ld,
+                                                 st, s);
     else
-        row_pass_e<FWD, LAST, 16>(c, grid, m, ld, st, s);
+        row_pass_e<FWD, LAST, 8, kTileElems>(c, dim3((unsigned)(c.n / kTileElems), (unsigned)blocks), m, ld, st, s);
 }
 
 // Forward transform: column pass (load functor) -> row pass (store functor); the

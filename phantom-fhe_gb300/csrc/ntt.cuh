@@ -38,13 +38,16 @@ constexpr int kTileElems = 4096;  // V * M coefficients per CTA
 
 // E coefficients per thread: 16 (radix-16 register phases, 256 threads per tile) for large
 // launches, or 8 (radix-8 phases, 512 threads per tile: half the serial work per thread, so
-// about half the time per tile) for launches of a few waves, which are latency-bound.
-template <int E>
+// about half the time per tile) for launches of a few waves, which are latency-bound.  Small
+// launches may also use half-size tiles (TILE = 2048 coefficients, 256 threads at E = 8): twice
+// the CTAs, so a launch of a few hundred tiles spreads more evenly over the SMs.
+template <int E, int TILE = kTileElems>
 struct NttShape {
     static_assert(E == 8 || E == 16, "8 or 16 coefficients per thread");
+    static_assert(TILE == kTileElems || (TILE == kTileElems / 2 && E == 8), "4096, or 2048 at E = 8");
     static constexpr int LGE = E == 16 ? 4 : 3;
-    static constexpr int kThreads = kTileElems / E;
-    static constexpr int kMinBlocks = E == 16 ? 3 : 2;
+    static constexpr int kThreads = TILE / E;
+    static constexpr int kMinBlocks = E == 16 ? 3 : (TILE == kTileElems ? 2 : 4);
 };
 
 __host__ __device__ constexpr int ntt_num_phases(int lm, int lge) { return (lm + lge - 1) / lge; }
@@ -203,15 +206,16 @@ struct NttTables {
 // pass hands canonical values to its Store functor.
 
 // Column pass: vectors are V consecutive columns, each of M = N1 elements (stride N2).  Thread
-// t works on column t % V, so every global access of a warp covers whole 128-byte row
-// segments; the first and last register phases load and store global memory directly.
-template <int LM, bool FWD, bool LAST, class Map, class Load, class Store, int E = 16>
-__global__ void __launch_bounds__(NttShape<E>::kThreads, NttShape<E>::kMinBlocks)
+// t works on column t % V, so every global access of a warp covers whole row segments of V
+// words (128 bytes for 4096-coefficient tiles up to N1 = 256); the first and last register
+// phases load and store global memory directly.
+template <int LM, bool FWD, bool LAST, class Map, class Load, class Store, int E = 16, int TILE = kTileElems>
+__global__ void __launch_bounds__(NttShape<E, TILE>::kThreads, NttShape<E, TILE>::kMinBlocks)
         ntt_col_pass(NttTables T, Map map, Load ld, Store st) {
     pdl_wait();
     pdl_release();
     constexpr int M = 1 << LM;
-    constexpr int V = kTileElems / M;
+    constexpr int V = TILE / M;
     constexpr int VP = M + M / 16 + 1;  // padded vector length (odd: column sweeps hit distinct banks)
     using F = PhaseAt<LM, FWD, 0, E>;
     using L = PhaseAt<LM, FWD, F::NPH - 1, E>;
@@ -251,23 +255,23 @@ __global__ void __launch_bounds__(NttShape<E>::kThreads, NttShape<E>::kMinBlocks
 // Row pass: vectors are V consecutive rows of M = N2 contiguous elements.  The forward pass
 // loads its first phase directly (lane-contiguous) and stores through a coalesced sweep;
 // the inverse pass loads through the sweep and stores its last phase directly.
-template <int LM, bool FWD, bool LAST, class Map, class Load, class Store, int E = 16>
-__global__ void __launch_bounds__(NttShape<E>::kThreads, NttShape<E>::kMinBlocks)
+template <int LM, bool FWD, bool LAST, class Map, class Load, class Store, int E = 16, int TILE = kTileElems>
+__global__ void __launch_bounds__(NttShape<E, TILE>::kThreads, NttShape<E, TILE>::kMinBlocks)
         ntt_row_pass(NttTables T, Map map, Load ld, Store st) {
     pdl_wait();
     pdl_release();
     constexpr int M = 1 << LM;
     constexpr int TPV = M / E;
-    constexpr int V = kTileElems / M;
+    constexpr int V = TILE / M;
     constexpr int VP = M + M / 16 + 1;
-    constexpr int NT = NttShape<E>::kThreads;
+    constexpr int NT = NttShape<E, TILE>::kThreads;
     using F = PhaseAt<LM, FWD, 0, E>;
     using L = PhaseAt<LM, FWD, F::NPH - 1, E>;
     __shared__ uint64_t sm[V * VP];
     int poly, k, tbl;
     if (!map((int)blockIdx.y, poly, k, tbl)) return;  // uniform per block, before any barrier
     const uint64_t q = T.mods[tbl].q;
-    const uint32_t base = blockIdx.x * kTileElems;
+    const uint32_t base = blockIdx.x * TILE;
     const int vv = threadIdx.x / TPV, u = threadIdx.x % TPV;
     const uint32_t row = blockIdx.x * V + vv;
     uint64_t *vec = sm + vv * VP;
