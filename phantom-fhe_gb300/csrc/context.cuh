@@ -21,10 +21,12 @@
 namespace pfg {
 
 // Default small-launch bound for the 8-coefficients-per-thread NTT passes, in 4096-coefficient
-// tiles.  Measured on GB300 (N = 2^16, 30 + 5 primes; N = 2^15 BFV): passes of up to ~500 tiles
-// (the 30-limb inverse transform of a key switch, the 12-limb mod-down transform) are about 1 %
-// faster end to end with 8 per thread; passes of 528 tiles and more are faster with 16.
-constexpr int kNttSmallLaunchTiles = 512;
+// tiles.  Measured on GB300 with the half-size (2048-coefficient) tiles of those passes (N = 2^16,
+// 30 + 5 primes; N = 2^15 BFV): up to 1024 tiles (the 30-limb inverse transform, the 12-limb
+// mod-down transform, the 58-limb mod-down / rescale forward transform) is fastest end to end
+// (HMult 0.4134 -> 0.4112 ms against a bound of 512, BFV mult+relin 0.386 -> 0.378 ms); the
+// 180-limb mod-up transform (2880 tiles) stays faster at 16 per thread.
+constexpr int kNttSmallLaunchTiles = 1024;
 
 // Block cap of the grid-stride element-wise kernels: 16 blocks of 256 threads per SM of GB300's
 // 152 SMs (8 resident per SM, two waves); a larger grid only adds block scheduling.
