@@ -99,7 +99,7 @@ int fhe_context_autotune(fhe_context *ctx, int *chosen_l1, float *best_us);
 /* NTT passes over at most `tiles` tiles of 4096 coefficients (limbs x N / 4096) run the
  * 8-coefficients-per-thread kernels, which finish a tile in about half the time of the
  * 16-per-thread kernels and so suit launches of a few waves; larger passes run 16 per thread.
- * -1 restores the default (1024 tiles, measured on GB300); 0 disables the small
+ * -1 restores the default (512 tiles, measured on GB300); 0 disables the small
  * kernels.  Every setting gives the same words.  No counterpart in the reference. */
 /* Kernel chains of one call launched with programmatic dependent launch (on by default): a
  * kernel may be scheduled while its predecessor drains its last wave and starts once that
@@ -111,11 +111,16 @@ int fhe_context_set_launch_overlap(fhe_context *ctx, int enable);
 int fhe_context_ntt_small_launch(const fhe_context *ctx);
 int fhe_context_set_ntt_small_launch(fhe_context *ctx, int tiles);
 
-/* Coefficients per CTA of those small-launch passes: 2048 (the default: twice the CTAs, so a
- * launch of a few hundred tiles spreads evenly over the SMs) or 4096.  Every setting gives the
- * same words.  No counterpart in the reference. */
+/* Coefficients per CTA of those small-launch passes: 1024 (the default) or 2048.  Smaller CTAs
+ * spread a launch of a few hundred tiles evenly over the SMs and wait less at their barriers.
+ * Every setting gives the same words.  No counterpart in the reference. */
 int fhe_context_ntt_small_tile(const fhe_context *ctx);
 int fhe_context_set_ntt_small_tile(fhe_context *ctx, int coefficients);
+
+/* Coefficients per CTA of the larger (16 coefficients per thread) NTT passes: 2048 (the default)
+ * or 4096.  Every setting gives the same words.  No counterpart in the reference. */
+int fhe_context_ntt_tile(const fhe_context *ctx);
+int fhe_context_set_ntt_tile(fhe_context *ctx, int coefficients);
 
 /* Reads and clears the context's device status word (synchronises the device).  Non-zero
  * means a bounded wait inside a tensor-core kernel gave up and that call's output is invalid.

@@ -166,9 +166,23 @@ int fhe_context_ntt_small_tile(const fhe_context *ctx) {
 int fhe_context_set_ntt_small_tile(fhe_context *ctx, int coefficients) {
     return guarded([&] {
         pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
-        if (coefficients != pfg::kTileElems && coefficients != pfg::kTileElems / 2)
-            throw std::invalid_argument("small-launch tile must be 2048 or 4096 coefficients");
+        if (coefficients != pfg::kTileElems / 2 && coefficients != pfg::kTileElems / 4)
+            throw std::invalid_argument("small-launch tile must be 1024 or 2048 coefficients");
         c.ntt_small_tile = coefficients;
+    }, false);
+}
+
+int fhe_context_ntt_tile(const fhe_context *ctx) {
+    if (!ctx || !ctx->c) return 0;
+    return ctx->c->ntt_tile;
+}
+
+int fhe_context_set_ntt_tile(fhe_context *ctx, int coefficients) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        if (coefficients != pfg::kTileElems && coefficients != pfg::kTileElems / 2)
+            throw std::invalid_argument("NTT tile must be 2048 or 4096 coefficients");
+        c.ntt_tile = coefficients;
     }, false);
 }
 

@@ -21,12 +21,12 @@
 namespace pfg {
 
 // Default small-launch bound for the 8-coefficients-per-thread NTT passes, in 4096-coefficient
-// tiles.  Measured on GB300 with the half-size (2048-coefficient) tiles of those passes (N = 2^16,
-// 30 + 5 primes; N = 2^15 BFV): up to 1024 tiles (the 30-limb inverse transform, the 12-limb
-// mod-down transform, the 58-limb mod-down / rescale forward transform) is fastest end to end
-// (HMult 0.4134 -> 0.4112 ms against a bound of 512, BFV mult+relin 0.386 -> 0.378 ms); the
-// 180-limb mod-up transform (2880 tiles) stays faster at 16 per thread.
-constexpr int kNttSmallLaunchTiles = 1024;
+// tiles.  Measured on GB300 with 1024-coefficient tiles for those passes and 2048 for the others
+// (N = 2^16, 30 + 5 primes; N = 2^15 BFV): a bound of 512 (the 30-limb inverse transform and the
+// 12-limb mod-down transform at 8 per thread, the 58-limb forward transform of the mod-down /
+// rescale at 16) gives HMult 0.4012 ms against 0.4028 at 1024 and 0.4169 at 4096; BFV
+// mult+relin prefers 1024 (0.3677 vs 0.3718 ms).
+constexpr int kNttSmallLaunchTiles = 512;
 
 // Block cap of the grid-stride element-wise kernels: 16 blocks of 256 threads per SM of GB300's
 // 152 SMs (8 resident per SM, two waves); a larger grid only adds block scheduling.
@@ -129,9 +129,11 @@ struct Context {
     // NTT passes over at most this many 4096-coefficient tiles run 8 coefficients per thread
     // (NttShape<8>); larger ones 16.  -1: the default, kNttSmallLaunchTiles.
     int ntt_small_tiles = -1;
-    // coefficients per CTA of those small passes: 2048 (twice the CTAs) or 4096; any setting
-    // gives the same words
-    int ntt_small_tile = kTileElems / 2;
+    // coefficients per CTA of those small passes (1024 or 2048) and of the larger, 16-per-thread
+    // passes (2048 or 4096); smaller CTAs spread a launch more evenly over the SMs and wait less
+    // at their barriers.  Any setting gives the same words.
+    int ntt_small_tile = kTileElems / 4;
+    int ntt_tile = kTileElems / 2;
     // kernel chains launched with programmatic dependent launch (pdl.cuh); any setting gives the
     // same words
     bool pdl = true;

@@ -112,32 +112,47 @@ void row_pass_e(const Context &c, dim3 grid, Map m, Load ld, Store st, cudaStrea
 }
 
 // One pass over `blocks` limbs (blockIdx.y) of N / TILE tiles each (blockIdx.x).  Launches of
-// at most c.ntt_small_limit() 4096-coefficient tiles take the 8-coefficients-per-thread kernels,
-// on tiles of c.ntt_small_tile coefficients; larger ones 16 per thread on 4096.
+// at most c.ntt_small_limit() 4096-coefficient tiles take the 8-coefficients-per-thread kernels
+// on tiles of c.ntt_small_tile coefficients; larger ones 16 per thread on c.ntt_tile.
+template <bool COL, bool FWD, bool LAST, int E, class Map, class Load, class Store>
+void pass_tiles(const Context &c, int tile, int blocks, Map m, Load ld, Store st, cudaStream_t s) {
+    auto go = [&]<int TILE>() {
+        const dim3 grid((unsigned)(c.n / TILE), (unsigned)blocks);
+        if constexpr (COL)
+            col_pass_e<FWD, LAST, E, TILE>(c, grid, m, ld, st, s);
+        else
+            row_pass_e<FWD, LAST, E, TILE>(c, grid, m, ld, st, s);
+    };
+    // built shapes: 16 per thread on 2048 or 4096 coefficients, 8 per thread on 1024 or 2048
+    if constexpr (E == 16) {
+        if (tile == kTileElems)
+            go.template operator()<kTileElems>();
+        else
+            go.template operator()<kTileElems / 2>();
+    } else {
+        if (tile == kTileElems / 2)
+            go.template operator()<kTileElems / 2>();
+        else
+            go.template operator()<kTileElems / 4>();
+    }
+}
+
 template <bool FWD, bool LAST, class Map, class Load, class Store>
 void col_pass(const Context &c, int blocks, Map m, Load ld, Store st, cudaStream_t s) {
-    const long long tiles = (long long)(c.n / kTileElems) * blocks;
     count_launch();
-    if (tiles > c.ntt_small_limit())
-        col_pass_e<FWD, LAST, 16, kTileElems>(c, dim3((unsigned)(c.n / kTileElems), (unsigned)blocks), m, ld, st, s);
-    else if (c.ntt_small_tile == kTileElems / 2)
-        col_pass_e<FWD, LAST, 8, kTileElems / 2>(c, dim3((unsigned)(c.n / (kTileElems / 2)), (unsigned)blocks), m, ld,
-                                                 st, s);
+    if ((long long)(c.n / kTileElems) * blocks > c.ntt_small_limit())
+        pass_tiles<true, FWD, LAST, 16>(c, c.ntt_tile, blocks, m, ld, st, s);
     else
-        col_pass_e<FWD, LAST, 8, kTileElems>(c, dim3((unsigned)(c.n / kTileElems), (unsigned)blocks), m, ld, st, s);
+        pass_tiles<true, FWD, LAST, 8>(c, c.ntt_small_tile, blocks, m, ld, st, s);
 }
 
 template <bool FWD, bool LAST, class Map, class Load, class Store>
 void row_pass(const Context &c, int blocks, Map m, Load ld, Store st, cudaStream_t s) {
-    const long long tiles = (long long)(c.n / kTileElems) * blocks;
     count_launch();
-    if (tiles > c.ntt_small_limit())
-        row_pass_e<FWD, LAST, 16, kTileElems>(c, dim3((unsigned)(c.n / kTileElems), (unsigned)blocks), m, ld, st, s);
-    else if (c.ntt_small_tile == kTileElems / 2)
-        row_pass_e<FWD, LAST, 8, kTileElems / 2>(c, dim3((unsigned)(c.n / (kTileElems / 2)), (unsigned)blocks), m, ld,
-                                                 st, s);
+    if ((long long)(c.n / kTileElems) * blocks > c.ntt_small_limit())
+        pass_tiles<false, FWD, LAST, 16>(c, c.ntt_tile, blocks, m, ld, st, s);
     else
-        row_pass_e<FWD, LAST, 8, kTileElems>(c, dim3((unsigned)(c.n / kTileElems), (unsigned)blocks), m, ld, st, s);
+        pass_tiles<false, FWD, LAST, 8>(c, c.ntt_small_tile, blocks, m, ld, st, s);
 }
 
 // Forward transform: column pass (load functor) -> row pass (store functor); the

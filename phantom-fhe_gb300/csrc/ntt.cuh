@@ -8,12 +8,11 @@
 // Design.  N = N1 * N2 (N1 = 2^L1 rows, N2 = 2^L2 columns of the row-major limb).  The first
 // L1 stages only pair elements of the same column, the last L2 stages only pair elements of
 // the same row, so a transform is two passes: a column pass and a row pass.  Each CTA
-// stages a tile of V whole vectors (columns or rows, V*M = 4096 coefficients, 34 KB) in
-// shared memory with one coalesced sweep, runs all of that pass's stages as register
-// phases of up to four radix-2 stages (16 coefficients per thread; 8 and radix-8 phases for small
-// launches, see NttShape; Harvey lazy butterflies,
-// twiddle and Shoup quotient fetched as one 16-byte pair), and writes the tile back with one
-// coalesced sweep.  Every launch covers all limbs (and polynomials) of an operation; the
+// stages a tile of V whole vectors (columns or rows, V*M = 1024, 2048 or 4096 coefficients,
+// 9-34 KB) in shared memory with one coalesced sweep, runs all of that pass's stages as
+// register phases of up to four radix-2 stages (16 coefficients per thread; 8 and radix-8
+// phases for small launches, see NttShape; Harvey-style lazy butterflies, twiddle and Shoup
+// quotient fetched as one 16-byte pair), and writes the tile back with one coalesced sweep.  Every launch covers all limbs (and polynomials) of an operation; the
 // load and store sweeps take functors so neighbouring element-wise work (base-conversion
 // input, scaling, mod-down combine, inner-product accumulation) fuses into the pass.
 #pragma once
@@ -38,16 +37,19 @@ constexpr int kTileElems = 4096;  // V * M coefficients per CTA
 
 // E coefficients per thread: 16 (radix-16 register phases, 256 threads per tile) for large
 // launches, or 8 (radix-8 phases, 512 threads per tile: half the serial work per thread, so
-// about half the time per tile) for launches of a few waves, which are latency-bound.  Small
-// launches may also use half-size tiles (TILE = 2048 coefficients, 256 threads at E = 8): twice
-// the CTAs, so a launch of a few hundred tiles spreads more evenly over the SMs.
+// about half the time per tile) for launches of a few waves, which are latency-bound.  A tile
+// may also hold 2048 or 1024 coefficients (TILE): more, smaller CTAs, which spread a launch of a
+// few hundred tiles evenly over the SMs and stall less at their barriers (the defaults are 2048
+// at E = 16 and 1024 at E = 8).
 template <int E, int TILE = kTileElems>
 struct NttShape {
     static_assert(E == 8 || E == 16, "8 or 16 coefficients per thread");
-    static_assert(TILE == kTileElems || (TILE == kTileElems / 2 && E == 8), "4096, or 2048 at E = 8");
+    static_assert(TILE == kTileElems || TILE == kTileElems / 2 || TILE == kTileElems / 4,
+                  "4096, 2048 or 1024 coefficients per tile");
     static constexpr int LGE = E == 16 ? 4 : 3;
     static constexpr int kThreads = TILE / E;
-    static constexpr int kMinBlocks = E == 16 ? 3 : (TILE == kTileElems ? 2 : 4);
+    // 80 registers a thread at 16 per thread, 64 at 8
+    static constexpr int kMinBlocks = (E == 16 ? 3 : 2) * (kTileElems / TILE);
 };
 
 __host__ __device__ constexpr int ntt_num_phases(int lm, int lge) { return (lm + lge - 1) / lge; }

@@ -66,6 +66,8 @@ def _load():
     L.fhe_context_set_launch_overlap.argtypes = [_vp, ctypes.c_int]
     L.fhe_context_ntt_small_tile.argtypes = [_vp]
     L.fhe_context_set_ntt_small_tile.argtypes = [_vp, ctypes.c_int]
+    L.fhe_context_ntt_tile.argtypes = [_vp]
+    L.fhe_context_set_ntt_tile.argtypes = [_vp, ctypes.c_int]
     L.fhe_context_ntt_small_launch.argtypes = [_vp]
     L.fhe_context_set_ntt_small_launch.argtypes = [_vp, ctypes.c_int]
     L.fhe_context_autotune.argtypes = [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)]
@@ -230,8 +232,17 @@ class Context:
         _check(lib.fhe_context_set_launch_overlap(self._h, int(bool(on))))
 
     @property
+    def ntt_tile(self):
+        """Coefficients per CTA (2048 or 4096) of the 16-per-thread NTT passes (same words)."""
+        return int(lib.fhe_context_ntt_tile(self._h))
+
+    @ntt_tile.setter
+    def ntt_tile(self, coefficients):
+        _check(lib.fhe_context_set_ntt_tile(self._h, int(coefficients)))
+
+    @property
     def ntt_small_tile(self):
-        """Coefficients per CTA (2048 or 4096) of the small-launch NTT passes (same words)."""
+        """Coefficients per CTA (1024 or 2048) of the small-launch NTT passes (same words)."""
         return int(lib.fhe_context_ntt_small_tile(self._h))
 
     @ntt_small_tile.setter

@@ -161,9 +161,9 @@ def test_every_ntt_split_gives_the_same_words(pg, log_n, splits):
 
 @pytest.mark.parametrize("log_n", [12, 13, 16])
 def test_small_launch_kernels_give_the_same_words(pg, log_n):
-    """NTT passes with 8 coefficients per thread (small launches, on 2048- or 4096-coefficient
-    tiles) and with 16 give the same words: every pass forced to one shape, then the others, on
-    the NTT, a key switch and HMult."""
+    """NTT passes with 8 coefficients per thread (small launches, on 1024- or 2048-coefficient
+    tiles) and with 16 (on 2048- or 4096-coefficient tiles) give the same words: every pass
+    forced to one shape, then the others, on the NTT, a key switch and HMult."""
     n = 1 << log_n
     bits = [60] + [40] * 5 + [60, 60]
     mods = pg.create_coeff_modulus(n, bits)
@@ -181,10 +181,13 @@ def test_small_launch_kernels_give_the_same_words(pg, log_n):
     want_ntt = oc.ntt_fwd(x.reshape(-1, n), tbl=list(range(len(mods))) * 2).reshape(x.shape)
     want_ks = oc.keyswitch(6, ct, c2, key)
     want_hm = oc.rescale(6, oc.ckks_mul_relin(6, a, b, key))
-    for tiles, tile in ((0, 2048), (1 << 30, 4096), (1 << 30, 2048), (-1, 2048)):
+    # (small-launch bound, coefficients per CTA at 8 per thread, at 16 per thread)
+    for tiles, small, large in ((0, 1024, 4096), (0, 1024, 2048), (1 << 30, 2048, 2048),
+                                (1 << 30, 1024, 2048), (-1, 1024, 2048)):
         ctx.ntt_small_launch = tiles
-        ctx.ntt_small_tile = tile  # coefficients per CTA of the 8-per-thread passes
-        what = f"small-launch bound {tiles}, tile {tile}"
+        ctx.ntt_small_tile = small
+        ctx.ntt_tile = large
+        what = f"small-launch bound {tiles}, tiles {small} / {large}"
         t = pg.to_device(x)
         ctx.ntt_forward(t, 2, len(mods))
         _eq(t, want_ntt, f"forward NTT, {what}")
@@ -196,11 +199,13 @@ def test_small_launch_kernels_give_the_same_words(pg, log_n):
         out = torch.empty((2, 5, n), dtype=torch.int64, device="cuda")
         ctx.multiply_relin_rescale(ws, pg.to_device(a), pg.to_device(b), out, 1, k)
         _eq(out, want_hm, f"HMult, {what}")
-    assert ctx.ntt_small_launch == 1024 and ctx.ntt_small_tile == 2048
+    assert (ctx.ntt_small_launch, ctx.ntt_small_tile, ctx.ntt_tile) == (512, 1024, 2048)
     with pytest.raises(pg.InvalidArgument):
         ctx.ntt_small_launch = -2
     with pytest.raises(pg.InvalidArgument):
-        ctx.ntt_small_tile = 1024
+        ctx.ntt_small_tile = 4096
+    with pytest.raises(pg.InvalidArgument):
+        ctx.ntt_tile = 1024
 
 
 @pytest.mark.parametrize("log_n", [12, 14])
