@@ -99,7 +99,7 @@ int fhe_context_autotune(fhe_context *ctx, int *chosen_l1, float *best_us);
 /* NTT passes over at most `tiles` tiles of 4096 coefficients (limbs x N / 4096) run the
  * 8-coefficients-per-thread kernels, which finish a tile in about half the time of the
  * 16-per-thread kernels and so suit launches of a few waves; larger passes run 16 per thread.
- * -1 restores the default (512 tiles, measured on GB300); 0 disables the small
+ * -1 restores the default (measured on GB300: 512 tiles for N >= 2^16, 1024 below); 0 disables the small
  * kernels.  Every setting gives the same words.  No counterpart in the reference. */
 /* Kernel chains of one call launched with programmatic dependent launch (on by default): a
  * kernel may be scheduled while its predecessor drains its last wave and starts once that

@@ -20,13 +20,14 @@
 
 namespace pfg {
 
-// Default small-launch bound for the 8-coefficients-per-thread NTT passes, in 4096-coefficient
-// tiles.  Measured on GB300 with 1024-coefficient tiles for those passes and 2048 for the others
-// (N = 2^16, 30 + 5 primes; N = 2^15 BFV): a bound of 512 (the 30-limb inverse transform and the
-// 12-limb mod-down transform at 8 per thread, the 58-limb forward transform of the mod-down /
-// rescale at 16) gives HMult 0.4012 ms against 0.4028 at 1024 and 0.4169 at 4096; BFV
-// mult+relin prefers 1024 (0.3677 vs 0.3718 ms).
+// Default small-launch bounds for the 8-coefficients-per-thread NTT passes, in 4096-coefficient
+// tiles, measured on GB300 with 1024-coefficient tiles for those passes and 2048 for the others.
+// N >= 2^16 (30 + 5 primes): 512 — the 30-limb inverse transform and the 12-limb mod-down
+// transform at 8 per thread, the 58-limb forward transform of the mod-down / rescale at 16 —
+// gives HMult 0.4012 ms against 0.4028 at 1024 and 0.4169 at 4096.  N = 2^15 (BFV, 16 + 2
+// primes): 1024 gives mult+relin 0.3677 ms against 0.3718 at 512.
 constexpr int kNttSmallLaunchTiles = 512;
+constexpr int kNttSmallLaunchTilesBelow2_16 = 1024;
 
 // Block cap of the grid-stride element-wise kernels: 16 blocks of 256 threads per SM of GB300's
 // 152 SMs (8 resident per SM, two waves); a larger grid only adds block scheduling.
@@ -127,7 +128,7 @@ struct Context {
     // supported split gives the same words; the autotuner (fhe_context_autotune) picks one.
     int l1_sel = 0;  // 0: log_n / 2
     // NTT passes over at most this many 4096-coefficient tiles run 8 coefficients per thread
-    // (NttShape<8>); larger ones 16.  -1: the default, kNttSmallLaunchTiles.
+    // (NttShape<8>); larger ones 16.  -1: the default for the degree (kNttSmallLaunchTiles*).
     int ntt_small_tiles = -1;
     // coefficients per CTA of those small passes (1024 or 2048) and of the larger, 16-per-thread
     // passes (2048 or 4096); smaller CTAs spread a launch more evenly over the SMs and wait less
@@ -137,7 +138,10 @@ struct Context {
     // kernel chains launched with programmatic dependent launch (pdl.cuh); any setting gives the
     // same words
     bool pdl = true;
-    long long ntt_small_limit() const { return ntt_small_tiles >= 0 ? ntt_small_tiles : kNttSmallLaunchTiles; }
+    long long ntt_small_limit() const {
+        if (ntt_small_tiles >= 0) return ntt_small_tiles;
+        return log_n >= 16 ? kNttSmallLaunchTiles : kNttSmallLaunchTilesBelow2_16;
+    }
     int l1() const { return l1_sel ? l1_sel : log_n / 2; }
     int l2() const { return log_n - l1(); }
     bool split_ok(int l) const { return l >= 6 && l <= 8 && log_n - l >= 6 && log_n - l <= 9; }

@@ -199,7 +199,7 @@ def test_small_launch_kernels_give_the_same_words(pg, log_n):
         out = torch.empty((2, 5, n), dtype=torch.int64, device="cuda")
         ctx.multiply_relin_rescale(ws, pg.to_device(a), pg.to_device(b), out, 1, k)
         _eq(out, want_hm, f"HMult, {what}")
-    assert (ctx.ntt_small_launch, ctx.ntt_small_tile, ctx.ntt_tile) == (512, 1024, 2048)
+    assert (ctx.ntt_small_launch, ctx.ntt_small_tile, ctx.ntt_tile) == (512 if log_n >= 16 else 1024, 1024, 2048)
     with pytest.raises(pg.InvalidArgument):
         ctx.ntt_small_launch = -2
     with pytest.raises(pg.InvalidArgument):
