@@ -471,19 +471,21 @@ def run_ours(args):
     da = [torch.empty((2, l, N), dtype=torch.int64, device="cuda") for _ in range(2)]
     db = [torch.empty((2, l, N), dtype=torch.int64, device="cuda") for _ in range(2)]
     do = [torch.empty((2, l - 1, N), dtype=torch.int64, device="cuda") for _ in range(2)]
-    h2d_s, d2h_s = torch.cuda.Stream(), torch.cuda.Stream()
-    ev = {k: [torch.cuda.Event() for _ in range(2)] for k in ("h2d", "comp", "d2h")}
+    # the two input ciphertexts travel on two streams, so two copy engines carry them at once
+    h2d_s, h2d_s2, d2h_s = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+    ev = {k: [torch.cuda.Event() for _ in range(2)] for k in ("h2d", "h2d2", "comp", "d2h")}
     started = [False, False]
 
     def e2e_step(i):
         b = i % 2
-        with torch.cuda.stream(h2d_s):
-            if started[b]:
-                h2d_s.wait_event(ev["comp"][b])  # inputs of the operation two steps back consumed
-            da[b].copy_(pin_a[i % PAIRS], non_blocking=True)
-            db[b].copy_(pin_b[i % PAIRS], non_blocking=True)
-            ev["h2d"][b].record(h2d_s)
+        for hs, dst, src, e in ((h2d_s, da, pin_a, "h2d"), (h2d_s2, db, pin_b, "h2d2")):
+            with torch.cuda.stream(hs):
+                if started[b]:
+                    hs.wait_event(ev["comp"][b])  # inputs of the operation two steps back consumed
+                dst[b].copy_(src[i % PAIRS], non_blocking=True)
+                ev[e][b].record(hs)
         stream.wait_event(ev["h2d"][b])
+        stream.wait_event(ev["h2d2"][b])
         if started[b]:
             stream.wait_event(ev["d2h"][b])  # its output buffer read back
         ctx.multiply_relin_rescale(ws, da[b], db[b], do[b], CHAIN, key, stream)
@@ -499,6 +501,7 @@ def run_ours(args):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         h2d_s.wait_event(e0)
+        h2d_s2.wait_event(e0)
         for i in range(k):
             e2e_step(i)
         stream.wait_stream(d2h_s)  # every result back on the host
