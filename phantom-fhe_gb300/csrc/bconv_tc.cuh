@@ -117,7 +117,10 @@ __global__ void __launch_bounds__(tc::kPipeThreads, 1)
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ uint64_t s_p[NSLOT][tc::kMaxOut], s_off[NSLOT][tc::kMaxOut];
     __shared__ float s_inv[NSLOT][tc::kMaxOut];
-    __shared__ TcGroup s_grp[NSLOT];
+    // raw storage: TcGroup's default member initialisers would ask for a dynamic initialisation
+    // that shared memory does not have; every slot is written (thread 0, in fill) before it is read
+    __shared__ __align__(alignof(TcGroup)) unsigned char s_grp_raw[NSLOT * sizeof(TcGroup)];
+    TcGroup *const s_grp = reinterpret_cast<TcGroup *>(s_grp_raw);
     __shared__ int s_bslot[NSLOT];
     __shared__ uint64_t s_z[tc::kRows];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
