@@ -18,6 +18,10 @@
  *  - Calls enqueue work on `stream` (a cudaStream_t; NULL = the legacy default stream) and
  *    return without synchronising.  Calls never allocate device memory: scratch comes from an
  *    fhe_workspace, which must not be shared by two calls that can run concurrently.
+ *  - A context is read-only for the evaluation calls, so any number of host threads may use
+ *    one context at once (each with its own workspace).  The tuning setters below
+ *    (fhe_context_set_* and fhe_context_autotune) change it: call them before the context is
+ *    shared, or with no other call on it in flight.
  *  - Return value: FHE_OK or a negative status.  FHE_ERR_INVALID_ARGUMENT and FHE_ERR_LOGIC
  *    correspond to the std::invalid_argument / std::logic_error the reference throws;
  *    fhe_last_error() returns the message of the calling thread's last failure.
