@@ -35,12 +35,12 @@ __device__ __forceinline__ TwPair ld_tw(const TwPair *t, uint32_t idx) {
 
 constexpr int kTileElems = 4096;  // V * M coefficients per CTA
 
-// E coefficients per thread: 16 (radix-16 register phases, 256 threads per tile) for large
-// launches, or 8 (radix-8 phases, 512 threads per tile: half the serial work per thread, so
-// about half the time per tile) for launches of a few waves, which are latency-bound.  A tile
-// may also hold 2048 or 1024 coefficients (TILE): more, smaller CTAs, which spread a launch of a
-// few hundred tiles evenly over the SMs and stall less at their barriers (the defaults are 2048
-// at E = 16 and 1024 at E = 8).
+// E coefficients per thread: 16 (radix-16 register phases) for large launches, or 8 (radix-8
+// phases: half the serial work per thread) for launches of a few waves, which are
+// latency-bound.  A tile holds TILE = 4096, 2048 or 1024 coefficients, TILE / E threads: the
+// smaller tiles give more, smaller CTAs, which spread a launch of a few hundred tiles evenly
+// over the SMs and stall less at their barriers (the defaults are 2048 at E = 16, 128 threads,
+// and 1024 at E = 8, 128 threads).
 template <int E, int TILE = kTileElems>
 struct NttShape {
     static_assert(E == 8 || E == 16, "8 or 16 coefficients per thread");
