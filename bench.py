@@ -233,8 +233,11 @@ def matvec_bench(pg, torch, timed, stream, rank, profile_only=False):
 
     batch(True)
     if profile_only:
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("matvec_case")  # lets a profiler skip the setup's launches
         batch(True)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         return {}
     torch.cuda.synchronize()
     l0 = pg.lib.fhe_kernel_launches()
