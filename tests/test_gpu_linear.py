@@ -111,7 +111,7 @@ def _diags(rng, mods, l, n):
     return O.random_residues(rng, mods[:l], n, D)
 
 
-def _plain_sum(babies, diags, g, mods, l):
+def _plain_sum(babies, diags, g, mods, l, G=G):
     acc = None
     for b in range(G):
         k = g * G + b
@@ -144,8 +144,9 @@ def test_bsgs_reference_loop_word_for_word(lin, pg, chain):
     _eq(out, oc.rescale(l, result), "BSGS (reference loop)")
 
 
-@pytest.mark.parametrize("chain", [1, 3])
-def test_bsgs_hoisted_horner_word_for_word(lin, pg, chain):
+# (G, B): a ragged last giant step (G = 4, B = 3, D = 10) and a deeper Horner chain (G = 2, B = 5)
+@pytest.mark.parametrize("chain,G,B", [(1, G, B), (3, G, B), (1, 2, 5)])
+def test_bsgs_hoisted_horner_word_for_word(lin, pg, chain, G, B):
     ctx, oc, mods, keys, gks, ws = lin
     rng = np.random.default_rng(20 + chain)
     l = ctx.level(chain)
@@ -164,7 +165,7 @@ def test_bsgs_hoisted_horner_word_for_word(lin, pg, chain):
     for g in reversed(range(B)):
         if result is not None:
             result = oc.ckks_apply_galois(l, result, *_key_of(ctx, keys, G))
-        inner = _plain_sum(babies, diags, g, mods, l)
+        inner = _plain_sum(babies, diags, g, mods, l, G)
         result = inner if result is None else _addmod(result, inner, mods[:l])
     _eq(out, oc.rescale(l, result), "BSGS (hoisted, Horner)")
 
