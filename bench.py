@@ -173,7 +173,10 @@ def run_reference(args):
     dt = time.perf_counter() - t0
     value = steps / dt
     sample = f"{steps} full HMult+relin+rescale ops at N=2^16, l=30 (of {args.steps} requested)"
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "ops/s", "n_gpus": world,
+    line = {"impl": "reference", "arm": "cpu_port",
+            "arm_note": ("PhantomFHE has no CPU implementation of this path: this arm is the CPU restatement "
+                         "(oracle/) on the host cores, not the reference's CUDA kernels"),
+            "metric": METRIC, "value": value, "unit": "ops/s", "n_gpus": world,
             "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1000 * dt / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic", "config": CONFIG,

@@ -188,11 +188,13 @@ int fhe_rescale_to_next(const fhe_context *ctx, fhe_workspace *ws, const uint64_
 /* No counterpart in the reference: fhe_rescale_to_next for callers that may not allocate
  * device memory (for example a plugin whose host process owns all device memory and passes
  * in only the input and output buffers), so cannot hold an fhe_workspace.  Its scratch is a
- * fixed 2 MiB array inside the library (kept by every GPU that loads it), which limits
- * size * N to 2^18 words; larger requests fail with FHE_ERR_INVALID_ARGUMENT.  It calls no
- * allocator.  The first call on a device looks up the array's device address, so make it
- * before any stream capture.  All calls on a device share the array: calls that overlap on
- * the GPU race and must be serialised by the caller. */
+ * fixed 2 MiB array inside the library, which limits size * N to 2^18 words; larger requests
+ * fail with FHE_ERR_INVALID_ARGUMENT.  It calls no allocator.  The driver commits the 2 MiB
+ * on a device when it loads the library's module there, which (with lazy module loading) is
+ * the address lookup fhe_context_create makes, and the device keeps it until the process
+ * exits.  The address is kept in the context, so call this on the context's device (another
+ * device is rejected) and create the context before any stream capture.  All calls on a device
+ * share the array: calls that overlap on the GPU race and must be serialised by the caller. */
 int fhe_rescale_to_next_noalloc(const fhe_context *ctx, const uint64_t *in, uint64_t *out, size_t size,
                                 size_t chain_index, void *stream);
 

@@ -160,6 +160,8 @@ std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, cons
     const int nQ = c->nQ, nP = c->nP;
     int dev = 0;
     check(cudaGetDevice(&dev), "cudaGetDevice");
+    c->device = dev;
+    c->noalloc_scratch = noalloc_scratch_address(&c->noalloc_words);
     check(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev), "multiprocessor count");
     check(cudaDeviceGetAttribute(&c->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "shared memory limit");
     {

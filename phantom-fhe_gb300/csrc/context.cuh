@@ -138,6 +138,12 @@ struct Context {
     // kernel chains launched with programmatic dependent launch (pdl.cuh); any setting gives the
     // same words
     bool pdl = true;
+    // device the context's tables live on, and the device address of the fixed scratch array of
+    // fhe_rescale_to_next_noalloc on it (looked up at creation, with that device current, so the
+    // address belongs to the CUDA context the tables were made in)
+    int device = 0;
+    uint64_t *noalloc_scratch = nullptr;
+    size_t noalloc_words = 0;
     long long ntt_small_limit() const {
         if (ntt_small_tiles >= 0) return ntt_small_tiles;
         return log_n >= 16 ? kNttSmallLaunchTiles : kNttSmallLaunchTilesBelow2_16;
@@ -154,6 +160,10 @@ struct Context {
     int qlp_table(int l, int jj) const { return jj < l ? jj : nQ + (jj - l); }
     const uint32_t *perm_table(uint32_t elt);  // builds and caches on first use
 };
+
+// Device address and size (words) of the no-allocation scratch array on the current device
+// (noalloc.cu); throws std::runtime_error when the lookup fails.
+uint64_t *noalloc_scratch_address(size_t *words);
 
 // Builds every table; throws std::invalid_argument / std::logic_error on bad parameters.
 std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, const std::vector<uint64_t> &coeff_modulus,

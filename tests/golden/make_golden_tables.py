@@ -4,7 +4,7 @@ Builds oracle/_ref/ref_dump (oracle/Makefile.ref compiles PhantomFHE's src/host/
 unmodified, from the reference checkout named by REF) and stores its output.  Arrays
 longer than 64 words are stored as the SHA-256 of their little-endian uint64 bytes plus
 their first and last 4 entries; shorter arrays are stored in full.  Run from the repo
-root:  python tests/golden/make_golden_tables.py [REF]
+root:  python tests/golden/make_golden_tables.py [REF]  (default: $PHANTOM_FHE_REFERENCE)
 """
 import hashlib
 import json
@@ -30,7 +30,9 @@ def compact(obj):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PHANTOM_FHE_REFERENCE")
+    if not ref:
+        sys.exit("name the PhantomFHE source checkout: make_golden_tables.py REF or PHANTOM_FHE_REFERENCE=REF")
     subprocess.check_call(["make", "-s", "-f", "oracle/Makefile.ref", f"REF={ref}", "-j8"], cwd=ROOT)
     raw = subprocess.check_output([os.path.join(ROOT, "oracle", "_ref", "ref_dump")])
     data = compact(json.loads(raw))

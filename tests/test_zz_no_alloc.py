@@ -27,17 +27,19 @@ def _call_noalloc(pg, ctx, src, dst, size, chain):
                                            size, chain, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
 
 
-@pytest.mark.parametrize("log_n,bits,special", [
-    (16, [60] + [40] * 29 + [60] * 5, 5),
-    (12, [60, 40, 40, 40, 40, 40, 60, 60], 2),
+@pytest.mark.parametrize("log_n,bits,special,calls", [
+    (16, [60] + [40] * 29 + [60] * 5, 5, ((1, 2), (3, 3), (1, 2))),
+    (12, [60, 40, 40, 40, 40, 40, 60, 60], 2, ((1, 2), (3, 3), (1, 2))),
+    # size * N = 2^18 exactly: the largest request the scratch accepts, twice in a row
+    (17, [60, 40, 40, 40, 40, 60, 60], 2, ((1, 2), (2, 2))),
 ])
-def test_noalloc_rescale_matches_workspace_rescale(pg, log_n, bits, special):
+def test_noalloc_rescale_matches_workspace_rescale(pg, log_n, bits, special, calls):
     n = 1 << log_n
     mods = pg.create_coeff_modulus(n, bits)
     ctx = pg.Context(n, mods, special)
     ws = ctx.workspace()
     rng = np.random.default_rng(99 + log_n)
-    for chain, size in ((1, 2), (3, 3), (1, 2)):  # consecutive calls share the scratch
+    for chain, size in calls:  # consecutive calls share the scratch
         l = ctx.level(chain)
         ct = pg.to_device(O.random_residues(rng, mods[:l], n, size))
         want = torch.empty((size, l - 1, n), dtype=torch.int64, device="cuda")
@@ -48,11 +50,11 @@ def test_noalloc_rescale_matches_workspace_rescale(pg, log_n, bits, special):
         assert torch.equal(got, want)
 
 
-def test_noalloc_rescale_rejects_sizes_beyond_its_scratch(pg):
-    n = 1 << 16
+@pytest.mark.parametrize("log_n,size", [(16, 5), (17, 3)])  # 5 * 2^16 and 3 * 2^17 words > 2^18
+def test_noalloc_rescale_rejects_sizes_beyond_its_scratch(pg, log_n, size):
+    n = 1 << log_n
     mods = pg.create_coeff_modulus(n, [60] + [40] * 5 + [60])
     ctx = pg.Context(n, mods, 1)
-    size = 5  # 5 * 2^16 words > the 2^18-word scratch
     l = ctx.level(1)
     ct = torch.zeros((size, l, n), dtype=torch.int64, device="cuda")
     out = torch.zeros((size, l - 1, n), dtype=torch.int64, device="cuda")
