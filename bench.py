@@ -203,8 +203,8 @@ def matvec_bench(pg, torch, timed, stream, rank, profile_only=False):
     hsteps = list(range(1, G + 1))
     xsteps = list(range(1, G)) + [g * G for g in range(1, B)]
     ctx = pg.Context(n, mods, 4, galois_elts=sorted({pg.elt_from_step(s, n) for s in hsteps + xsteps}))
-    ctx.autotune()
     ws = ctx.workspace()
+    ctx.autotune(ws)
     rng = np.random.default_rng(5000 + rank)
     sk = SecretKey(ctx, rng)
     gks = sk.galois_keys(ws, sorted(set(hsteps + xsteps)))
@@ -281,8 +281,8 @@ def run_ours(args):
     nq = len(BITS) - SPECIAL
     l = nq
     ctx = pg.Context(N, mods, SPECIAL)
-    tuning = ctx.autotune()  # NTT stage split, chosen by timing (setup, outside every timed region)
     ws = ctx.workspace()
+    tuning = ctx.autotune(ws)  # kernel shapes, chosen by timing this operation (setup, outside every timed region)
     rng = np.random.default_rng(1000 + rank)
     key = pg.KeySwitchKey(pg.to_device(random_residues(rng, mods, N, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), N)))
     elt1 = pg.elt_from_step(1, N)
@@ -380,6 +380,11 @@ def run_ours(args):
     t_hm_cc = timed(step, k2)
     t_ks_cc = timed(lambda i: ctx.keyswitch(ws, ct, c2, CHAIN, key, stream), k2)
     ctx.tensor_cores = tc_default
+    # ... and with the mod-up's row pass and the inner product as two kernels (t_mod_up written)
+    ctx.fused_keyswitch = False
+    t_hm_unfused = timed(step, k2)
+    t_ks_unfused = timed(lambda i: ctx.keyswitch(ws, ct, c2, CHAIN, key, stream), k2)
+    ctx.fused_keyswitch = True
     tc_status = ctx.device_status()
     # NTT throughput: 64 polynomials x 35 limbs (1.17 GB > 4x L2), forward transform
     polys, limbs = 64, len(mods)
@@ -441,8 +446,8 @@ def run_ours(args):
     nb = 1 << 15
     bmods = pg.create_coeff_modulus(nb, bfv_bits)
     bctx = pg.Context(nb, bmods, 2, scheme=pg.SCHEME_BFV, plain_modulus=65537)
-    btuning = bctx.autotune()
     bws = bctx.workspace()
+    btuning = bctx.autotune(bws)
     bkey = pg.KeySwitchKey(pg.to_device(random_residues(rng, bmods, nb, 2 * bctx.dnum)
                                         .reshape(bctx.dnum, 2, len(bmods), nb)))
     bct = [pg.to_device(random_residues(rng, bmods[:16], nb, 2)) for _ in range(2)]
@@ -541,7 +546,8 @@ def run_ours(args):
     line = {"metric": METRIC, "value": value, "unit": "ops/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": 1000 * t / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "config": dict(CONFIG, ntt_split=f"{tuning['ntt_split']}+{16 - tuning['ntt_split']} (autotuned)"),
+            "config": dict(CONFIG, tuning=dict({k: v for k, v in tuning.items() if k not in ("best_us",)},
+                                               source="autotuned on this operation")),
             "clocks": ck,
             "e2e": {"value": replica_throughput(args.steps, world, t_e2e), "unit": "ops/s",
                     "h2d_bytes_per_step": 2 * 2 * l * N * 8, "d2h_bytes_per_step": 2 * (l - 1) * N * 8},
@@ -555,7 +561,7 @@ def run_ours(args):
                       "bfv_n15_mult_relin_graph128_ops_per_s": 128 * world / t_graph,
                       "bfv_n15_mult_relin_loop128_ops_per_s": 128 * world / t_bloop,
                       "bfv_n15_mult_relin_loop128_cuda_core_ops_per_s": 128 * world / t_bloop_cc,
-                      "bfv_n15_ntt_split": btuning["ntt_split"],
+                      "bfv_n15_tuning": btuning,
                       "batch64_uneven_levels_ops_per_s": 64 * world / t_batch,
                       "batch64_as_single_calls_ops_per_s": 64 * world / t_loop,
                       "keyswitch_batch64_uneven_levels_per_s": 64 * world / t_ksb,
@@ -564,6 +570,8 @@ def run_ours(args):
                       "tensor_core_bconv": tc_default, "tensor_core_status": tc_status,
                       "hmult_relin_rescale_cuda_core_bconv_ops_per_s": k2 * world / t_hm_cc,
                       "keyswitch_cuda_core_bconv_per_s": k2 * world / t_ks_cc,
+                      "hmult_relin_rescale_unfused_modup_ops_per_s": k2 * world / t_hm_unfused,
+                      "keyswitch_unfused_modup_per_s": k2 * world / t_ks_unfused,
                       "ntt_forward_ms_64x35": 1000 * t_ntt,
                       "hmult_relin_rescale_algorithmic_bytes": 313524224,
                       "hmult_hbm_frac": 313524224 * value / world / 1e9 / peak,

@@ -100,6 +100,30 @@ int fhe_context_ntt_split(const fhe_context *ctx);
 int fhe_context_set_ntt_split(fhe_context *ctx, int l1);
 int fhe_context_autotune(fhe_context *ctx, int *chosen_l1, float *best_us);
 
+/* The context's kernel shapes; every setting gives the same words.  No counterpart in the
+ * reference, whose shapes are fixed (include/common.h, include/ntt.cuh:131-153). */
+typedef struct fhe_tuning {
+    int ntt_split;        /* NTT stages of the column pass (l1) */
+    int ntt_tile;         /* coefficients per CTA of the 16-per-thread NTT passes: 2048 or 4096 */
+    int ntt_small_tile;   /* ... of the 8-per-thread passes: 1024 or 2048 */
+    int ntt_small_launch; /* passes of at most this many 4096-coefficient tiles run 8 per thread */
+    int fused_keyswitch;  /* mod-up row pass fused with the inner product (CKKS) */
+    int tensor_cores;     /* base conversions on the tensor cores (where available) */
+    float best_us;        /* time of one timed operation with these shapes (autotuner) */
+    int evaluated;        /* configurations the autotuner timed (0: taken from the cache) */
+} fhe_tuning;
+
+/* Autotuner over the operation itself: times the context's benchmark workload at its top level,
+ * batch 1 (CKKS multiply + relinearise + rescale; BFV HPS multiply + relinearise), on uniform
+ * residues, over the NTT split, both NTT tiles, the small-launch bound, the fused key switch and
+ * the tensor-core conversions (coordinate descent, two sweeps), and applies the fastest.  With a
+ * cache_path, a JSON-lines file keyed by GPU name, scheme, N, |Q|, |P| and batch holds the choice:
+ * a matching entry is applied without timing (out->evaluated = 0), a new one is appended.  A
+ * one-time set-up call: it allocates its inputs and a key and synchronises. */
+int fhe_context_autotune_op(fhe_context *ctx, fhe_workspace *ws, const char *cache_path, fhe_tuning *out);
+int fhe_context_tuning(const fhe_context *ctx, fhe_tuning *out);
+int fhe_context_set_tuning(fhe_context *ctx, const fhe_tuning *t);
+
 /* NTT passes over at most `tiles` tiles of 4096 coefficients (limbs x N / 4096) run the
  * 8-coefficients-per-thread kernels, which finish a tile in about half the time of the
  * 16-per-thread kernels and so suit launches of a few waves; larger passes run 16 per thread.
@@ -111,6 +135,15 @@ int fhe_context_autotune(fhe_context *ctx, int *chosen_l1, float *best_us);
  * reference. */
 int fhe_context_launch_overlap(const fhe_context *ctx);
 int fhe_context_set_launch_overlap(fhe_context *ctx, int enable);
+
+/* The mod-up's forward NTT row pass fused with the key-switching inner product (on by default):
+ * one kernel finishes each digit's transform tile by tile and accumulates it against the key, so
+ * the mod-up output (src/rns_bconv.cu:530-628) is never written to or read back from device
+ * memory.  Used by the key switch, relinearisation, HMult and Galois calls; hoisted rotations keep
+ * the materialised mod-up (they reuse it).  Every setting gives the same words.  No counterpart in
+ * the reference. */
+int fhe_context_fused_keyswitch(const fhe_context *ctx);
+int fhe_context_set_fused_keyswitch(fhe_context *ctx, int enable);
 
 int fhe_context_ntt_small_launch(const fhe_context *ctx);
 int fhe_context_set_ntt_small_launch(fhe_context *ctx, int tiles);
@@ -293,6 +326,22 @@ int fhe_ckks_bsgs_matvec(const fhe_context *ctx, fhe_workspace *ws, uint64_t *sc
  * ciphertext's limbs, e an int64 polynomial of N coefficients; pt may be NULL (zero). */
 int fhe_ckks_encrypt_symmetric(const fhe_context *ctx, const uint64_t *pt, const uint64_t *s_ntt, const uint64_t *a,
                                const int64_t *e, uint64_t *out, size_t chain_index, void *stream);
+
+/* PhantomCKKSEncoder::encode (include/ckks.h, src/ckks.cu:68-138): `count` (1 .. N/2) complex
+ * slot values (device memory, interleaved re/im doubles) at `scale` -> plaintext pt [l][N]
+ * (device, NTT form) at chain_index.  The reference's FP64 special FFT (src/fft.cu), rounding and
+ * residues (src/rns_base.cu:49-163), so pt equals the reference's words.  Errors as the reference:
+ * "Input vector is empty" / "exceeds max slots", "scale out of bounds", "encoded values are too
+ * large" (FHE_ERR_INVALID_ARGUMENT).  Synchronises the stream once (the magnitude check). */
+int fhe_ckks_encode(const fhe_context *ctx, fhe_workspace *ws, const double *values, size_t count, double scale,
+                    size_t chain_index, uint64_t *pt, void *stream);
+
+/* PhantomCKKSEncoder::decode (src/ckks.cu:340-400): pt [l][N] (device, NTT form) at chain_index
+ * with its scale -> N/2 complex slots (device, interleaved re/im doubles): inverse NTT, CRT
+ * compose over every limb (src/rns_base.cu:169-253), FP64 special FFT, bit for bit the
+ * reference's. */
+int fhe_ckks_decode(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *pt, size_t chain_index, double scale,
+                    double *values, void *stream);
 
 /* PhantomSecretKey::decrypt, CKKS (src/secretkey.cu:693-720): pt = c0 + c1 * s (NTT form). */
 int fhe_ckks_decrypt(const fhe_context *ctx, const uint64_t *ct, const uint64_t *s_ntt, uint64_t *pt,

@@ -609,6 +609,25 @@ void orc_divide_round_q_last(const orc_ctx *c, int l, int size, const uint64_t *
     }
 }
 
+/* acc[p][k] += a[p][k] * b[k] mod q_k over `polys` polynomials of l limbs: the reference's
+ * multiply_plain (multiply_rns_poly, src/polymath.cu) followed by add_inplace (add_rns_poly,
+ * src/polymath.cu:41-55), as the matrix-vector inner sums use them
+ * (python/src/binding.cu:545-566). */
+void orc_mul_add(const orc_ctx *c, int l, int polys, const uint64_t *a, const uint64_t *b, uint64_t *acc) {
+    const int n = c->n;
+#pragma omp parallel for schedule(static) num_threads(OMP_THREADS)
+    for (int pk = 0; pk < polys * l; pk++) {
+        const int k = pk % l;
+        const uint64_t q = c->mod[k];
+        const uint64_t *ap = a + (size_t)pk * n, *bp = b + (size_t)k * n;
+        uint64_t *cp = acc + (size_t)pk * n;
+        for (int i = 0; i < n; i++) {
+            uint64_t t = orc_mulmod(ap[i], bp[i], q) + cp[i];
+            cp[i] = t >= q ? t - q : t;
+        }
+    }
+}
+
 /* ------------------------------------------------------------------ Galois */
 
 uint32_t orc_elt_from_step(int step, uint64_t n) {

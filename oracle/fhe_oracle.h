@@ -93,6 +93,8 @@ void orc_ckks_mul_relin(const orc_ctx *ctx, int l, const uint64_t *a, const uint
 void orc_rescale(const orc_ctx *ctx, int l, int size, const uint64_t *in, uint64_t *out);
 /* divide_and_round_q_last (src/rns.cu:1082-1126), BFV coefficient domain. */
 void orc_divide_round_q_last(const orc_ctx *ctx, int l, int size, const uint64_t *in, uint64_t *out);
+/* acc[p][k] = (acc[p][k] + a[p][k] * b[k]) mod q_k, p < polys, k < l (canonical inputs) */
+void orc_mul_add(const orc_ctx *ctx, int l, int polys, const uint64_t *a, const uint64_t *b, uint64_t *acc);
 /* Galois tables (include/galois.cuh:16-49, 98-113). */
 uint32_t orc_elt_from_step(int step, uint64_t n);
 void orc_galois_perm(int log_n, uint32_t elt, uint32_t *perm);

@@ -63,6 +63,7 @@ def lib():
         L.orc_ckks_mul_relin.argtypes = [ctypes.c_void_p, ctypes.c_int, _u64p, _u64p, _u64p, _u64p]
         L.orc_rescale.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _u64p, _u64p]
         L.orc_divide_round_q_last.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _u64p, _u64p]
+        L.orc_mul_add.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _u64p, _u64p, _u64p]
         L.orc_elt_from_step.restype = ctypes.c_uint32
         L.orc_elt_from_step.argtypes = [ctypes.c_int, ctypes.c_uint64]
         L.orc_galois_perm.argtypes = [ctypes.c_int, ctypes.c_uint32, _u32p]
@@ -239,6 +240,14 @@ class Context:
         out = np.zeros((size, l - 1, self.n), dtype=np.uint64)
         lib().orc_divide_round_q_last(self._h, l, size, p64(np.ascontiguousarray(ct)), p64(out))
         return out
+
+    def mul_add(self, l, acc, a, b):
+        """acc (polys x l x N) += a (polys x l x N) * b (l x N) mod q, in place."""
+        assert acc.flags["C_CONTIGUOUS"] and acc.dtype == np.uint64
+        polys = acc.size // (l * self.n)
+        lib().orc_mul_add(self._h, l, polys, p64(np.ascontiguousarray(a, dtype=np.uint64)),
+                          p64(np.ascontiguousarray(b, dtype=np.uint64)), p64(acc))
+        return acc
 
     def apply_galois_ntt(self, src, elt):
         src = np.ascontiguousarray(src, dtype=np.uint64)

@@ -431,70 +431,26 @@ private:
     PhantomDeviceBuffer data_;
 };
 
-namespace phantom::detail {
-// In-place radix-2 complex FFT of a power-of-two length: a_k <- sum_j a_j exp(sign * 2 pi i j k / len)
-// (iterative Cooley-Tukey, bit-reversal permutation first).
-inline void fft(std::vector<std::complex<double>> &a, int sign) {
-    const std::size_t len = a.size();
-    for (std::size_t i = 1, j = 0; i < len; i++) {
-        std::size_t bit = len >> 1;
-        for (; j & bit; bit >>= 1) j ^= bit;
-        j ^= bit;
-        if (i < j) std::swap(a[i], a[j]);
-    }
-    const double pi = std::acos(-1.0);
-    for (std::size_t h = 1; h < len; h <<= 1) {
-        for (std::size_t k = 0; k < h; k++) {
-            const std::complex<double> w = std::polar(1.0, sign * pi * (double)k / (double)h);
-            for (std::size_t s = 0; s < len; s += 2 * h) {
-                const std::complex<double> u = a[s + k], v = a[s + k + h] * w;
-                a[s + k] = u + v;
-                a[s + k + h] = u - v;
-            }
-        }
-    }
-}
-}  // namespace phantom::detail
-
 // CKKS canonical embedding (PhantomCKKSEncoder, include/ckks.h:88-150): slot i of a plaintext
-// holds m(zeta^(5^i mod 2N)) / scale, zeta = exp(i pi / N), i < N / 2.  The embedding runs in FP64
-// on the host (one length-2N FFT); residues and the NTT run on the GPU.  decode reads the
-// plaintext's first limb, so the message must stay below q_0 / 2 in magnitude.
+// holds m(zeta^(5^i mod 2N)) / scale, zeta = exp(i pi / N), i < N / 2.  encode and decode run on the
+// GPU (fhe_ckks_encode / fhe_ckks_decode): the reference's FP64 special FFT, rounding and residues,
+// and a CRT compose over every limb on decode, so the words and slots equal the reference's.
 class PhantomCKKSEncoder {
 public:
-    explicit PhantomCKKSEncoder(const PhantomContext &context) : n_(context.poly_modulus_degree()) {
-        group_.resize(n_ / 2);
-        std::uint64_t pos = 1;
-        for (std::size_t i = 0; i < n_ / 2; i++) {
-            group_[i] = pos;
-            pos = (pos * 5) % (2 * n_);
-        }
-    }
+    explicit PhantomCKKSEncoder(const PhantomContext &context) : n_(context.poly_modulus_degree()) {}
     [[nodiscard]] std::size_t slot_count() const noexcept { return n_ / 2; }
 
     void encode(const PhantomContext &context, const std::vector<std::complex<double>> &values, double scale,
                 PhantomPlaintext &destination, std::size_t chain_index = 1) const {
-        if (values.empty() || values.size() > n_ / 2) throw std::invalid_argument("need 1..N/2 slot values");
-        if (scale <= 0) throw std::invalid_argument("scale out of bounds");
-        std::vector<std::complex<double>> w(2 * n_);
-        for (std::size_t i = 0; i < values.size(); i++) w[group_[i]] = values[i];
-        phantom::detail::fft(w, -1);  // sum_i z_i zeta^(-g_i k)
+        if (values.empty()) throw std::invalid_argument("Input vector is empty");
+        if (values.size() > n_ / 2) throw std::invalid_argument("Input vector exceeds max slots");
         destination.resize(context, chain_index);
-        const std::size_t limbs = destination.coeff_modulus_size();
-        std::vector<std::uint64_t> res(limbs * n_);
-        for (std::size_t k = 0; k < n_; k++) {
-            const double c = std::nearbyint(w[k].real() * (2.0 * scale / (double)n_));
-            if (!(std::fabs(c) < 4.6e18)) throw std::invalid_argument("encoded values are too large");
-            const auto v = static_cast<std::int64_t>(c);
-            for (std::size_t j = 0; j < limbs; j++) {
-                const auto q = static_cast<std::int64_t>(context.modulus(j));
-                std::int64_t r = v % q;
-                res[j * n_ + k] = static_cast<std::uint64_t>(r < 0 ? r + q : r);
-            }
-        }
-        phantom::detail::cuda_check(cudaMemcpyAsync(destination.data(), res.data(), res.size() * 8,
+        PhantomDeviceBuffer dv(2 * values.size());  // interleaved re, im doubles (8-byte words)
+        phantom::detail::cuda_check(cudaMemcpyAsync(dv.get(), values.data(), values.size() * 16,
                                                     cudaMemcpyHostToDevice, cudaStreamPerThread));
-        phantom::detail::check(fhe_ntt_forward(context.handle(), destination.data(), 1, limbs, 0, cudaStreamPerThread));
+        phantom::detail::check(fhe_ckks_encode(context.handle(), context.workspace(),
+                                               reinterpret_cast<const double *>(dv.get()), values.size(), scale,
+                                               chain_index, destination.data(), cudaStreamPerThread));
         phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
         destination.set_scale(scale);
     }
@@ -513,22 +469,14 @@ public:
 
     void decode(const PhantomContext &context, const PhantomPlaintext &plain,
                 std::vector<std::complex<double>> &destination) const {
-        const std::size_t limbs = plain.coeff_modulus_size();
-        PhantomDeviceBuffer t(limbs * n_);
-        phantom::detail::cuda_check(cudaMemcpyAsync(t.get(), plain.data(), limbs * n_ * 8, cudaMemcpyDeviceToDevice,
-                                                    cudaStreamPerThread));
-        phantom::detail::check(fhe_ntt_inverse(context.handle(), t.get(), 1, limbs, 0, cudaStreamPerThread));
-        std::vector<std::uint64_t> limb0(n_);
-        phantom::detail::cuda_check(
-                cudaMemcpyAsync(limb0.data(), t.get(), n_ * 8, cudaMemcpyDeviceToHost, cudaStreamPerThread));
-        phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
-        const std::uint64_t q = context.modulus(0);
-        std::vector<std::complex<double>> c(2 * n_);
-        for (std::size_t k = 0; k < n_; k++)
-            c[k] = limb0[k] > q / 2 ? -(double)(q - limb0[k]) : (double)limb0[k];
-        phantom::detail::fft(c, +1);  // v_j = sum_k c_k zeta^(j k)
+        PhantomDeviceBuffer out(n_);  // N/2 complex doubles
+        phantom::detail::check(fhe_ckks_decode(context.handle(), context.workspace(), plain.data(),
+                                               plain.chain_index(), plain.scale(),
+                                               reinterpret_cast<double *>(out.get()), cudaStreamPerThread));
         destination.resize(n_ / 2);
-        for (std::size_t i = 0; i < n_ / 2; i++) destination[i] = c[group_[i]] / plain.scale();
+        phantom::detail::cuda_check(cudaMemcpyAsync(destination.data(), out.get(), n_ * 8, cudaMemcpyDeviceToHost,
+                                                    cudaStreamPerThread));
+        phantom::detail::cuda_check(cudaStreamSynchronize(cudaStreamPerThread));
     }
     void decode(const PhantomContext &context, const PhantomPlaintext &plain, std::vector<double> &destination) const {
         std::vector<std::complex<double>> z;
@@ -545,7 +493,6 @@ public:
 
 private:
     std::size_t n_;
-    std::vector<std::uint64_t> group_;  // 5^i mod 2N
 };
 
 // Secret key (PhantomSecretKey, include/secretkey.h:276-330) for CKKS: uniform ternary s, the

@@ -198,6 +198,18 @@ int fhe_context_set_launch_overlap(fhe_context *ctx, int enable) {
     }, false);
 }
 
+int fhe_context_fused_keyswitch(const fhe_context *ctx) {
+    if (!ctx || !ctx->c) return 0;
+    return ctx->c->ks_fused ? 1 : 0;
+}
+
+int fhe_context_set_fused_keyswitch(fhe_context *ctx, int enable) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        c.ks_fused = enable != 0;
+    }, false);
+}
+
 int fhe_context_autotune(fhe_context *ctx, int *chosen_l1, float *best_us) {
     return guarded([&] {
         pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
@@ -206,52 +218,89 @@ int fhe_context_autotune(fhe_context *ctx, int *chosen_l1, float *best_us) {
         const size_t poly_bytes = (size_t)limbs * c.n * 8;
         const int polys = (int)std::min<size_t>(64, std::max<size_t>(1, ((size_t)256 << 20) / poly_bytes + 1));
         const size_t words = (size_t)polys * limbs * c.n;
-        uint64_t *buf = nullptr;
-        if (cudaMalloc(&buf, words * 8) != cudaSuccess) throw std::runtime_error("autotune scratch allocation failed");
-        cudaMemset(buf, 0, words * 8);
-        cudaStream_t s;
-        cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-        cudaEvent_t e0, e1;
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
+        struct Guard {  // scratch, stream and events released on every exit path
+            uint64_t *buf = nullptr;
+            cudaStream_t s = nullptr;
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            ~Guard() {
+                if (s) cudaStreamSynchronize(s);
+                if (buf) cudaFree(buf);
+                if (e0) cudaEventDestroy(e0);
+                if (e1) cudaEventDestroy(e1);
+                if (s) cudaStreamDestroy(s);
+            }
+        } g;
+        auto ck = [](cudaError_t e, const char *what) {
+            if (e != cudaSuccess) throw std::runtime_error(std::string("autotune: ") + what + ": " + cudaGetErrorString(e));
+        };
+        ck(cudaMalloc(&g.buf, words * 8), "cudaMalloc");
+        ck(cudaStreamCreateWithFlags(&g.s, cudaStreamNonBlocking), "cudaStreamCreateWithFlags");
+        ck(cudaEventCreate(&g.e0), "cudaEventCreate");
+        ck(cudaEventCreate(&g.e1), "cudaEventCreate");
+        ck(cudaMemsetAsync(g.buf, 0, words * 8, g.s), "cudaMemsetAsync");
         const int keep = c.l1_sel;
         int best = 0;
         float best_t = 0.f;
-        for (int l1 = 6; l1 <= 8; l1++) {
-            if (!c.split_ok(l1)) continue;
-            c.l1_sel = l1;
-            for (int i = 0; i < 2; i++) {
-                pfg::ntt_forward(c, buf, polys, limbs, 0, s);
-                pfg::ntt_inverse(c, buf, polys, limbs, 0, s);
-            }
-            const int reps = 3;
-            float us = 0.f;
-            for (int trial = 0; trial < 3; trial++) {  // best of three
-                cudaEventRecord(e0, s);
-                for (int i = 0; i < reps; i++) {
-                    pfg::ntt_forward(c, buf, polys, limbs, 0, s);
-                    pfg::ntt_inverse(c, buf, polys, limbs, 0, s);
+        try {
+            for (int l1 = 6; l1 <= 8; l1++) {
+                if (!c.split_ok(l1)) continue;
+                c.l1_sel = l1;
+                for (int i = 0; i < 2; i++) {
+                    pfg::ntt_forward(c, g.buf, polys, limbs, 0, g.s);
+                    pfg::ntt_inverse(c, g.buf, polys, limbs, 0, g.s);
                 }
-                cudaEventRecord(e1, s);
-                cudaEventSynchronize(e1);
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                const float t = 1000.f * ms / reps;
-                if (trial == 0 || t < us) us = t;
+                const int reps = 3;
+                float us = 0.f;
+                for (int trial = 0; trial < 3; trial++) {  // best of three
+                    ck(cudaEventRecord(g.e0, g.s), "cudaEventRecord");
+                    for (int i = 0; i < reps; i++) {
+                        pfg::ntt_forward(c, g.buf, polys, limbs, 0, g.s);
+                        pfg::ntt_inverse(c, g.buf, polys, limbs, 0, g.s);
+                    }
+                    ck(cudaEventRecord(g.e1, g.s), "cudaEventRecord");
+                    ck(cudaGetLastError(), "timed launches");
+                    ck(cudaEventSynchronize(g.e1), "cudaEventSynchronize");
+                    float ms = 0.f;
+                    ck(cudaEventElapsedTime(&ms, g.e0, g.e1), "cudaEventElapsedTime");
+                    const float t = 1000.f * ms / reps;
+                    if (trial == 0 || t < us) us = t;
+                }
+                if (!best || us < best_t) {
+                    best = l1;
+                    best_t = us;
+                }
             }
-            if (!best || us < best_t) {
-                best = l1;
-                best_t = us;
-            }
+        } catch (...) {
+            c.l1_sel = keep;
+            throw;
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        cudaStreamDestroy(s);
-        cudaFree(buf);
         c.l1_sel = best ? best : keep;
         if (chosen_l1) *chosen_l1 = c.l1();
         if (best_us) *best_us = best_t;
     });
+}
+
+int fhe_context_autotune_op(fhe_context *ctx, fhe_workspace *ws, const char *cache_path, fhe_tuning *out) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        pfg::Workspace w = ws_of(ctx, ws);
+        const fhe_tuning t = pfg::autotune_op(c, w, cache_path);
+        if (out) *out = t;
+    });
+}
+
+int fhe_context_tuning(const fhe_context *ctx, fhe_tuning *out) {
+    return guarded([&] {
+        need_ptr(out, "out");
+        *out = pfg::tuning_of(ctx_of(ctx));
+    }, false);
+}
+
+int fhe_context_set_tuning(fhe_context *ctx, const fhe_tuning *t) {
+    return guarded([&] {
+        need_ptr(t, "tuning");
+        pfg::apply_tuning(*const_cast<pfg::Context *>(&ctx_of(ctx)), *t);
+    }, false);
 }
 
 int fhe_context_moduli(const fhe_context *ctx, uint64_t *out) {
@@ -615,6 +664,30 @@ int fhe_ckks_encrypt_symmetric(const fhe_context *ctx, const uint64_t *pt, const
         need_ptr(e, "e");
         need_ptr(out, "out");
         pfg::ckks_encrypt_sk(c, pt, s_ntt, a, e, out, level_of(c, chain_index), st(stream));
+    });
+}
+
+int fhe_ckks_encode(const fhe_context *ctx, fhe_workspace *ws, const double *values, size_t count, double scale,
+                    size_t chain_index, uint64_t *pt, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("unsupported scheme");
+        pfg::Workspace w = ws_of(ctx, ws);
+        need_ptr(values, "values");
+        need_ptr(pt, "pt");
+        pfg::ckks_encode(c, w, values, count, scale, level_of(c, chain_index), pt, st(stream));
+    });
+}
+
+int fhe_ckks_decode(const fhe_context *ctx, fhe_workspace *ws, const uint64_t *pt, size_t chain_index, double scale,
+                    double *values, void *stream) {
+    return guarded([&] {
+        const pfg::Context &c = ctx_of(ctx);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("unsupported scheme");
+        pfg::Workspace w = ws_of(ctx, ws);
+        need_ptr(pt, "pt");
+        need_ptr(values, "values");
+        pfg::ckks_decode(c, w, pt, scale, level_of(c, chain_index), values, st(stream));
     });
 }
 

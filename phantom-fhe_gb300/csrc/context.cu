@@ -481,6 +481,7 @@ std::unique_ptr<Context> make_context(int scheme, int mul_tech, uint64_t n, cons
     // permutation tables for every Galois element, built up front so that no evaluator call
     // allocates or copies host data (include/galois.cuh:98-113)
     for (uint32_t elt : c->galois_elts) c->perm_table(elt);
+    if (scheme == kSchemeCKKS) build_codec_tables(*c);
     return c;
 }
 

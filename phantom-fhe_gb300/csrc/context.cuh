@@ -76,6 +76,15 @@ struct LevelTables {
     bool tc_moddown_ok = false, tc_rescale_ok = false;
 };
 
+// CKKS encoder: CRT-compose constants of base Q_l (one data level), little-endian words
+struct ComposeTables {
+    DevBuf q_prod;     // [l] Q_l
+    DevBuf q_hat;      // [l][l] Q_l / q_i
+    DevBuf q_hat_inv;  // [l][2] (Q_l / q_i)^-1 mod q_i (value, Shoup)
+    DevBuf upper;      // [l] (Q_l + 1) / 2
+    int bits = 0;      // significant bits of Q_l
+};
+
 struct Context {
     int scheme = kSchemeCKKS, mul_tech = kMulHPS;
     int log_n = 0;
@@ -113,6 +122,10 @@ struct Context {
     DevBuf dec_mod_t, dec_mod_t_b;    // [nQ levels][nQ][2]
     DevBuf dec_frac, dec_frac_b;      // [nQ levels][nQ] doubles
     int q_msb = 0, t_msb = 0;
+    // CKKS encoder (ckks_codec.cu): the 2N-th roots of unity as complex doubles [2N], the rotation
+    // group 5^i mod 2N [N/4] (u32) and, per data level l (index l), the compose constants
+    DevBuf codec_roots, codec_group;
+    std::vector<std::unique_ptr<ComposeTables>> compose;
     // Galois
     std::vector<uint32_t> galois_elts;
     std::map<uint32_t, std::unique_ptr<DevBuf>> perms;
@@ -138,6 +151,8 @@ struct Context {
     // kernel chains launched with programmatic dependent launch (pdl.cuh); any setting gives the
     // same words
     bool pdl = true;
+    // mod-up row pass fused with the inner product (ks_fused.cuh); any setting gives the same words
+    bool ks_fused = true;
     // device the context's tables live on, and the device address of the fixed scratch array of
     // fhe_rescale_to_next_noalloc on it (looked up at creation, with that device current, so the
     // address belongs to the CUDA context the tables were made in)
@@ -160,6 +175,9 @@ struct Context {
     int qlp_table(int l, int jj) const { return jj < l ? jj : nQ + (jj - l); }
     const uint32_t *perm_table(uint32_t elt);  // builds and caches on first use
 };
+
+// Builds the CKKS encoder's tables (ckks_codec.cu).
+void build_codec_tables(Context &c);
 
 // Device address and size (words) of the no-allocation scratch array on the current device
 // (noalloc.cu); throws std::runtime_error when the lookup fails.

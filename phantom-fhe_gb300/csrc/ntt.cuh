@@ -76,7 +76,11 @@ __device__ __forceinline__ int grp_elem(int u, int gg, int j) {
 // a + b and a - b + 4q.  Twiddle for local stage s of vector `row`:
 // tw[(1 << (loff + s)) + (row << s) + (element >> (LM - s))].  All of a group's twiddle pairs
 // are fetched before its butterflies so their latency overlaps.
-template <int LM, int K, int SA, int E>
+//
+// SMALLQ (q < kFwdSmallQ): the csub is dropped, so each stage widens the range by 4q; after all
+// stages of a transform of up to 2^17 coefficients the values stay below (8 + 4 * 17) q < 2^64,
+// and the last pass reduces them with one truncated Barrett quotient (fwd_canonical).
+template <int LM, int K, int SA, int E, bool SMALLQ>
 __device__ __forceinline__ void fwd_regs(uint64_t (&x)[E], int u, const TwPair *tw, int loff, uint32_t row,
                                          uint64_t q) {
     constexpr int M = 1 << LM, TPV = M / E, G = E >> K, GS = 1 << K, TMIN = M >> (SA + K);
@@ -98,7 +102,7 @@ __device__ __forceinline__ void fwd_regs(uint64_t (&x)[E], int u, const TwPair *
             for (int j = 0; j < GS; j++) {
                 if (j & h) continue;
                 const TwPair t = w[(1 << k) - 1 + (j >> (K - k))];
-                const uint64_t a = csub(y[j], q4);
+                const uint64_t a = SMALLQ ? y[j] : csub(y[j], q4);
                 const uint64_t b = mul_shoup_lazy4n(y[j + h], t.w, t.ws, nq);
                 y[j] = a + b;
                 y[j + h] = a - b + q4;
@@ -111,9 +115,14 @@ __device__ __forceinline__ void fwd_regs(uint64_t (&x)[E], int u, const TwPair *
 // reduced by csub(., 4q), difference (a - b + 4q) * w in [0, 4q) (mul_shoup_lazy4).  The global
 // stage-0 butterfly (loff == 0, local stage 0) scales its sum by n^-1 instead; its difference
 // twiddle already carries n^-1 (src/host/ntt.cu:53-55).
-template <int LM, int K, int SA, int E>
+//
+// SMALLQ (q < kInvSmallQ): the sum's csub is dropped.  After d inverse stages every value lies
+// below B_d = 4q 2^d (a sum doubles the bound, a product resets it to 4q), so the difference
+// is taken as a - b + B_d; dep0 is the number of stages the transform's earlier pass ran.  With
+// at most 17 stages, 2 B_17 = q 2^20 < 2^64, and the last stage's outputs are products again.
+template <int LM, int K, int SA, int E, bool SMALLQ>
 __device__ __forceinline__ void inv_regs(uint64_t (&x)[E], int u, const TwPair *itw, int loff, uint32_t row,
-                                         uint64_t q, uint64_t ninv, uint64_t ninv_s) {
+                                         uint64_t q, uint64_t ninv, uint64_t ninv_s, int dep0) {
     constexpr int M = 1 << LM, TPV = M / E, G = E >> K, GS = 1 << K, TMIN = M >> (SA + K);
     const uint64_t q4 = 4 * q, nq = 0 - q;
 #pragma unroll
@@ -130,14 +139,15 @@ __device__ __forceinline__ void inv_regs(uint64_t (&x)[E], int u, const TwPair *
         for (int k = K - 1; k >= 0; k--) {
             const int h = GS >> (k + 1);
             const bool first_stage = (SA + k == 0) && (loff == 0);
+            const uint64_t bnd = SMALLQ ? q4 << (dep0 + (LM - 1 - (SA + k))) : q4;
 #pragma unroll
             for (int j = 0; j < GS; j++) {
                 if (j & h) continue;
                 const TwPair t = w[(1 << k) - 1 + (j >> (K - k))];
                 const uint64_t a = y[j], b = y[j + h];
                 const uint64_t s = a + b;
-                y[j] = first_stage ? mul_shoup_lazy4n(s, ninv, ninv_s, nq) : csub(s, q4);
-                y[j + h] = mul_shoup_lazy4n(a - b + q4, t.w, t.ws, nq);
+                y[j] = first_stage ? mul_shoup_lazy4n(s, ninv, ninv_s, nq) : (SMALLQ ? s : csub(s, q4));
+                y[j + h] = mul_shoup_lazy4n(a - b + bnd, t.w, t.ws, nq);
             }
         }
     }
@@ -172,21 +182,47 @@ struct PhaseAt {
 
 // Runs processing steps PI..NPH-1 on the registers; between steps the vector goes through
 // shared memory (group_store, barrier, group_load of the next step's groups).
-template <int LM, bool FWD, int PI, int E>
+template <int LM, bool FWD, int PI, int E, bool SMALLQ>
 __device__ __forceinline__ void run_phases(uint64_t (&x)[E], uint64_t *vec, int u, const TwPair *tw, int loff,
-                                           uint32_t row, uint64_t q, uint64_t ninv, uint64_t ninv_s) {
+                                           uint32_t row, uint64_t q, uint64_t ninv, uint64_t ninv_s, int dep0) {
     using P = PhaseAt<LM, FWD, PI, E>;
     if constexpr (FWD)
-        fwd_regs<LM, P::K, P::SA, E>(x, u, tw, loff, row, q);
+        fwd_regs<LM, P::K, P::SA, E, SMALLQ>(x, u, tw, loff, row, q);
     else
-        inv_regs<LM, P::K, P::SA, E>(x, u, tw, loff, row, q, ninv, ninv_s);
+        inv_regs<LM, P::K, P::SA, E, SMALLQ>(x, u, tw, loff, row, q, ninv, ninv_s, dep0);
     if constexpr (PI + 1 < P::NPH) {
         using Q = PhaseAt<LM, FWD, PI + 1, E>;
         grp_store<LM, P::K, P::SA, E>(x, vec, u);
         __syncthreads();
         grp_load<LM, Q::K, Q::SA, E>(x, vec, u);
-        run_phases<LM, FWD, PI + 1, E>(x, vec, u, tw, loff, row, q, ninv, ninv_s);
+        run_phases<LM, FWD, PI + 1, E, SMALLQ>(x, vec, u, tw, loff, row, q, ninv, ninv_s, dep0);
     }
+}
+
+// Prime classes of the lazy butterflies (uniform per CTA: one limb per block): below these
+// bounds the forward / inverse butterflies skip their conditional subtractions (fwd_regs,
+// inv_regs).  Forward: (8 + 4 * 17) q < 2^64; inverse: 2 * 4q * 2^17 < 2^64.
+constexpr uint64_t kFwdSmallQ = uint64_t(1) << 57;
+constexpr uint64_t kInvSmallQ = uint64_t(1) << 44;
+
+template <int LM, bool FWD, int E>
+__device__ __forceinline__ void run_pass(uint64_t (&x)[E], uint64_t *vec, int u, const TwPair *tw, int loff,
+                                         uint32_t row, uint64_t q, uint64_t ninv, uint64_t ninv_s, int dep0) {
+    if (q < (FWD ? kFwdSmallQ : kInvSmallQ))
+        run_phases<LM, FWD, 0, E, true>(x, vec, u, tw, loff, row, q, ninv, ninv_s, dep0);
+    else
+        run_phases<LM, FWD, 0, E, false>(x, vec, u, tw, loff, row, q, ninv, ninv_s, dep0);
+}
+
+// Canonical residue of a forward transform's output: [0, 8q) for the large class, below
+// (8 + 4 log N) q for the small one (any value below 2^64: the truncated Barrett quotient by
+// floor(2^64 / q) is short by at most 3, so x - t q lies in [0, 4q)).
+__device__ __forceinline__ uint64_t fwd_canonical(uint64_t y, const Mod &m) {
+    if (m.q < kFwdSmallQ) {
+        y -= mulhi_trunc(y, m.mu_hi) * m.q;
+        return csub(csub(y, 2 * m.q), m.q);
+    }
+    return csub(csub(csub(y, 4 * m.q), 2 * m.q), m.q);
 }
 
 struct NttTables {
@@ -239,16 +275,21 @@ __global__ void __launch_bounds__(NttShape<E, TILE>::kThreads, NttShape<E, TILE>
         ni = T.ninv[2 * tbl];
         nis = T.ninv[2 * tbl + 1];
     }
-    run_phases<LM, FWD, 0, E>(x, sm + v * VP, u, (FWD ? T.tw : T.itw) + ((size_t)tbl << T.log_n), 0, 0u, q, ni,
-                              nis);
+    // the inverse column pass runs after the row pass's l2 stages
+    run_pass<LM, FWD, E>(x, sm + v * VP, u, (FWD ? T.tw : T.itw) + ((size_t)tbl << T.log_n), 0, 0u, q, ni, nis,
+                         FWD ? 0 : T.l2);
+    Mod md{};
+    if constexpr (FWD && LAST) md = T.mods[tbl];
 #pragma unroll
     for (int gg = 0; gg < (E >> L::K); gg++)
 #pragma unroll
         for (int j = 0; j < (1 << L::K); j++) {
             uint64_t y = x[gg * (1 << L::K) + j];
             if (LAST) {
-                if (FWD) y = csub(y, 4 * q);
-                y = csub(csub(y, 2 * q), q);
+                if (FWD)
+                    y = fwd_canonical(y, md);
+                else
+                    y = csub(csub(y, 2 * q), q);
             }
             st(poly, k, tbl, (uint32_t)grp_elem<LM, L::K, L::SA, E>(u, gg, j) * n2 + col, y);
         }
@@ -295,14 +336,16 @@ __global__ void __launch_bounds__(NttShape<E, TILE>::kThreads, NttShape<E, TILE>
         ni = T.ninv[2 * tbl];
         nis = T.ninv[2 * tbl + 1];
     }
-    run_phases<LM, FWD, 0, E>(x, vec, u, (FWD ? T.tw : T.itw) + ((size_t)tbl << T.log_n), T.l1, row, q, ni, nis);
+    run_pass<LM, FWD, E>(x, vec, u, (FWD ? T.tw : T.itw) + ((size_t)tbl << T.log_n), T.l1, row, q, ni, nis, 0);
     if constexpr (FWD) {
         grp_store<LM, L::K, L::SA, E>(x, vec, u);
+        Mod md{};
+        if constexpr (LAST) md = T.mods[tbl];
         __syncthreads();
 #pragma unroll 4
         for (int i = threadIdx.x; i < V * M; i += NT) {
             uint64_t y = sm[(i / M) * VP + pad_idx(i % M)];
-            if (LAST) y = csub(csub(csub(y, 4 * q), 2 * q), q);
+            if (LAST) y = fwd_canonical(y, md);
             st(poly, k, tbl, base + i, y);
         }
     } else {

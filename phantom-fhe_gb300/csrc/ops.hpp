@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "context.cuh"
+#include "phantom_gb300.h"
 
 namespace pfg {
 
@@ -85,6 +86,20 @@ void sample_small(const Context &c, const uint8_t *seed, int kind, int64_t *out,
 void secret_key_from_seed(const Context &c, const uint8_t *seed, uint64_t *s_ntt, int64_t *scratch, cudaStream_t s);
 void kswitch_keygen_seeded(Context &c, uint32_t elt, const uint64_t *s_ntt, const uint8_t *seeds_a,
                            const uint8_t *seeds_e, uint64_t *key, uint64_t *scratch, cudaStream_t s);
+
+// Autotuner (autotune.cu): times the context's benchmark operation over its kernel shapes.
+using Tuning = fhe_tuning;
+Tuning autotune_op(Context &c, const Workspace &w, const char *cache_path);
+Tuning tuning_of(const Context &c);
+void apply_tuning(Context &c, const Tuning &t);
+
+// CKKS encoder (ckks_codec.cu): values are complex doubles (re, im) in device memory.
+size_t codec_encode_words(const Context &c);
+size_t codec_decode_words(const Context &c, int l);
+void ckks_encode(const Context &c, const Workspace &w, const double *values, size_t count, double scale, int l,
+                 uint64_t *pt, cudaStream_t s);
+void ckks_decode(const Context &c, const Workspace &w, const uint64_t *pt, double scale, int l, double *values,
+                 cudaStream_t s);
 
 // BFV plaintexts (bfv_io.cu).
 void bfv_encode(const Context &c, const uint64_t *values, size_t count, uint64_t *pt, cudaStream_t s);

@@ -26,6 +26,7 @@
 #include "bconv.cuh"
 #include "bconv_tc.cuh"
 #include "keyswitch.cuh"
+#include "ks_fused.cuh"
 #include "launch.cuh"
 #include "ntt_small.cuh"
 #include "ops.hpp"
@@ -168,8 +169,10 @@ void modup_bconv_tc_launch(const Context &c, const LevelTables &lt, uint64_t *tm
                            c.d_status.as<unsigned>(), s, c.pdl);
 }
 
+// y = iNTT(c2) * partQlHatInv; tm = bconv(y) for every digit's complement limbs, then the
+// forward NTT's column pass over them (lazy output in tm).
 template <class C2Load>
-static void modup_ckks(const Context &c, const KsBuffers &b, C2Load c2ld, int l, cudaStream_t s) {
+static void modup_to_column_pass(const Context &c, const KsBuffers &b, C2Load c2ld, int l, cudaStream_t s) {
     const LevelTables &lt = *c.levels[l];
     const int alpha = c.nP, qlp = l + alpha, beta = lt.beta;
     const long long yps = (long long)l << c.log_n;
@@ -187,7 +190,35 @@ static void modup_ckks(const Context &c, const KsBuffers &b, C2Load c2ld, int l,
         });
     }
     PtrStore ts{b.tm, tps, c.log_n};
-    ntt_fwd(c, beta * qlp, ModupMap{qlp, l, c.nQ, alpha, true}, PtrLoad{b.tm, tps, c.log_n}, ts, ts, s);
+    col_pass<true, false>(c, beta * qlp, ModupMap{qlp, l, c.nQ, alpha, true}, PtrLoad{b.tm, tps, c.log_n}, ts, s);
+}
+
+// Steps 1-2: the whole mod-up, T_d in NTT form in tm (hoisted rotations reuse it).
+template <class C2Load>
+static void modup_ckks(const Context &c, const KsBuffers &b, C2Load c2ld, int l, cudaStream_t s) {
+    const int alpha = c.nP, qlp = l + alpha, beta = c.levels[l]->beta;
+    const long long tps = (long long)qlp << c.log_n;
+    modup_to_column_pass(c, b, c2ld, l, s);
+    PtrStore ts{b.tm, tps, c.log_n};
+    row_pass<true, true>(c, beta * qlp, ModupMap{qlp, l, c.nQ, alpha, true}, PtrLoad{b.tm, tps, c.log_n}, ts, s);
+}
+
+// Steps 2 (row pass) and 3 fused: one kernel per (output limb, row tile) over every digit.
+template <class Own>
+static void modup_row_inner_product(const Context &c, const KsBuffers &b, Own own, int l, const uint64_t *const *evk,
+                                    cudaStream_t s) {
+    const int alpha = c.nP, qlp = l + alpha;
+    const dim3 grid((unsigned)(c.n / kFusedTile), (unsigned)qlp), block(kFusedTile / kFusedE);
+    const NttTables T = c.ntt();
+    const uint64_t *tm = b.tm;
+    count_launch();
+    switch (c.l2()) {
+        case 6: launch_pdl(c.pdl, ks_modup_ip<6, Own>, grid, block, 0, s, T, tm, own, evk, b.cx, l, c.nQ, alpha, c.beta(l), c.nQ + c.nP); break;
+        case 7: launch_pdl(c.pdl, ks_modup_ip<7, Own>, grid, block, 0, s, T, tm, own, evk, b.cx, l, c.nQ, alpha, c.beta(l), c.nQ + c.nP); break;
+        case 8: launch_pdl(c.pdl, ks_modup_ip<8, Own>, grid, block, 0, s, T, tm, own, evk, b.cx, l, c.nQ, alpha, c.beta(l), c.nQ + c.nP); break;
+        case 9: launch_pdl(c.pdl, ks_modup_ip<9, Own>, grid, block, 0, s, T, tm, own, evk, b.cx, l, c.nQ, alpha, c.beta(l), c.nQ + c.nP); break;
+        default: throw std::logic_error("unsupported NTT split");
+    }
 }
 
 // Step 3
@@ -199,6 +230,19 @@ static void inner_product(const Context &c, const KsBuffers &b, Own own, int l, 
     count_launch();
     launch_pdl(c.pdl, ks_inner_product<Own, false>, dim3(grid_for(work, 256)), dim3(256), 0, s, b.cx,
                (const uint64_t *)b.tm, own, evk, c.d_mods.as<Mod>(), c.log_n, l, c.nQ, c.nP, c.beta(l), c.nQ + c.nP);
+}
+
+// Steps 1-3: cx = <ModUp(c2), evk> (fused or as separate kernels; the same words).
+template <class C2Load, class Own>
+static void modup_inner_product(const Context &c, const KsBuffers &b, C2Load c2ld, Own own, int l,
+                                const uint64_t *const *evk, cudaStream_t s) {
+    if (c.ks_fused) {
+        modup_to_column_pass(c, b, c2ld, l, s);
+        modup_row_inner_product(c, b, own, l, evk, s);
+    } else {
+        modup_ckks(c, b, c2ld, l, s);
+        inner_product(c, b, own, l, evk, s);
+    }
 }
 
 // Step 4: P limbs of both cx polynomials back to coefficients, times PHatInv.
@@ -267,8 +311,7 @@ void ckks_keyswitch(const Context &c, const Workspace &w, uint64_t *ct, const ui
                     const uint64_t *const *evk, cudaStream_t s) {
     const KsBuffers b = ks_buffers(c, w);
     const long long lps = (long long)l << c.log_n;
-    modup_ckks(c, b, PtrLoad{c2, lps, c.log_n}, l, s);
-    inner_product(c, b, PlainOwn{c2, c.log_n}, l, evk, s);
+    modup_inner_product(c, b, PtrLoad{c2, lps, c.log_n}, PlainOwn{c2, c.log_n}, l, evk, s);
     moddown_intt_p(c, b, l, s);
     moddown_ntt(c, b, b.tm, l, ct, ct + lps, InplaceBase{ct, lps, c.log_n}, s);
 }
@@ -278,8 +321,8 @@ void ckks_mul_relin(const Context &c, const Workspace &w, uint64_t *ct1, const u
     const KsBuffers b = ks_buffers(c, w);
     const long long lps = (long long)l << c.log_n;
     const uint64_t *a1 = ct1 + lps, *b1 = ct2 + lps;
-    modup_ckks(c, b, TensorD2Load{a1, b1, c.d_mods.as<Mod>(), c.log_n}, l, s);
-    inner_product(c, b, TensorOwn{a1, b1, c.log_n}, l, rlk, s);
+    modup_inner_product(c, b, TensorD2Load{a1, b1, c.d_mods.as<Mod>(), c.log_n}, TensorOwn{a1, b1, c.log_n}, l, rlk,
+                        s);
     moddown_intt_p(c, b, l, s);
     // poly 0 goes to scratch first: poly 1's base still reads a0 at every position
     moddown_ntt(c, b, b.tm, l, b.g, ct1 + lps, TensorBase{ct1, ct2, lps, c.log_n}, s);
@@ -434,8 +477,7 @@ void ckks_mul_relin_rescale(const Context &c, const Workspace &w, const uint64_t
     const long long lps = (long long)l << c.log_n;
     const uint64_t *a1 = ct1 + lps, *b1 = ct2 + lps;
     const TensorBase tb{ct1, ct2, lps, c.log_n};
-    modup_ckks(c, b, TensorD2Load{a1, b1, mods, c.log_n}, l, s);
-    inner_product(c, b, TensorOwn{a1, b1, c.log_n}, l, rlk, s);
+    modup_inner_product(c, b, TensorD2Load{a1, b1, mods, c.log_n}, TensorOwn{a1, b1, c.log_n}, l, rlk, s);
     const int alpha = c.nP, qlp = l + alpha;
     const long long cps = (long long)qlp << c.log_n, ops = (long long)(l - 1) << c.log_n;
     uint64_t *zc = b.z, *zd = b.z + (2 << c.log_n);
@@ -482,8 +524,7 @@ void ckks_apply_galois(const Context &c, const Workspace &w, uint64_t *ct, int l
     count_launch();
     launch_pdl(c.pdl, galois_permute, dim3(grid_for(total, 256)), dim3(256), 0, s, b.g, ct, perm, c.log_n, total);
     const uint64_t *g1 = b.g + lps;
-    modup_ckks(c, b, PtrLoad{g1, lps, c.log_n}, l, s);
-    inner_product(c, b, PlainOwn{g1, c.log_n}, l, gk, s);
+    modup_inner_product(c, b, PtrLoad{g1, lps, c.log_n}, PlainOwn{g1, c.log_n}, l, gk, s);
     moddown_intt_p(c, b, l, s);
     moddown_ntt(c, b, b.tm, l, ct, ct + lps, FirstPolyBase{b.g, c.log_n}, s);
 }

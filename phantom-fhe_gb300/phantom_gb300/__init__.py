@@ -47,6 +47,23 @@ class _KsItem(ctypes.Structure):
     _fields_ = [("ct", _vp), ("c2", _vp), ("chain_index", _sz)]
 
 
+class Tuning(ctypes.Structure):
+    """fhe_tuning: the context's kernel shapes (every setting gives the same words)."""
+    _fields_ = [("ntt_split", ctypes.c_int), ("ntt_tile", ctypes.c_int), ("ntt_small_tile", ctypes.c_int),
+                ("ntt_small_launch", ctypes.c_int), ("fused_keyswitch", ctypes.c_int),
+                ("tensor_cores", ctypes.c_int), ("best_us", ctypes.c_float), ("evaluated", ctypes.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+    @classmethod
+    def from_dict(cls, d):
+        t = cls()
+        for f, _ in cls._fields_:
+            setattr(t, f, type(getattr(t, f))(d[f]))
+        return t
+
+
 def _load():
     if not os.path.exists(LIB_PATH):
         raise ImportError(f"{LIB_PATH} is not built; run __graft_entry__.build()")
@@ -64,6 +81,8 @@ def _load():
     L.fhe_context_set_ntt_split.argtypes = [_vp, ctypes.c_int]
     L.fhe_context_launch_overlap.argtypes = [_vp]
     L.fhe_context_set_launch_overlap.argtypes = [_vp, ctypes.c_int]
+    L.fhe_context_fused_keyswitch.argtypes = [_vp]
+    L.fhe_context_set_fused_keyswitch.argtypes = [_vp, ctypes.c_int]
     L.fhe_context_ntt_small_tile.argtypes = [_vp]
     L.fhe_context_set_ntt_small_tile.argtypes = [_vp, ctypes.c_int]
     L.fhe_context_ntt_tile.argtypes = [_vp]
@@ -71,6 +90,9 @@ def _load():
     L.fhe_context_ntt_small_launch.argtypes = [_vp]
     L.fhe_context_set_ntt_small_launch.argtypes = [_vp, ctypes.c_int]
     L.fhe_context_autotune.argtypes = [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)]
+    L.fhe_context_autotune_op.argtypes = [_vp, _vp, ctypes.c_char_p, _vp]
+    L.fhe_context_tuning.argtypes = [_vp, _vp]
+    L.fhe_context_set_tuning.argtypes = [_vp, _vp]
     L.fhe_context_sizes.argtypes = [_vp] + [ctypes.POINTER(_u64)] + [ctypes.POINTER(_sz)] * 4
     L.fhe_context_moduli.argtypes = [_vp, ctypes.POINTER(_u64)]
     L.fhe_context_galois_elts.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(_sz)]
@@ -104,6 +126,8 @@ def _load():
                                        ctypes.c_int, _vp]
     L.fhe_ckks_encrypt_symmetric.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]
     L.fhe_ckks_decrypt.argtypes = [_vp, _vp, _vp, _vp, _sz, _vp]
+    L.fhe_ckks_encode.argtypes = [_vp, _vp, _vp, _sz, ctypes.c_double, _sz, _vp, _vp]
+    L.fhe_ckks_decode.argtypes = [_vp, _vp, _vp, _sz, ctypes.c_double, _vp, _vp]
     L.fhe_kswitch_keygen.argtypes = [_vp, _vp, ctypes.c_uint32, _vp, _vp, _vp, _vp, _vp]
     L.fhe_bfv_encode.argtypes = [_vp, _vp, _sz, _vp, _vp]
     L.fhe_bfv_decode.argtypes = [_vp, _vp, _vp, _vp, _vp]
@@ -232,6 +256,15 @@ class Context:
         _check(lib.fhe_context_set_launch_overlap(self._h, int(bool(on))))
 
     @property
+    def fused_keyswitch(self):
+        """Mod-up row pass fused with the key-switching inner product (same words either way)."""
+        return bool(lib.fhe_context_fused_keyswitch(self._h))
+
+    @fused_keyswitch.setter
+    def fused_keyswitch(self, on):
+        _check(lib.fhe_context_set_fused_keyswitch(self._h, int(bool(on))))
+
+    @property
     def ntt_tile(self):
         """Coefficients per CTA (2048 or 4096) of the 16-per-thread NTT passes (same words)."""
         return int(lib.fhe_context_ntt_tile(self._h))
@@ -258,28 +291,34 @@ class Context:
     def ntt_small_launch(self, tiles):
         _check(lib.fhe_context_set_ntt_small_launch(self._h, int(tiles)))
 
-    def autotune(self, cache_path=None):
-        """Chooses the NTT stage split by timing every supported one (forward + inverse on
-        scratch limbs).  With cache_path, a JSON file keyed by GPU, degree and modulus count
-        stores the choice so later contexts skip the timing.  Returns {"ntt_split": l1, ...}."""
-        import json
-        import torch
-        key = f"{torch.cuda.get_device_name()}|N={self.n}|moduli={len(self.moduli)}"
-        cache = {}
-        if cache_path and os.path.exists(cache_path):
-            with open(cache_path) as f:
-                cache = json.load(f)
-        if key in cache:
-            self.ntt_split = cache[key]["ntt_split"]
-            return dict(cache[key], cached=True)
+    def autotune(self, ws=None, cache_path=None):
+        """Chooses the kernel shapes (NTT split and tiles, small-launch bound, fused key switch,
+        tensor-core conversions) by timing the context's benchmark operation at its top level
+        (CKKS HMult + relinearise + rescale, BFV multiply + relinearise), and applies them.  With
+        cache_path, a JSON-lines file keyed by GPU, scheme, N, |Q|, |P| and batch keeps the choice
+        so later contexts skip the timing.  Returns the chosen shapes as a dict."""
+        t = Tuning()
+        w = ws if ws is not None else self.workspace()
+        path = cache_path.encode() if cache_path else None
+        _check(lib.fhe_context_autotune_op(self._h, w._h, path, ctypes.byref(t)))
+        return t.as_dict()
+
+    def autotune_ntt_split(self):
+        """Times every supported NTT stage split on scratch limbs and keeps the fastest."""
         l1, us = ctypes.c_int(), ctypes.c_float()
         _check(lib.fhe_context_autotune(self._h, ctypes.byref(l1), ctypes.byref(us)))
-        result = {"ntt_split": int(l1.value), "roundtrip_us": float(us.value)}
-        if cache_path:
-            cache[key] = result
-            with open(cache_path, "w") as f:
-                json.dump(cache, f, indent=1, sort_keys=True)
-        return dict(result, cached=False)
+        return {"ntt_split": int(l1.value), "roundtrip_us": float(us.value)}
+
+    @property
+    def tuning(self):
+        t = Tuning()
+        _check(lib.fhe_context_tuning(self._h, ctypes.byref(t)))
+        return t.as_dict()
+
+    @tuning.setter
+    def tuning(self, d):
+        t = Tuning.from_dict(dict(self.tuning, **d))
+        _check(lib.fhe_context_set_tuning(self._h, ctypes.byref(t)))
 
     def device_status(self):
         """Reads and clears the device status word (0 = every bounded wait completed)."""
@@ -390,6 +429,18 @@ class Context:
 
     def decrypt(self, ct, s_ntt, pt, chain_index, stream=None):
         _check(lib.fhe_ckks_decrypt(self._h, _ptr(ct), _ptr(s_ntt), _ptr(pt), chain_index, _stream(stream)))
+
+    def ckks_encode(self, ws, values, scale, chain_index, pt, count=None, stream=None):
+        """values: device float64 tensor [count][2] (re, im) -> pt [l][N] (NTT form), the
+        reference's encoder word for word."""
+        n = values.numel() // 2 if count is None else count
+        _check(lib.fhe_ckks_encode(self._h, ws._h, _ptr(values), n, float(scale), chain_index, _ptr(pt),
+                                   _stream(stream)))
+
+    def ckks_decode(self, ws, pt, scale, chain_index, values, stream=None):
+        """pt [l][N] (NTT form) -> values: device float64 tensor [N/2][2] (re, im)."""
+        _check(lib.fhe_ckks_decode(self._h, ws._h, _ptr(pt), chain_index, float(scale), _ptr(values),
+                                   _stream(stream)))
 
     def kswitch_keygen(self, ws, galois_elt, s_ntt, a, e, key, stream=None):
         """galois_elt 0: relinearisation key (s^2); else the Galois key of that element."""

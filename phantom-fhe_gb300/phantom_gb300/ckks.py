@@ -1,13 +1,11 @@
-"""CKKS host side: canonical-embedding encoder/decoder (FP64) and secret-key material with
-seeded randomness.
+"""CKKS host side: the encoder front end (the FP64 canonical embedding runs on the GPU, bit for
+bit the reference's) and secret-key material with seeded randomness.
 
-Encoder (restates PhantomCKKSEncoder, src/ckks.cu:17-140 and its decode path): slot i of a
-plaintext holds m(zeta^(5^i mod 2N)) / scale, zeta = exp(i*pi/N), for i < N/2; the conjugate
-slots hold the conjugates, so m has real coefficients.  The reference evaluates the embedding
-with its own special FFT on the device; here it is one length-2N numpy FFT per direction in
-FP64, which gives the same rounded integer coefficients except where a coefficient lies within
-FP64 rounding of a half-integer, and the same decoded slots to FP64 accuracy.  Only the
-embedding runs on the host; residues, NTT and every ciphertext operation run on the device.
+Encoder (PhantomCKKSEncoder, src/ckks.cu:17-400): slot i of a plaintext holds
+m(zeta^(5^i mod 2N)) / scale, zeta = exp(i*pi/N), for i < N/2.  encode / decode call
+fhe_ckks_encode / fhe_ckks_decode: the reference's special FFT in FP64, its rounding and residues,
+and on decode the CRT compose over every limb of the plaintext, so any message below Q_l / 2
+round-trips and the words equal the reference encoder's.
 
 Keys (PhantomSecretKey, src/secretkey.cu:232-460): a uniform ternary secret, uniform `a`
 polynomials and errors from the reference's centred binomial distribution (difference of the
@@ -34,35 +32,21 @@ def rotation_group(n):
 
 
 class CkksEncoder:
+    """GPU encoder for one context degree; keeps one workspace per context it has served."""
+
     def __init__(self, n):
         self.n = n
         self.slots = n // 2
         self.group = rotation_group(n)
+        self._ws = {}
 
-    def encode_coeffs(self, values, scale):
-        """Complex slot values (<= N/2 of them, zero-padded) -> int64 coefficients of
-        round(scale * m)."""
-        n = self.n
-        z = np.zeros(self.slots, dtype=np.complex128)
-        v = np.asarray(values, dtype=np.complex128)
-        if v.size == 0 or v.size > self.slots:
-            raise ValueError("need 1..N/2 slot values")
-        z[: v.size] = v
-        # m_k = (1/N) sum_i (z_i zeta^(-g_i k) + conj(z_i) zeta^(g_i k)) = (2/N) Re(sum_i z_i zeta^(-g_i k))
-        w = np.zeros(2 * n, dtype=np.complex128)
-        w[self.group] = z
-        coeffs = np.fft.fft(w)[:n].real * (2.0 * scale / n)
-        if np.max(np.abs(coeffs)) >= 2.0 ** 62:
-            raise ValueError("encoded values are too large")
-        return np.rint(coeffs).astype(np.int64)
-
-    def decode_coeffs(self, coeffs, scale):
-        """Real coefficients (float or int) -> N/2 complex slots."""
-        n = self.n
-        c = np.zeros(2 * n, dtype=np.complex128)
-        c[:n] = np.asarray(coeffs, dtype=np.float64)
-        v = np.fft.ifft(c) * (2 * n)  # v_j = sum_k c_k zeta^(j k)
-        return v[self.group] / scale
+    def _workspace(self, ctx, ws):
+        if ws is not None:
+            return ws
+        w = self._ws.get(id(ctx))
+        if w is None or w[0] is not ctx:
+            w = self._ws[id(ctx)] = (ctx, ctx.workspace())
+        return w[1]
 
     @staticmethod
     def to_rns(coeffs, moduli):
@@ -70,28 +54,23 @@ class CkksEncoder:
         c = np.asarray(coeffs, dtype=np.int64)
         return np.stack([np.mod(c, np.int64(q)).astype(np.uint64) for q in moduli])
 
-    @staticmethod
-    def centered(residues, q):
-        """Residues of one limb -> centred integers (float64), valid when |m| < q / 2."""
-        r = np.asarray(residues, dtype=np.uint64)
-        half = np.uint64(q // 2)
-        return np.where(r > half, -(np.uint64(q) - r).astype(np.float64), r.astype(np.float64))
-
-    def encode(self, ctx, values, scale, chain_index):
-        """-> device plaintext [limbs][N] in NTT form at chain_index."""
+    def encode(self, ctx, values, scale, chain_index, ws=None):
+        """Complex slot values (1..N/2 of them) -> device plaintext [limbs][N] in NTT form."""
+        import torch
+        v = np.asarray(values, dtype=np.complex128).reshape(-1)
+        vt = torch.from_numpy(np.stack([v.real, v.imag], axis=1).copy()).cuda()
         l = ctx.level(chain_index)
-        pt = to_device(self.to_rns(self.encode_coeffs(values, scale), ctx.moduli[:l]))
-        ctx.ntt_forward(pt, 1, l)
+        pt = torch.empty((l, ctx.n), dtype=torch.int64, device="cuda")
+        ctx.ckks_encode(self._workspace(ctx, ws), vt, scale, chain_index, pt)
         return pt
 
-    def decode(self, ctx, pt, scale, chain_index):
-        """Device plaintext (NTT form) -> complex slots, reading limb 0 (q_0 is the largest
-        prime of the chain; the message must stay below q_0 / 2)."""
-        l = ctx.level(chain_index)
-        t = pt.clone()
-        ctx.ntt_inverse(t, 1, l)
-        limb0 = t[0].cpu().numpy().view(np.uint64)
-        return self.decode_coeffs(self.centered(limb0, ctx.moduli[0]), scale)
+    def decode(self, ctx, pt, scale, chain_index, ws=None):
+        """Device plaintext (NTT form) -> N/2 complex slots (numpy), composed over every limb."""
+        import torch
+        out = torch.empty((self.slots, 2), dtype=torch.float64, device="cuda")
+        ctx.ckks_decode(self._workspace(ctx, ws), pt, scale, chain_index, out)
+        o = out.cpu().numpy()
+        return o[:, 0] + 1j * o[:, 1]
 
 
 class SecretKey:

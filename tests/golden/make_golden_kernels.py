@@ -7,6 +7,8 @@ cubins in oracle/_ref/ are then portable to any host with the driver).  Usage:
 
     python tests/golden/make_golden_kernels.py OUT.json          # golden digests
     python tests/golden/make_golden_kernels.py --time OUT.json   # GB300 timings of the same kernels
+    python tests/golden/make_golden_kernels.py --time-batched OUT.json   # ... over the batched workloads
+    python tests/golden/make_golden_kernels.py --extra OUT.json  # only the cases of extra_cases()
 
 Every case replays the reference's host-side launch sequence (grid, block, dynamic shared
 memory, argument order) for one operation, citing the host function it follows, on seeded
@@ -17,6 +19,7 @@ compare digests.
 """
 import hashlib
 import json
+import math
 import os
 import sys
 
@@ -99,6 +102,7 @@ class Kernels:
         self.add_to_ct = k("rns_bconv", "add_to_ct_kernel")
         self.ip = k("eval_key_switch", "key_switch_inner_prod_c2_and_evk")
         self.dr_reduce = k("rns", "divide_and_round_reduce_q_last_kernel")
+        self.dr_q_last = k("rns", "divide_and_round_q_last_kernel")
         self.dr_scalar = k("rns", "divide_and_round_ntt_inv_scalar_kernel")
         self.sr_qr_r = k("rns", "scaleAndRound_HPS_QR_R_kernel")
         self.tensor = k("polymath", "tensor_prod_2x2_rns_poly")
@@ -121,6 +125,18 @@ class Kernels:
         self.dec = {v: k("rns", "hps_decrypt_scale_and_round_kernel_" + v)
                     for v in ("small", "small_lazy", "large", "large_lazy")}
         self.galois = k("galois", "apply_galois_ntt_permutation")
+        for stem in ("ckks", "fft", "rns_base"):
+            m[stem] = R.Module(stem)
+        self.bitrev = k("ckks", "bit_reverse_kernel")
+        self.fft_base = k("fft", "inplace_special_ffft_base_kernel")
+        self.fft_iter = k("fft", "inplace_special_ffft_iter_kernel")
+        self.ifft_base = k("fft", "inplace_special_ifft_base_kernel")
+        self.ifft_iter = k("fft", "inplace_special_ifft_iter_kernel")
+        self.dec64 = k("rns_base", "decompose_array_uint64_kernel")
+        self.dec128 = k("rns_base", "decompose_array_uint128_kernel")
+        self.dec_slow1 = k("rns_base", "decompose_array_uint_slow_first_part")
+        self.dec_slow2 = k("rns_base", "decompose_array_uint_slow_second_part")
+        self.compose = k("rns_base", "compose_array_kernel")
 
     # nwt_2d_radix8_forward_inplace, src/ntt/fntt_2d.cu:620-653
     def ntt_fwd(self, T, buf, size, start):
@@ -194,13 +210,10 @@ class Scratch:
         return t
 
 
-def ref_keyswitch(K, T, oc, L, ct_d, c2_d, evk_ptrs, scratch=None, keep=False):
-    """keyswitch_inplace for CKKS, src/eval_key_switch.cu:95-182, with DRNSTool::modup
-    (src/rns_bconv.cu:530-628), key_switch_inner_prod (src/eval_key_switch.cu:71-92) and
-    DRNSTool::moddown_from_NTT (src/rns_bconv.cu:776-828).  ct_d (2 x l x N, device) is updated
-    in place; with keep=True returns the host copies of t_mod_up and cx."""
-    S = scratch or Scratch()
-    n, nq, a, qp = oc.n, oc.n_q, oc.n_p, oc.n_q + oc.n_p
+def ref_modup(K, T, oc, L, c2_d, S):
+    """DRNSTool::modup for CKKS (src/rns_bconv.cu:530-628): c2_d (l x N, NTT form, device) ->
+    t_mod_up [beta][l + alpha][N] (a scratch buffer of S)."""
+    n, a, qp = oc.n, oc.n_p, oc.n_q + oc.n_p
     l, qlp, beta = L.l, L.qlp, L.beta
     s_fwd = sample_size(n)
     s2_inv = sample_size(n)
@@ -223,13 +236,26 @@ def ref_keyswitch(K, T, oc, L, ct_d, c2_d, evk_ptrs, scratch=None, keep=False):
                  n, s_fwd, PAD, lo, hi)
         K.mu_f2x(GRID_NTT, BLOCK_NTT, BLOCK_NTT * 64, part, T.tw, T.tws, T.mod, qlp, 0, qp, a, n, s_fwd,
                  n // s_fwd, lo, hi)
-    tm = R.host(t_mod_up, beta * qlp * n) if keep else None
-    # inner product; reduction_threshold as src/eval_key_switch.cu:156-157
+    return t_mod_up
+
+
+def ref_inner_product(K, T, oc, L, cx, t_mod_up, evk_ptrs):
+    """key_switch_inner_prod_c2_and_evk launched as src/eval_key_switch.cu:156-160 (the
+    reduction_threshold of :156-157): cx [2][l + alpha][N]."""
+    n, nq, qp = oc.n, oc.n_q, oc.n_q + oc.n_p
     thr = (1 << (64 - int(np.log2(float(T.mods[0]))) - 1)) - 1
-    cx = S("cx", 2 * qlp * n + n)
-    K.ip(qlp * n // BLOCK_GLB, BLOCK_GLB, 0, cx, t_mod_up, evk_ptrs, T.mod, n, qp, qp * n, qlp, qlp * n, nq, l,
-         beta, thr)
-    cxh = R.host(cx, 2 * qlp * n) if keep else None
+    K.ip(L.qlp * n // BLOCK_GLB, BLOCK_GLB, 0, cx, t_mod_up, evk_ptrs, T.mod, n, qp, qp * n, L.qlp, L.qlp * n, nq,
+         L.l, L.beta, thr)
+
+
+def ref_moddown(K, T, oc, L, cx, S):
+    """DRNSTool::moddown_from_NTT for CKKS (src/rns_bconv.cu:776-828) on both polynomials of
+    cx [2][l + alpha][N], in place (the first l limbs of each hold the result)."""
+    n, a, qp = oc.n, oc.n_p, oc.n_q + oc.n_p
+    l, qlp = L.l, L.qlp
+    s_fwd = sample_size(n)
+    s2_inv = sample_size(n)
+    s1_inv = n // s2_inv
     for i in range(2):
         cx_i = R.Ptr(cx, i * qlp * n)
         # nwt_2d_radix8_backward_inplace_include_special_mod (src/ntt/intt_2d.cu:796-834)
@@ -248,9 +274,63 @@ def ref_keyswitch(K, T, oc, L, ct_d, c2_d, evk_ptrs, scratch=None, keep=False):
                 s_fwd, PAD)
         K.md_f2(GRID_NTT, BLOCK_NTT, BLOCK_NTT * 64, cx_i, cx_i, L.p_inv, L.p_inv_s, delta, T.tw, T.tws, T.mod,
                 l, 0, n, s_fwd, n // s_fwd)
+
+
+def ref_keyswitch(K, T, oc, L, ct_d, c2_d, evk_ptrs, scratch=None, keep=False):
+    """keyswitch_inplace for CKKS, src/eval_key_switch.cu:95-182, with DRNSTool::modup
+    (src/rns_bconv.cu:530-628), key_switch_inner_prod (src/eval_key_switch.cu:71-92) and
+    DRNSTool::moddown_from_NTT (src/rns_bconv.cu:776-828).  ct_d (2 x l x N, device) is updated
+    in place; with keep=True returns the host copies of t_mod_up and cx."""
+    S = scratch or Scratch()
+    n = oc.n
+    l, qlp, beta = L.l, L.qlp, L.beta
+    t_mod_up = ref_modup(K, T, oc, L, c2_d, S)
+    tm = R.host(t_mod_up, beta * qlp * n) if keep else None
+    cx = S("cx", 2 * qlp * n + n)
+    ref_inner_product(K, T, oc, L, cx, t_mod_up, evk_ptrs)
+    cxh = R.host(cx, 2 * qlp * n) if keep else None
+    ref_moddown(K, T, oc, L, cx, S)
     for i in range(2):
         K.add_to_ct(l * n // BLOCK_GLB, BLOCK_GLB, 0, R.Ptr(ct_d, i * l * n), R.Ptr(cx, i * qlp * n), T.mod, n, l)
     return tm, cxh
+
+
+def ref_hoisting(K, T, oc, L, ct_d, perms, keys, S):
+    """hoisting_inplace for CKKS, src/evaluate.cu:1670-1865: one mod-up of c1; per step the Galois
+    permutation of c0 and of every digit of the mod-up (apply_galois_ntt over Ql / QlP limbs,
+    src/galois.cu:86-102), the inner product with that step's key, and the sums (add_rns_poly,
+    src/polymath.cu:41-55); one mod-down of the summed products; ct = (acc_c0 + cx_0, cx_1)."""
+    n = oc.n
+    l, qlp, beta = L.l, L.qlp, L.beta
+    qlp_mod = R.dev(dmod(L.qlp_mods), 8)
+    c0 = S("h_c0", l * n + n)
+    c0[: l * n].copy_(ct_d[: l * n])
+    acc_c0 = S("h_acc_c0", l * n + n)
+    K.galois(l * n // BLOCK_GLB, BLOCK_GLB, 0, acc_c0, c0, perms[0], n, l)
+    c1 = S("h_c1", l * n + n)
+    c1[: l * n].copy_(ct_d[l * n: 2 * l * n])
+    modup_c1 = ref_modup(K, T, oc, L, c1, S)
+    tmp_mu = S("h_tmp_modup", beta * qlp * n + n)
+    for b in range(beta):
+        K.galois(qlp * n // BLOCK_GLB, BLOCK_GLB, 0, R.Ptr(tmp_mu, b * qlp * n), R.Ptr(modup_c1, b * qlp * n),
+                 perms[0], n, qlp)
+    acc_cx = S("h_acc_cx", 2 * qlp * n + n)
+    ref_inner_product(K, T, oc, L, acc_cx, tmp_mu, keys[0])
+    temp_c0 = S("h_temp_c0", l * n + n)
+    temp_cx = S("h_temp_cx", 2 * qlp * n + n)
+    for i in range(1, len(perms)):
+        K.galois(l * n // BLOCK_GLB, BLOCK_GLB, 0, temp_c0, c0, perms[i], n, l)
+        K.add_poly(l * n // BLOCK_GLB, BLOCK_GLB, 0, acc_c0, temp_c0, T.mod, acc_c0, n, l)
+        for b in range(beta):
+            K.galois(qlp * n // BLOCK_GLB, BLOCK_GLB, 0, R.Ptr(tmp_mu, b * qlp * n),
+                     R.Ptr(modup_c1, b * qlp * n), perms[i], n, qlp)
+        ref_inner_product(K, T, oc, L, temp_cx, tmp_mu, keys[i])
+        K.add_poly(qlp * n // BLOCK_GLB, BLOCK_GLB, 0, acc_cx, temp_cx, qlp_mod, acc_cx, n, qlp)
+        K.add_poly(qlp * n // BLOCK_GLB, BLOCK_GLB, 0, R.Ptr(acc_cx, qlp * n), R.Ptr(temp_cx, qlp * n), qlp_mod,
+                   R.Ptr(acc_cx, qlp * n), n, qlp)
+    ref_moddown(K, T, oc, L, acc_cx, S)
+    K.add_poly(l * n // BLOCK_GLB, BLOCK_GLB, 0, acc_c0, acc_cx, T.mod, ct_d, n, l)
+    ct_d[l * n: 2 * l * n].copy_(acc_cx[qlp * n: qlp * n + l * n])
 
 
 def rescale_tables(T, l):
@@ -351,6 +431,208 @@ def case_rotate(K, log_n, bits, special, l, step, seed):
     ref_keyswitch(K, T, oc, KsLevel(oc, T, l), ct, temp, evk_ptrs)
     return {"log_n": log_n, "bits": bits, "special": special, "l": l, "step": step, "elt": elt, "seed": seed,
             "rotate": sha(R.host(ct, 2 * l * n))}
+
+
+def case_hoisting(K, log_n, bits, special, l, steps, seed):
+    """hoisting_inplace for CKKS (src/evaluate.cu:1670-1865) with one Galois key per step, drawn
+    in step order before the ciphertext."""
+    n = 1 << log_n
+    mods = O.create_coeff_modulus(n, bits)
+    nq = len(bits) - special
+    oc = O.Context(log_n, mods, nq, special)
+    T = Tables(log_n, mods)
+    rng = np.random.default_rng(seed)
+    keys, elts, perms = [], [], []
+    for st in steps:
+        keys.append(key_setup(rng, mods, n, nq, special))
+        elt = O.elt_from_step(st, n)
+        elts.append(elt)
+        perms.append(torch.from_numpy(O.galois_perm(log_n, elt).view(np.int32).copy()).cuda())
+    ct = R.dev(O.random_residues(rng, mods[:l], n, 2), n)
+    ref_hoisting(K, T, oc, KsLevel(oc, T, l), ct, perms, [k[1] for k in keys], Scratch())
+    return {"log_n": log_n, "bits": bits, "special": special, "l": l, "steps": steps, "elts": elts, "seed": seed,
+            "hoisting": sha(R.host(ct, 2 * l * n))}
+
+
+def case_bfv_modswitch(K, log_n, bits, special, t, l, seed):
+    """BFV mod_switch_to_next (src/evaluate.cu:1376-1427 -> DRNSTool::divide_and_round_q_last,
+    src/rns.cu:1082-1126) on a size-2 ciphertext in coefficient form with l data limbs."""
+    n = 1 << log_n
+    mods = O.create_coeff_modulus(n, bits)
+    T = Tables(log_n, mods)
+    ct = O.random_residues(np.random.default_rng(seed), mods[:l], n, 2)
+    src = R.dev(ct, n)
+    dst = R.zeros(2 * (l - 1) * n + n)
+    inv, inv_s = rescale_tables(T, l)
+    for i in range(2):
+        K.dr_q_last(n * (l - 1) // BLOCK_GLB, BLOCK_GLB, 0, R.Ptr(dst, i * (l - 1) * n), R.Ptr(src, i * l * n),
+                    T.mod, inv, inv_s, n, l - 1)
+    return {"log_n": log_n, "bits": bits, "special": special, "t": t, "l": l, "seed": seed,
+            "mod_switch": sha(R.host(dst, 2 * (l - 1) * n))}
+
+
+SWITCH_POINT, FFT_THREADS = 2048, 1024  # include/common.h:13-15
+
+
+def ckks_roots(log_n):
+    """The encoder's twiddle table: ComplexRoots of degree m = 2N (src/fft.cu:12-41, polar(1, 2 pi i
+    / m) for i <= m/8) read through get_root for every index < m, as [m][2] doubles."""
+    m = 2 << log_n
+    base = [(math.cos(2 * math.pi * i / m), math.sin(2 * math.pi * i / m)) for i in range(m // 8 + 1)]
+
+    def get_root(i):
+        i &= m - 1
+        if i <= m // 8:
+            return base[i]
+        if i <= m // 4:
+            r = base[m // 4 - i]
+            return (r[1], r[0])
+        if i <= m // 2:
+            r = get_root(m // 2 - i)
+            return (0.0 - r[0], 0.0 - (-r[1]))
+        if i <= 3 * m // 4:
+            r = get_root(i - m // 2)
+            return (0.0 - r[0], 0.0 - r[1])
+        r = get_root(m - i)
+        return (r[0], -r[1])
+
+    return np.array([get_root(i) for i in range(m)], dtype=np.float64)
+
+
+def rotation_group(log_n):
+    """5^i mod 2N for i < N/4 (src/ckks.cu:36-46)."""
+    m, out, pos = 2 << log_n, [], 1
+    for _ in range((1 << log_n) // 4):
+        out.append(pos)
+        pos = pos * 5 % m
+    return np.array(out, dtype=np.uint32)
+
+
+class Codec:
+    """Device tables of PhantomCKKSEncoder (src/ckks.cu:17-66) for one degree."""
+
+    def __init__(self, log_n):
+        self.log_n, self.n = log_n, 1 << log_n
+        self.slots, self.m = self.n // 2, 2 * self.n
+        self.roots = R.dev(ckks_roots(log_n))
+        self.group = torch.from_numpy(rotation_group(log_n).view(np.int32).copy()).cuda()
+
+
+def ref_fft_backward(K, C, buf, scalar):
+    """special_fft_backward (src/fft.cu:374-413)."""
+    n, logn = C.slots, C.log_n - 1
+    if n <= SWITCH_POINT:
+        K.ifft_base(1, n // 2, n * 16, buf, C.roots, C.group, n, logn, 1, 0, C.m, scalar)
+        return
+    it, groups = logn - 11, n // SWITCH_POINT
+    blocks = -(-n // FFT_THREADS // 2)
+    K.ifft_base(blocks, FFT_THREADS, SWITCH_POINT * 16, buf, C.roots, C.group, n, logn, groups, it, C.m, scalar)
+    groups >>= 1
+    while groups >= 1:
+        it -= 1
+        K.ifft_iter(blocks, FFT_THREADS, 0, buf, C.roots, C.group, n, logn, groups, it, C.m, scalar)
+        groups >>= 1
+
+
+def ref_fft_forward(K, C, buf):
+    """special_fft_forward (src/fft.cu:340-368)."""
+    n, logn = C.slots, C.log_n - 1
+    if n <= SWITCH_POINT:
+        K.fft_base(1, n // 2, n * 16, buf, C.roots, C.group, n, logn, 1, 0, C.m)
+        return
+    it, groups = 0, 1
+    blocks = -(-n // FFT_THREADS // 2)
+    while groups < n // SWITCH_POINT:
+        K.fft_iter(blocks, FFT_THREADS, 0, buf, C.roots, C.group, n, logn, groups, it, C.m)
+        it += 1
+        groups <<= 1
+    K.fft_base(blocks, FFT_THREADS, SWITCH_POINT * 16, buf, C.roots, C.group, n, logn, groups, it, C.m)
+
+
+def ref_encode(K, T, C, values, scale, l):
+    """PhantomCKKSEncoder::encode_internal (src/ckks.cu:68-138) of complex `values` at `scale`
+    into l limbs; returns the plaintext (device, NTT form)."""
+    n, slots = C.n, C.slots
+    count = len(values)
+    temp = R.dev(np.stack([values.real, values.imag], axis=1).astype(np.float64))
+    buf = torch.zeros(2 * slots, dtype=torch.float64, device="cuda")
+    K.bitrev(-(-count // BLOCK_GLB), BLOCK_GLB, 0, buf, temp, count, C.log_n - 1)
+    ref_fft_backward(K, C, buf, scale / float(slots))
+    z = buf.cpu().numpy()
+    max_coeff = float(np.max(np.abs(z))) if z.size else 0.0
+    max_bits = int(math.ceil(math.log2(max(max_coeff, 1.0)))) + 1
+    q_bits = math.prod(int(q) for q in T.mods[:l]).bit_length()
+    assert max_bits < q_bits, "encoded values are too large"
+    pt = R.zeros(l * n + n)
+    grid = n * l // BLOCK_GLB
+    if max_bits <= 64:
+        K.dec64(grid, BLOCK_GLB, 0, pt, buf, T.mod, n)
+    elif max_bits <= 128:
+        K.dec128(grid, BLOCK_GLB, 0, pt, buf, T.mod, n)
+    else:
+        coeffu = R.zeros(n * (l + 1))
+        K.dec_slow1(grid, BLOCK_GLB, 0, coeffu, buf, n, l)
+        K.dec_slow2(grid, BLOCK_GLB, 0, pt, coeffu, T.mod, n, l)
+    K.ntt_fwd(T, pt, l, 0)
+    return pt, max_bits
+
+
+def compose_tables(mods):
+    """DRNSBase of Q_l (src/rns_base.cu:11-47): Q_l, Q_l / q_i, (Q_l / q_i)^-1 mod q_i (+ Shoup)
+    and the context's upper_half_threshold (Q_l + 1) / 2 (src/context.cu:106-110), as words."""
+    l = len(mods)
+    Q = math.prod(int(q) for q in mods)
+
+    def words(v):
+        return [(v >> (64 * w)) & ((1 << 64) - 1) for w in range(l)]
+    hats = [Q // int(q) for q in mods]
+    inv = [pow(h % int(q), -1, int(q)) for h, q in zip(hats, mods)]
+    return (R.dev(np.array(words(Q), dtype=np.uint64), 8),
+            R.dev(np.array([w for h in hats for w in words(h)], dtype=np.uint64), 8),
+            *pair(inv, mods),
+            R.dev(np.array(words((Q + 1) >> 1), dtype=np.uint64), 8))
+
+
+def ref_decode(K, T, C, pt, scale, l):
+    """PhantomCKKSEncoder::decode_internal (src/ckks.cu:340-400): plaintext (l limbs, NTT form)
+    -> N/2 complex slots as [N/2][2] doubles (host)."""
+    n, slots = C.n, C.slots
+    copy = R.zeros(l * n + n)
+    copy[: l * n].copy_(pt[: l * n])
+    K.ntt_inv(T, copy, l, 0)
+    qprod, qhat, qinv, qinv_s, upper = compose_tables(T.mods[:l])
+    buf = torch.zeros(2 * slots, dtype=torch.float64, device="cuda")
+    temp_prod, acc = R.zeros(n * l), R.zeros(n * l)
+    K.compose(n // BLOCK_GLB, BLOCK_GLB, 0, buf, temp_prod, acc, copy, l, T.mod, qprod, qhat, qinv, qinv_s, upper,
+              1.0 / scale, n)
+    ref_fft_forward(K, C, buf)
+    out = torch.zeros(2 * slots, dtype=torch.float64, device="cuda")
+    K.bitrev(-(-slots // BLOCK_GLB), BLOCK_GLB, 0, out, buf, slots, C.log_n - 1)
+    return out.cpu().numpy()
+
+
+def unit_disk(rng, count):
+    r, th = np.sqrt(rng.uniform(0, 1, count)), 2 * np.pi * rng.uniform(0, 1, count)
+    return r * np.cos(th) + 1j * r * np.sin(th)
+
+
+def case_codec(K, log_n, bits, special, l, scale, count, seed):
+    """The CKKS encoder: encode `count` slots uniform in the unit disk at `scale` into l limbs,
+    decode that plaintext, and decode a plaintext of uniform random residues (both halves of the
+    compose's centring)."""
+    n = 1 << log_n
+    mods = O.create_coeff_modulus(n, bits)
+    T = Tables(log_n, mods)
+    C = Codec(log_n)
+    rng = np.random.default_rng(seed)
+    vals = unit_disk(rng, count)
+    pt, max_bits = ref_encode(K, T, C, vals, scale, l)
+    dec = ref_decode(K, T, C, pt, scale, l)
+    rnd = R.dev(O.random_residues(rng, mods[:l], n, 1), n)
+    dec_rnd = ref_decode(K, T, C, rnd, scale, l)
+    return {"log_n": log_n, "bits": bits, "special": special, "l": l, "scale": scale, "count": count, "seed": seed,
+            "max_coeff_bits": max_bits, "encode": sha(R.host(pt, l * n)), "decode": sha(dec.view(np.uint64)),
+            "decode_random": sha(dec_rnd.view(np.uint64))}
 
 
 def case_rescale(K, log_n, bits, special, l, seed):
@@ -846,6 +1128,153 @@ def time_reference(K, path):
     print(json.dumps(res))
 
 
+def ref_apply_galois(K, T, oc, L, ct, perm, key_ptrs, temp, S):
+    """apply_galois_inplace for CKKS (src/evaluate.cu:1567-1630) on ct (2 x l x N, device)."""
+    n, l = oc.n, L.l
+    K.galois(l * n // BLOCK_GLB, BLOCK_GLB, 0, temp, ct, perm, n, l)
+    ct[: l * n].copy_(temp[: l * n])
+    K.galois(l * n // BLOCK_GLB, BLOCK_GLB, 0, temp, R.Ptr(ct, l * n), perm, n, l)
+    ct[l * n: 2 * l * n].zero_()
+    ref_keyswitch(K, T, oc, L, ct, temp, key_ptrs, scratch=S)
+
+
+def time_reference_batched(K, path):
+    """Device time of the reference's own kernels over the two batched workloads, as the reference
+    serves a batch: a host loop of single-ciphertext calls (captured in CUDA graphs here, so host
+    launch and allocation costs are excluded, which can only favour the reference).
+    * 64 HMult + relinearise + rescale at levels drawn as bench.py draws them
+      (default_rng(2000).integers(5, 31, 64)), N = 2^16, 1x60 + 29x40 + 5x60, one relinearisation key.
+    * 32 matrix-vector products 128 x 128 by the reference's loop (bsgs_complete_from_cpu,
+      python/src/binding.cu:507-595: G - 1 baby rotations, per giant step G plaintext products
+      (multiply_plain: copy + multiply_rns_poly, src/evaluate.cu:1224-1250) summed by add_inplace
+      (:116-195), a giant rotation by g G, the sum, one rescale) at N = 2^16, 1x60 + 19x40 + 4x60,
+      G = 11, B = 12, at the levels of bench.py's draw."""
+    res = {}
+    log_n, n = 16, 1 << 16
+    # ---- 64 HMult + relin + rescale at uneven levels
+    bits, special = [60] + [40] * 29 + [60] * 5, 5
+    mods = O.create_coeff_modulus(n, bits)
+    nq = 30
+    oc = O.Context(log_n, mods, nq, special)
+    T = Tables(log_n, mods)
+    levels = [int(x) for x in np.random.default_rng(2000).integers(5, 31, size=64)]
+    Ls = {lv: KsLevel(oc, T, lv) for lv in sorted(set(levels))}
+    rts = {lv: rescale_tables(T, lv) for lv in Ls}
+    rng = np.random.default_rng(7)
+    evk_t, evk_ptrs = key_setup(rng, mods, n, nq, special)
+    S = Scratch()
+    ins = [(R.dev(O.random_residues(rng, mods[:lv], n, 2), n), R.dev(O.random_residues(rng, mods[:lv], n, 2), n))
+           for lv in levels]
+    d = R.zeros(3 * nq * n + n)
+    cp = R.zeros(2 * nq * n + n)
+    outs = [R.zeros(2 * (lv - 1) * n + n) for lv in levels]
+
+    def hmult(i):
+        lv = levels[i]
+        a, b = ins[i]
+        K.tensor(lv * n // BLOCK_GLB, BLOCK_GLB, 0, a, b, T.mod, d, n, lv)
+        ref_keyswitch(K, T, oc, Ls[lv], d, R.Ptr(d, 2 * lv * n), evk_ptrs, scratch=S)
+        cp[: 2 * lv * n].copy_(d[: 2 * lv * n])
+        ref_rescale(K, T, cp, outs[i], lv, 2, rts[lv])
+
+    ms = graph_time(hmult, 64, 3, (S,))
+    res["ckks_hmult_relin_rescale_batch64_levels5_30_ms_per_op"] = ms
+    res["ckks_hmult_relin_rescale_batch64_levels5_30_ops_per_s"] = 1e3 / ms
+    res["batch64_levels"] = levels
+    del ins, outs, d, cp, evk_t, S, Ls
+    torch.cuda.empty_cache()
+
+    # ---- 32 matrix-vector products by the reference's loop
+    bits, special = [60] + [40] * 19 + [60] * 4, 4
+    mods = O.create_coeff_modulus(n, bits)
+    nq, G, B, D = 20, 11, 12, 128
+    oc = O.Context(log_n, mods, nq, special)
+    T = Tables(log_n, mods)
+    # bench.py's draw: 32 levels in 3..20 (default_rng(5000) after the key and matrix draws)
+    mv_levels = [17, 19, 11, 6, 9, 10, 16, 20, 5, 18, 10, 8, 8, 12, 15, 4, 16, 5, 5, 11, 15, 7, 5, 15, 14, 11, 4, 7,
+                 19, 4, 8, 19]
+    Ls = {lv: KsLevel(oc, T, lv) for lv in sorted(set(mv_levels))}
+    rts = {lv: rescale_tables(T, lv) for lv in Ls}
+    rng = np.random.default_rng(8)
+    steps = list(range(1, G)) + [g * G for g in range(1, B)]
+    keys = {st: key_setup(rng, mods, n, nq, special) for st in steps}
+    perms = {st: torch.from_numpy(O.galois_perm(log_n, O.elt_from_step(st, n)).view(np.int32).copy()).cuda()
+             for st in steps}
+    diags = R.dev(O.random_residues(rng, mods[:nq], n, D), n)  # [D][20][N]; level l reads limbs < l
+    cts = [R.dev(O.random_residues(rng, mods[:lv], n, 2), n) for lv in mv_levels]
+    S = Scratch()
+    babies = [R.zeros(2 * nq * n + n) for _ in range(G)]
+    term, inner, result = R.zeros(2 * nq * n + n), R.zeros(2 * nq * n + n), R.zeros(2 * nq * n + n)
+    temp, cpy = R.zeros(nq * n + n), R.zeros(2 * nq * n + n)
+    outs = [R.zeros(2 * (lv - 1) * n + n) for lv in mv_levels]
+
+    def add_inplace(dst, src, lv):
+        for p in range(2):
+            K.add_poly(lv * n // BLOCK_GLB, BLOCK_GLB, 0, R.Ptr(dst, p * lv * n), R.Ptr(src, p * lv * n), T.mod,
+                       R.Ptr(dst, p * lv * n), n, lv)
+
+    def matvec(i):
+        lv, ct = mv_levels[i], cts[i]
+        L = Ls[lv]
+        w = 2 * lv * n
+        babies[0][:w].copy_(ct[:w])
+        for b in range(1, G):  # phantom::rotate: copy, then rotate_inplace
+            babies[b][:w].copy_(ct[:w])
+            ref_apply_galois(K, T, oc, L, babies[b], perms[b], keys[b][1], temp, S)
+        for g in range(B):
+            first = True
+            for b in range(G):
+                k = g * G + b
+                if k >= D:
+                    continue
+                dst = inner if first else term
+                dst[:w].copy_(babies[b][:w])  # multiply_plain: copy, then multiply_plain_inplace
+                for p in range(2):
+                    K.mul_poly(lv * n // BLOCK_GLB, BLOCK_GLB, 0, R.Ptr(dst, p * lv * n), R.Ptr(diags, k * nq * n),
+                               T.mod, R.Ptr(dst, p * lv * n), n, lv)
+                if not first:
+                    add_inplace(inner, term, lv)
+                first = False
+            if g > 0:
+                ref_apply_galois(K, T, oc, L, inner, perms[g * G], keys[g * G][1], temp, S)
+            if g == 0:
+                result[:w].copy_(inner[:w])
+            else:
+                add_inplace(result, inner, lv)
+        cpy[:w].copy_(result[:w])
+        ref_rescale(K, T, cpy, outs[i], lv, 2, rts[lv])
+
+    ms = graph_time(matvec, len(mv_levels), 2, (S,))
+    res["ckks_matvec128_batch32_reference_loop_ms_per_matvec"] = ms
+    res["ckks_matvec128_batch32_reference_loop_per_s"] = 1e3 / ms
+    res["matvec_levels"] = mv_levels
+    res["note"] = ("reference kernels compiled from source for sm_103a, replayed in CUDA graphs on the reference's "
+                   "own launch configuration as a host loop of single-ciphertext calls; device time only")
+    with open(path, "w") as f:
+        json.dump(res, f, indent=1, sort_keys=True)
+    print(json.dumps(res))
+
+
+def extra_cases(K):
+    """Hoisted rotations (hoisting_inplace) and the BFV modulus switch."""
+    return {
+        "hoist_ckks_n12_a2": case_hoisting(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, [1, 2, 4, -1], 1213),
+        "hoist_ckks_n12_a2_l4": case_hoisting(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 4, [3, -5], 1214),
+        "hoist_ckks_n16_l30": case_hoisting(K, 16, [60] + [40] * 29 + [60] * 5, 5, 30, [1, 2, 4, -1], 1608),
+        "hoist_ckks_n16_l20_a4": case_hoisting(K, 16, [60] + [40] * 19 + [60] * 4, 4, 20, [1, 2, 11], 1609),
+        "modswitch_bfv_n12_4x50": case_bfv_modswitch(K, 12, [50, 50, 50, 50, 60, 60], 2, 65537, 4, 1215),
+        "modswitch_bfv_n15_16x50": case_bfv_modswitch(K, 15, [50] * 16 + [60, 60], 2, 65537, 16, 1504),
+        "modswitch_bfv_n15_16x50_l9": case_bfv_modswitch(K, 15, [50] * 16 + [60, 60], 2, 65537, 9, 1505),
+        "codec_n12_l5": case_codec(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, 2.0 ** 40, 2048, 1216),
+        "codec_n12_l3_partial": case_codec(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 3, 2.0 ** 30, 1027, 1217),
+        "codec_n12_l1": case_codec(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 1, 2.0 ** 40, 2048, 1218),
+        "codec_n16_l30": case_codec(K, 16, [60] + [40] * 29 + [60] * 5, 5, 30, 2.0 ** 40, 32768, 1610),
+        "codec_n16_l30_w128": case_codec(K, 16, [60] + [40] * 29 + [60] * 5, 5, 30, 2.0 ** 80, 32768, 1611),
+        "codec_n16_l30_wide": case_codec(K, 16, [60] + [40] * 29 + [60] * 5, 5, 30, 2.0 ** 150, 20000, 1612),
+        "codec_n16_l20_a4": case_codec(K, 16, [60] + [40] * 19 + [60] * 4, 4, 20, 2.0 ** 40, 32768, 1613),
+    }
+
+
 def main(path):
     torch.zeros(1, device="cuda")
     K = Kernels()
@@ -878,6 +1307,7 @@ def main(path):
         "bfv_n13_a3": case_bfv(K, 13, [50] * 6 + [60] * 3, 3, 65537, 1303),
         "bfv_n15_16x50": case_bfv(K, 15, [50] * 16 + [60, 60], 2, 65537, 1502),
     }
+    res.update(extra_cases(K))
     with open(path, "w") as f:
         json.dump(res, f, indent=1, sort_keys=True)
     print(json.dumps({k: "ok" for k in res}))
@@ -887,5 +1317,14 @@ if __name__ == "__main__":
     if len(sys.argv) == 3 and sys.argv[1] == "--time":
         torch.zeros(1, device="cuda")
         time_reference(Kernels(), sys.argv[2])
+    elif len(sys.argv) == 3 and sys.argv[1] == "--time-batched":
+        torch.zeros(1, device="cuda")
+        time_reference_batched(Kernels(), sys.argv[2])
+    elif len(sys.argv) == 3 and sys.argv[1] == "--extra":  # only the cases of extra_cases()
+        torch.zeros(1, device="cuda")
+        res = extra_cases(Kernels())
+        with open(sys.argv[2], "w") as f:
+            json.dump(res, f, indent=1, sort_keys=True)
+        print(json.dumps({k: "ok" for k in res}))
     else:
         main(sys.argv[1])

@@ -69,7 +69,7 @@ def elf_function_names(image):
 def param_sizes(mangled, ident):
     """Byte sizes of the parameters encoded after `ident` in an Itanium-mangled kernel name.
     Covers what these kernels use: pointers (P, with K qualifiers and S..._ substitutions),
-    unsigned long (m), unsigned int (j), double (d)."""
+    unsigned long (m), unsigned int (j), int (i), double (d)."""
     i = mangled.index(ident) + len(ident)
     if mangled[i] == "E":  # end of a nested name
         i += 1
@@ -91,7 +91,7 @@ def param_sizes(mangled, ident):
             sizes.append(8)
             continue
         i += 1
-        sizes.append(8 if ptr else {"m": 8, "j": 4, "d": 8, "y": 8}[c])
+        sizes.append(8 if ptr else {"m": 8, "j": 4, "i": 4, "d": 8, "y": 8}[c])
     return sizes
 
 

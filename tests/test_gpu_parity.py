@@ -75,8 +75,8 @@ def test_ntt_start_index_and_constant_inputs(small, pg):
         _eq(t, a, "round trip")
 
 
-def _primes_below_2_61(n, count):
-    """The largest primes q = 1 mod 2n below 2^61 (deterministic Miller-Rabin for 64 bits)."""
+def _primes_below_2_61(n, count, bits=61):
+    """The largest primes q = 1 mod 2n below 2^bits (deterministic Miller-Rabin for 64 bits)."""
     def is_prime(q):
         d, s = q - 1, 0
         while d % 2 == 0:
@@ -92,25 +92,29 @@ def _primes_below_2_61(n, count):
             else:
                 return False
         return True
-    out, q = [], ((1 << 61) - 1) // (2 * n) * (2 * n) + 1
+    out, q = [], ((1 << bits) - 1) // (2 * n) * (2 * n) + 1
     while len(out) < count:
-        if q < (1 << 61) and is_prime(q):
+        if q < (1 << bits) and is_prime(q):
             out.append(q)
         q -= 2 * n
     return out
 
 
 @pytest.mark.parametrize("small_launch", [-1, 0])
-def test_ntt_lazy_inputs_at_range_limits(pg, small_launch):
+@pytest.mark.parametrize("log_n,bits", [(14, 61), (14, 57), (17, 57), (14, 44), (17, 44)])
+def test_ntt_lazy_inputs_at_range_limits(pg, small_launch, log_n, bits):
     """Inside a transform the butterflies keep values in [0, 8q) (forward) and [0, 4q) (inverse)
     with a truncated-quotient Shoup product; producers fused into the passes hand over values in
-    those ranges.  Primes just below 2^61 (the context's limit) and inputs up to 8q - 1 / 4q - 1
-    put every bound at its edge; the outputs must still be the canonical transform."""
-    n = 1 << 14
-    mods = _primes_below_2_61(n, 3)
+    those ranges.  Below 2^57 the forward butterflies drop their conditional subtraction (the
+    range grows by 4q a stage), below 2^44 the inverse ones too (the sums double a stage).  The
+    largest primes of each class (just below 2^61, 2^57 and 2^44), the deepest transforms
+    (N = 2^17) and inputs up to 8q - 1 / 4q - 1 put every bound at its edge; the outputs must
+    still be the canonical transform."""
+    n = 1 << log_n
+    mods = _primes_below_2_61(n, 3, bits)
     ctx = pg.Context(n, mods, 1)
     ctx.ntt_small_launch = small_launch  # both the 8- and the 16-coefficient-per-thread passes
-    oc = O.Context(14, mods, 2, 1)
+    oc = O.Context(log_n, mods, 2, 1)
     rng = np.random.default_rng(61)
     a = O.random_residues(rng, mods, n, 2)
     q = np.array(mods, dtype=np.uint64).reshape(1, 3, 1)

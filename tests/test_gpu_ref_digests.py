@@ -61,11 +61,11 @@ def test_keyswitch_digests(pg, name):
     for l in sorted((int(k) for k in g["levels"]), reverse=True):  # the generator's draw order
         ct = O.random_residues(rng, mods[:l], n, 2)
         c2 = O.random_residues(rng, mods[:l], n, 1)[0]
-        for tc in (True, False):
-            ctx.tensor_cores = tc
+        for tc, fused in ((True, True), (False, True), (True, False)):
+            ctx.tensor_cores, ctx.fused_keyswitch = tc, fused
             t = pg.to_device(ct)
             ctx.keyswitch(ws, t, pg.to_device(c2), nq - l + 1, key)
-            assert sha(t) == g["levels"][str(l)]["keyswitch"], f"level {l}, tensor_cores={tc}"
+            assert sha(t) == g["levels"][str(l)]["keyswitch"], f"level {l}, tensor_cores={tc}, fused={fused}"
         assert ctx.device_status() == 0
 
 
@@ -108,14 +108,14 @@ def test_hmult_digests(pg, name):
     a = O.random_residues(rng, mods[:l], n, 2)
     b = O.random_residues(rng, mods[:l], n, 2)
     chain = nq - l + 1
-    for tc in (True, False):
-        ctx.tensor_cores = tc
+    for tc, fused in ((True, True), (False, True), (True, False)):
+        ctx.tensor_cores, ctx.fused_keyswitch = tc, fused
         out = torch.empty((2, l - 1, n), dtype=torch.int64, device="cuda")
         ctx.multiply_relin_rescale(ws, pg.to_device(a), pg.to_device(b), out, chain, key)
-        assert sha(out) == g["rescaled"], f"fused, tensor_cores={tc}"
+        assert sha(out) == g["rescaled"], f"one call, tensor_cores={tc}, fused key switch={fused}"
         ta = pg.to_device(a)
         ctx.multiply_and_relin(ws, ta, pg.to_device(b), chain, key)
-        assert sha(ta) == g["multiply_and_relin"], f"multiply_and_relin, tensor_cores={tc}"
+        assert sha(ta) == g["multiply_and_relin"], f"multiply_and_relin, tensor_cores={tc}, fused={fused}"
         out2 = torch.empty((2, l - 1, n), dtype=torch.int64, device="cuda")
         ctx.rescale_to_next(ws, ta, out2, 2, chain)
         assert sha(out2) == g["rescaled"], f"two calls, tensor_cores={tc}"
@@ -226,9 +226,79 @@ def test_rotate_digests(pg, name):
     gk = O.random_residues(rng, mods, n, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), n)
     key = pg.KeySwitchKey(pg.to_device(gk))
     ct = O.random_residues(rng, mods[:l], n, 2)
+    for tc, fused in ((True, True), (False, True), (True, False)):
+        ctx.tensor_cores, ctx.fused_keyswitch = tc, fused
+        t = pg.to_device(ct)
+        ctx.apply_galois(ws, t, nq - l + 1, g["elt"], key)
+        assert sha(t) == g["rotate"], f"tensor_cores={tc}, fused={fused}"
+    assert ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("name", [k for k in G if k.startswith("hoist_")])
+def test_hoisting_digests(pg, name):
+    """hoisting_inplace (one mod-up of c1, per-step permuted inner products summed, one mod-down)
+    gives the reference's words, with the tensor-core and the CUDA-core conversions."""
+    g = G[name]
+    n, l = 1 << g["log_n"], g["l"]
+    mods = pg.create_coeff_modulus(n, g["bits"])
+    nq = len(g["bits"]) - g["special"]
+    ctx = pg.Context(n, mods, g["special"], galois_elts=g["elts"])
+    ws = ctx.workspace()
+    rng = np.random.default_rng(g["seed"])
+    keys = [O.random_residues(rng, mods, n, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), n) for _ in g["steps"]]
+    gks = [None] * len(ctx.galois_elts)
+    for e, k in zip(g["elts"], keys):
+        gks[ctx.galois_elts.index(e)] = pg.KeySwitchKey(pg.to_device(k))
+    ct = O.random_residues(rng, mods[:l], n, 2)
     for tc in (True, False):
         ctx.tensor_cores = tc
         t = pg.to_device(ct)
-        ctx.apply_galois(ws, t, nq - l + 1, g["elt"], key)
-        assert sha(t) == g["rotate"], f"tensor_cores={tc}"
+        ctx.hoisting(ws, t, nq - l + 1, g["steps"], gks)
+        assert sha(t) == g["hoisting"], f"tensor_cores={tc}"
     assert ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("name", [k for k in G if k.startswith("modswitch_bfv_")])
+def test_bfv_mod_switch_digests(pg, name):
+    """BFV mod_switch_to_next (divide_and_round_q_last in the coefficient domain)."""
+    g = G[name]
+    n, l = 1 << g["log_n"], g["l"]
+    mods = pg.create_coeff_modulus(n, g["bits"])
+    nq = len(g["bits"]) - g["special"]
+    ctx = pg.Context(n, mods, g["special"], scheme=pg.SCHEME_BFV, plain_modulus=g["t"])
+    ct = O.random_residues(np.random.default_rng(g["seed"]), mods[:l], n, 2)
+    out = torch.empty((2, l - 1, n), dtype=torch.int64, device="cuda")
+    ctx.bfv_mod_switch_to_next(pg.to_device(ct), out, 2, nq - l + 1)
+    assert sha(out) == g["mod_switch"]
+
+
+def _unit_disk(rng, count):
+    r, th = np.sqrt(rng.uniform(0, 1, count)), 2 * np.pi * rng.uniform(0, 1, count)
+    return r * np.cos(th) + 1j * r * np.sin(th)
+
+
+@pytest.mark.parametrize("name", [k for k in G if k.startswith("codec_")])
+def test_ckks_encoder_digests(pg, name):
+    """The CKKS encoder (FP64 special FFT, rounding, residues, NTT) and decoder (inverse NTT, CRT
+    compose over every limb, FP64 special FFT) give the reference's plaintext words and the
+    reference's decoded doubles, bit for bit; decoding uniform random residues exercises both
+    halves of the compose's centring."""
+    g = G[name]
+    n, l = 1 << g["log_n"], g["l"]
+    mods = pg.create_coeff_modulus(n, g["bits"])
+    nq = len(g["bits"]) - g["special"]
+    ctx = pg.Context(n, mods, g["special"])
+    ws = ctx.workspace()
+    chain = nq - l + 1
+    rng = np.random.default_rng(g["seed"])
+    vals = _unit_disk(rng, g["count"])
+    vt = torch.from_numpy(np.stack([vals.real, vals.imag], axis=1).copy()).cuda()
+    pt = torch.empty((l, n), dtype=torch.int64, device="cuda")
+    ctx.ckks_encode(ws, vt, g["scale"], chain, pt)
+    assert sha(pt) == g["encode"], "encode"
+    out = torch.empty((n // 2, 2), dtype=torch.float64, device="cuda")
+    ctx.ckks_decode(ws, pt, g["scale"], chain, out)
+    assert sha(out.cpu().numpy().view(np.uint64)) == g["decode"], "decode of the encoding"
+    rnd = pg.to_device(O.random_residues(rng, mods[:l], n, 1))
+    ctx.ckks_decode(ws, rnd, g["scale"], chain, out)
+    assert sha(out.cpu().numpy().view(np.uint64)) == g["decode_random"], "decode of random residues"

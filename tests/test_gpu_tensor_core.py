@@ -155,7 +155,7 @@ def test_every_ntt_split_gives_the_same_words(pg, log_n, splits):
         _eq(tk, want_ks, f"keyswitch, split {l1}/{log_n - l1}")
     with pytest.raises(pg.InvalidArgument):
         ctx.ntt_split = 5
-    tuned = ctx.autotune()
+    tuned = ctx.autotune_ntt_split()
     assert tuned["ntt_split"] in splits and ctx.ntt_split == tuned["ntt_split"]
 
 

@@ -182,3 +182,29 @@ def test_rotate_matches_reference_kernels(golden, name):
     ct = O.random_residues(rng, mods[:l], n, 2)
     assert O.elt_from_step(g["step"], n) == g["elt"]
     assert sha(oc.ckks_apply_galois(l, ct, g["elt"], gk)) == g["rotate"]
+
+
+@pytest.mark.parametrize("name", _cases("hoist_"))
+def test_hoisting_matches_reference_kernels(golden, name):
+    g = golden[name]
+    n, l = 1 << g["log_n"], g["l"]
+    mods = O.create_coeff_modulus(n, g["bits"])
+    nq = len(g["bits"]) - g["special"]
+    oc = O.Context(g["log_n"], mods, nq, g["special"])
+    rng = np.random.default_rng(g["seed"])
+    dnum = -(-nq // g["special"])
+    keys = [O.random_residues(rng, mods, n, 2 * dnum).reshape(dnum, 2, len(mods), n) for _ in g["steps"]]
+    ct = O.random_residues(rng, mods[:l], n, 2)
+    assert [O.elt_from_step(s, n) for s in g["steps"]] == g["elts"]
+    assert sha(oc.ckks_hoisting(l, ct, g["elts"], keys)) == g["hoisting"]
+
+
+@pytest.mark.parametrize("name", _cases("modswitch_bfv_"))
+def test_bfv_mod_switch_matches_reference_kernels(golden, name):
+    g = golden[name]
+    n, l = 1 << g["log_n"], g["l"]
+    mods = O.create_coeff_modulus(n, g["bits"])
+    nq = len(g["bits"]) - g["special"]
+    oc = O.Context(g["log_n"], mods, nq, g["special"], g["t"])
+    ct = O.random_residues(np.random.default_rng(g["seed"]), mods[:l], n, 2)
+    assert sha(oc.divide_round_q_last(l, ct)) == g["mod_switch"]
