@@ -283,6 +283,8 @@ def run_ours(args):
     ctx = pg.Context(N, mods, SPECIAL)
     ws = ctx.workspace()
     tuning = ctx.autotune(ws)  # kernel shapes, chosen by timing this operation (setup, outside every timed region)
+    if args.case != "full" and "BENCH_FUSED" in os.environ:  # profiling cases: pick the key-switch form
+        ctx.fused_keyswitch = os.environ["BENCH_FUSED"] == "1"
     rng = np.random.default_rng(1000 + rank)
     key = pg.KeySwitchKey(pg.to_device(random_residues(rng, mods, N, 2 * ctx.dnum).reshape(ctx.dnum, 2, len(mods), N)))
     elt1 = pg.elt_from_step(1, N)
@@ -342,6 +344,7 @@ def run_ours(args):
             tb = torch.randint(0, 1 << 40, (2, lv, N), dtype=torch.int64, device="cuda")
             items.append((ta, tb, torch.empty((2, lv - 1, N), dtype=torch.int64, device="cuda"), nq - lv + 1))
         wsb = ctx.workspace(batch_items=64)
+        ctx.fused_keyswitch = os.environ.get("BENCH_BATCH_FUSED", "1") == "1"
         for _ in range(args.warmup + args.steps):
             ctx.multiply_relin_rescale_batch(wsb, items, key, stream)
         torch.cuda.synchronize()
@@ -428,15 +431,23 @@ def run_ours(args):
         tb = torch.randint(0, 1 << 40, (2, lv, N), dtype=torch.int64, device="cuda")
         items.append((ta, tb, torch.empty((2, lv - 1, N), dtype=torch.int64, device="cuda"), nq - lv + 1))
     wsb = ctx.workspace(batch_items=64)
-    ctx.multiply_relin_rescale_batch(wsb, items, key, stream)
     kb = 5
-    t_batch = timed(lambda i: ctx.multiply_relin_rescale_batch(wsb, items, key, stream), kb) / kb
+    ks_items = [(x[0], x[1][1], x[3]) for x in items]  # ct = the first operand, c2 = one poly of the second
+    tuned_fused = ctx.fused_keyswitch
+    t_batch, t_ksb = {}, {}
+    # both forms of the batched mod-up + inner product: the row pass fused with the inner product
+    # (every item's blocks for one key tile run together) and the two-kernel form
+    for fused in (True, False):
+        ctx.fused_keyswitch = fused
+        ctx.multiply_relin_rescale_batch(wsb, items, key, stream)
+        t_batch[fused] = timed(lambda i: ctx.multiply_relin_rescale_batch(wsb, items, key, stream), kb) / kb
+        # the same 64 levels as a batch of key switches (ct += KeySwitch(c2))
+        ctx.keyswitch_batch(wsb, ks_items, key, stream)
+        t_ksb[fused] = timed(lambda i: ctx.keyswitch_batch(wsb, ks_items, key, stream), kb) / kb
+    ctx.fused_keyswitch = tuned_fused
+    # ... and as loops of single calls
     t_loop = timed(lambda i: [ctx.multiply_relin_rescale(ws, x[0], x[1], x[2], x[3], key, stream) for x in items],
                    kb) / kb
-    # the same 64 levels as a batch of key switches (ct += KeySwitch(c2)), and as single calls
-    ks_items = [(x[0], x[1][1], x[3]) for x in items]  # ct = the first operand, c2 = one poly of the second
-    ctx.keyswitch_batch(wsb, ks_items, key, stream)
-    t_ksb = timed(lambda i: ctx.keyswitch_batch(wsb, ks_items, key, stream), kb) / kb
     t_ksl = timed(lambda i: [ctx.keyswitch(ws, x[0], x[1], x[2], key, stream) for x in ks_items], kb) / kb
     del items, ks_items, wsb
 
@@ -562,9 +573,13 @@ def run_ours(args):
                       "bfv_n15_mult_relin_loop128_ops_per_s": 128 * world / t_bloop,
                       "bfv_n15_mult_relin_loop128_cuda_core_ops_per_s": 128 * world / t_bloop_cc,
                       "bfv_n15_tuning": btuning,
-                      "batch64_uneven_levels_ops_per_s": 64 * world / t_batch,
+                      "batch64_uneven_levels_ops_per_s": 64 * world / min(t_batch.values()),
+                      "batch64_uneven_levels_fused_ops_per_s": 64 * world / t_batch[True],
+                      "batch64_uneven_levels_unfused_ops_per_s": 64 * world / t_batch[False],
                       "batch64_as_single_calls_ops_per_s": 64 * world / t_loop,
-                      "keyswitch_batch64_uneven_levels_per_s": 64 * world / t_ksb,
+                      "keyswitch_batch64_uneven_levels_per_s": 64 * world / min(t_ksb.values()),
+                      "keyswitch_batch64_uneven_levels_fused_per_s": 64 * world / t_ksb[True],
+                      "keyswitch_batch64_uneven_levels_unfused_per_s": 64 * world / t_ksb[False],
                       "keyswitch_batch64_as_single_calls_per_s": 64 * world / t_ksl,
                       "hrotate_step1_per_s": k2 * world / t_rot, "keyswitch_per_s": k2 * world / t_ks,
                       "tensor_core_bconv": tc_default, "tensor_core_status": tc_status,

@@ -139,9 +139,10 @@ int fhe_context_set_launch_overlap(fhe_context *ctx, int enable);
 /* The mod-up's forward NTT row pass fused with the key-switching inner product (on by default):
  * one kernel finishes each digit's transform tile by tile and accumulates it against the key, so
  * the mod-up output (src/rns_bconv.cu:530-628) is never written to or read back from device
- * memory.  Used by the key switch, relinearisation, HMult and Galois calls; hoisted rotations keep
- * the materialised mod-up (they reuse it).  Every setting gives the same words.  No counterpart in
- * the reference. */
+ * memory.  Used by the key switch, relinearisation, HMult, Galois and batched calls (in a batch,
+ * the blocks of every ciphertext that read one key tile run together); hoisted rotations keep
+ * the materialised mod-up (they reuse it).  Every setting gives the same words.  No counterpart
+ * in the reference. */
 int fhe_context_fused_keyswitch(const fhe_context *ctx);
 int fhe_context_set_fused_keyswitch(fhe_context *ctx, int enable);
 

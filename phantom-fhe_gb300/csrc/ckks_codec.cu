@@ -8,9 +8,10 @@
 //           Re z_k) for k < N/2, round(Im z_{k - N/2}) above -> residues mod q_i -> forward NTT;
 //   decode: inverse NTT -> CRT compose of every coefficient into a multi-word integer mod Q_l,
 //           centred and scaled by 1 / scale in FP64 -> forward special FFT -> bit-reversed order.
-// Every butterfly, scale and accumulation is the reference's own FP64 operation in its order
-// (cuComplex's cuCmul / cuCadd / cuCsub, the same twiddle table), so encoded words and decoded
-// slots equal the reference's bit for bit.  The integer parts are exact: a coefficient's residue
+// Every butterfly, scale and accumulation is the reference's own FP64 operation in its order and
+// in the contraction its compiled kernels use (written out with explicit round-to-nearest
+// intrinsics; the same twiddle table), so encoded words and decoded slots equal the reference's
+// bit for bit.  The integer parts are exact: a coefficient's residue
 // is its exact value mod q_i (any magnitude a double holds), and negative values map to
 // q_i - (|c| mod q_i) as the reference does (which gives q_i, not 0, for a multiple of q_i; the
 // forward NTT takes it as a lazy input and returns the canonical transform).
@@ -44,13 +45,48 @@ __global__ void codec_bitrev(cuDoubleComplex *dst, const cuDoubleComplex *src, u
         dst[brev_bits(i, log_slots)] = src[i];
 }
 
+// Complex product a * b with every FP64 operation written out, so that no compiler contraction
+// can change a rounding.  Real part: form 0 fma(a.x, b.x, -(a.y b.y)), form 1 fma(-a.y, b.y,
+// a.x b.x), form 2 a.x b.x - a.y b.y; imaginary part: form 0 fma(a.x, b.y, a.y b.x), form 1
+// fma(a.y, b.x, a.x b.y), form 2 a.x b.y + a.y b.x (each product rounded where it is not fused).
+template <int RE, int IM>
+__device__ __forceinline__ cuDoubleComplex cmul_form(cuDoubleComplex a, cuDoubleComplex b) {
+    double re, im;
+    if constexpr (RE == 0)
+        re = __fma_rn(a.x, b.x, -__dmul_rn(a.y, b.y));
+    else if constexpr (RE == 1)
+        re = __fma_rn(-a.y, b.y, __dmul_rn(a.x, b.x));
+    else
+        re = __dsub_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y));
+    if constexpr (IM == 0)
+        im = __fma_rn(a.x, b.y, __dmul_rn(a.y, b.x));
+    else if constexpr (IM == 1)
+        im = __fma_rn(a.y, b.x, __dmul_rn(a.x, b.y));
+    else
+        im = __dadd_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x));
+    return make_cuDoubleComplex(re, im);
+}
+
+// The reference runs its special FFT as two kernels (src/fft.cu:90-340): stages of a block of up
+// to 2048 slots in shared memory (`base`) and, above 2048 slots, single global stages (`iter`).
+// Compiled separately, the two evaluate the complex product of a butterfly with different FMA
+// contractions, and the decoded doubles carry that difference.  Each form below is the one
+// measured on the reference's compiled kernels (the same butterfly on seeded inputs, compared
+// with exact evaluations of every candidate), and each stage here uses the form of the kernel
+// that runs that stage in the reference.
+constexpr int kFftBaseRe = 0, kFftBaseIm = 1;
+constexpr int kFftIterRe = 0, kFftIterIm = 0;
+constexpr int kIfftBaseRe = 0, kIfftBaseIm = 1;
+constexpr int kIfftIterRe = 0, kIfftIterIm = 0;
+constexpr int kFftBlockLog = 11;  // slots handled by the reference's shared-memory kernel: 2^11
+
 // One stage `iter` of the special FFT over `slots` values (slots / 2 butterflies).  Butterfly
 // tid pairs g = 2 k 2^lp + j and g + 2^lp (lp = log_slots - iter - 1, k = tid >> lp, j = tid mod
 // 2^lp); its twiddle index is 5^r 2^lp mod 2N with r the bit-reversed k << lp (src/fft.cu:106-126).
 // Forward (decode): Cooley-Tukey, x0 + w x1, x0 - w x1 with w = roots[idx].  Inverse (encode):
 // Gentleman-Sande, x0 + x1, (x0 - x1) w with w = roots[2N - idx]; the last stage (iter 0)
 // multiplies both outputs by `scalar` when it is nonzero (src/fft.cu:209-277).
-template <bool FWD>
+template <bool FWD, int RE, int IM>
 __global__ void codec_fft_stage(cuDoubleComplex *x, const cuDoubleComplex *roots, const uint32_t *group,
                                 uint32_t slots, int log_slots, int iter, uint32_t m, double scalar) {
     const int lp = log_slots - iter - 1;
@@ -62,17 +98,16 @@ __global__ void codec_fft_stage(cuDoubleComplex *x, const cuDoubleComplex *roots
         psi = (psi << lp) & (m - 1);
         const cuDoubleComplex x0 = x[g], x1 = x[g + pairs];
         if constexpr (FWD) {
-            const cuDoubleComplex w = roots[psi];
-            const cuDoubleComplex s1 = cuCmul(x1, w);
-            x[g] = cuCadd(x0, s1);
-            x[g + pairs] = cuCsub(x0, s1);
+            const cuDoubleComplex s1 = cmul_form<RE, IM>(x1, roots[psi]);
+            x[g] = make_cuDoubleComplex(__dadd_rn(x0.x, s1.x), __dadd_rn(x0.y, s1.y));
+            x[g + pairs] = make_cuDoubleComplex(__dsub_rn(x0.x, s1.x), __dsub_rn(x0.y, s1.y));
         } else {
-            const cuDoubleComplex w = roots[m - psi];
-            cuDoubleComplex y0 = cuCadd(x0, x1);
-            cuDoubleComplex y1 = cuCmul(cuCsub(x0, x1), w);
+            cuDoubleComplex y0 = make_cuDoubleComplex(__dadd_rn(x0.x, x1.x), __dadd_rn(x0.y, x1.y));
+            cuDoubleComplex y1 = cmul_form<RE, IM>(make_cuDoubleComplex(__dsub_rn(x0.x, x1.x), __dsub_rn(x0.y, x1.y)),
+                                                   roots[m - psi]);
             if (iter == 0 && scalar != 0.0) {
-                y0 = make_cuDoubleComplex(y0.x * scalar, y0.y * scalar);
-                y1 = make_cuDoubleComplex(y1.x * scalar, y1.y * scalar);
+                y0 = make_cuDoubleComplex(__dmul_rn(y0.x, scalar), __dmul_rn(y0.y, scalar));
+                y1 = make_cuDoubleComplex(__dmul_rn(y1.x, scalar), __dmul_rn(y1.y, scalar));
             }
             x[g] = y0;
             x[g + pairs] = y1;
@@ -178,21 +213,23 @@ __global__ void codec_compose(cuDoubleComplex *x, const uint64_t *src, const Mod
                 upper_half = acc[w] > upper[w];
                 break;
             }
+        // each term rounded on its own, then added (the reference's compiled form: no fused
+        // multiply-add here, measured with a scale that is not a power of two)
         double res = 0.0, scaled = inv_scale;
         if (upper_half) {
-            for (int w = 0; w < l; w++, scaled *= 18446744073709551616.0) {
+            for (int w = 0; w < l; w++, scaled = __dmul_rn(scaled, 18446744073709551616.0)) {
                 if (acc[w] > q_prod[w]) {
                     const uint64_t diff = acc[w] - q_prod[w];
-                    res += diff ? static_cast<double>(diff) * scaled : 0.0;
+                    res = __dadd_rn(res, diff ? __dmul_rn(static_cast<double>(diff), scaled) : 0.0);
                 } else {
                     const uint64_t diff = q_prod[w] - acc[w];
-                    res -= diff ? static_cast<double>(diff) * scaled : 0.0;
+                    res = __dsub_rn(res, diff ? __dmul_rn(static_cast<double>(diff), scaled) : 0.0);
                 }
             }
         } else {
-            for (int w = 0; w < l; w++, scaled *= 18446744073709551616.0) {
+            for (int w = 0; w < l; w++, scaled = __dmul_rn(scaled, 18446744073709551616.0)) {
                 const uint64_t diff = acc[w];
-                res += diff ? static_cast<double>(diff) * scaled : 0.0;
+                res = __dadd_rn(res, diff ? __dmul_rn(static_cast<double>(diff), scaled) : 0.0);
             }
         }
         if (c < slots)
@@ -216,13 +253,27 @@ void fft_stages(const Context &c, cuDoubleComplex *x, bool fwd, double scalar, c
     const auto *roots = c.codec_roots.as<cuDoubleComplex>();
     const auto *group = c.codec_group.as<uint32_t>();
     const int g = codec_grid(slots / 2);
+    // stages iter < log_slots - 11 run in the reference's global-stage kernels, the rest in its
+    // shared-memory kernels (src/fft.cu:340-413)
+    const int split = log_slots - kFftBlockLog;
     for (int k = 0; k < log_slots; k++) {
         count_launch();
-        if (fwd)
-            codec_fft_stage<true><<<g, kCodecBlock, 0, s>>>(x, roots, group, slots, log_slots, k, m, 0.0);
-        else
-            codec_fft_stage<false><<<g, kCodecBlock, 0, s>>>(x, roots, group, slots, log_slots, log_slots - 1 - k,
-                                                            m, scalar);
+        if (fwd) {
+            if (k < split)
+                codec_fft_stage<true, kFftIterRe, kFftIterIm><<<g, kCodecBlock, 0, s>>>(x, roots, group, slots,
+                                                                                       log_slots, k, m, 0.0);
+            else
+                codec_fft_stage<true, kFftBaseRe, kFftBaseIm><<<g, kCodecBlock, 0, s>>>(x, roots, group, slots,
+                                                                                       log_slots, k, m, 0.0);
+        } else {
+            const int it = log_slots - 1 - k;
+            if (it < split)
+                codec_fft_stage<false, kIfftIterRe, kIfftIterIm><<<g, kCodecBlock, 0, s>>>(x, roots, group, slots,
+                                                                                          log_slots, it, m, scalar);
+            else
+                codec_fft_stage<false, kIfftBaseRe, kIfftBaseIm><<<g, kCodecBlock, 0, s>>>(x, roots, group, slots,
+                                                                                          log_slots, it, m, scalar);
+        }
     }
 }
 

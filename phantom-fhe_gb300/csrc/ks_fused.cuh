@@ -24,26 +24,33 @@ namespace pfg {
 constexpr int kFusedE = 8;       // coefficients per thread
 constexpr int kFusedTile = 1024; // coefficients per CTA (128 threads)
 
+// Shared-memory words of one CTA: its tile as V = TILE / M padded vectors of M = 2^LM words.
+template <int LM>
+__host__ __device__ constexpr int fused_smem_words() {
+    return (kFusedTile >> LM) * ((1 << LM) + (1 << LM) / 16 + 1);
+}
+
+// One CTA's work: output limb jj (prime table index tbl) of the rows in tile `tile`, over every
+// digit d < beta.  tm and cx are the ciphertext's mod-up and accumulator buffers, sm the CTA's
+// shared tile.
 template <int LM, class Own>
-__global__ void __launch_bounds__(kFusedTile / kFusedE, 4)
-        ks_modup_ip(NttTables T, const uint64_t *tm, Own own, const uint64_t *const *evk, uint64_t *cx, int l,
-                    int nQ, int alpha, int beta, int qp) {
-    pdl_wait();
-    pdl_release();
+__device__ __forceinline__ void modup_ip_tile(uint64_t *sm, const NttTables &T, const uint64_t *tm, const Own &own,
+                                              const uint64_t *const *evk, uint64_t *cx, int l, int nQ, int alpha,
+                                              int beta, int qp, int jj, uint32_t tile) {
     constexpr int E = kFusedE, TILE = kFusedTile;
     constexpr int M = 1 << LM, TPV = M / E, V = TILE / M, VP = M + M / 16 + 1;
     using F = PhaseAt<LM, true, 0, E>;
     using L = PhaseAt<LM, true, F::NPH - 1, E>;
     constexpr int LG = E >> L::K, LS = 1 << L::K;  // last phase: groups per thread, group size
     static_assert(LS % 2 == 0, "the last phase pairs consecutive positions");
-    __shared__ uint64_t sm[V * VP];
+    static_assert(V * VP == fused_smem_words<LM>(), "shared tile size");
     const int log_n = T.log_n;
-    const int qlp = l + alpha, jj = (int)blockIdx.y;
+    const int qlp = l + alpha;
     const int tbl = jj < l ? jj : nQ + (jj - l);
     const Mod md = T.mods[tbl];
     const int vv = threadIdx.x / TPV, u = threadIdx.x % TPV;
-    const uint32_t row = blockIdx.x * V + vv;
-    const uint32_t vbase = blockIdx.x * TILE + vv * M;  // this thread's row within the limb
+    const uint32_t row = tile * V + vv;
+    const uint32_t vbase = tile * TILE + vv * M;  // this thread's row within the limb
     uint64_t *vec = sm + vv * VP;
     const int own_d = jj < l ? jj / alpha : -1;
     const TwPair *tw = T.tw + ((size_t)tbl << log_n);
@@ -112,6 +119,17 @@ __global__ void __launch_bounds__(kFusedTile / kFusedE, 4)
             *reinterpret_cast<ulonglong2 *>(c0 + total + idx) =
                     make_ulonglong2(reduce128(a1[i], md), reduce128(a1[i + 1], md));
         }
+}
+
+// One ciphertext: grid (N / TILE row tiles, l + alpha output limbs).
+template <int LM, class Own>
+__global__ void __launch_bounds__(kFusedTile / kFusedE, 4)
+        ks_modup_ip(NttTables T, const uint64_t *tm, Own own, const uint64_t *const *evk, uint64_t *cx, int l,
+                    int nQ, int alpha, int beta, int qp) {
+    pdl_wait();
+    pdl_release();
+    __shared__ uint64_t sm[fused_smem_words<LM>()];
+    modup_ip_tile<LM>(sm, T, tm, own, evk, cx, l, nQ, alpha, beta, qp, (int)blockIdx.y, blockIdx.x);
 }
 
 }  // namespace pfg

@@ -24,6 +24,19 @@ struct SeqMap {
     }
 };
 
+// The same data with the blocks ordered limb-major: consecutive blockIdx.y values take the
+// same limb of successive polynomials, so the CTAs in flight share one limb's twiddle table
+// (1 MB at N = 2^16) in L2 instead of cycling through every limb's.
+struct LimbMajorMap {
+    int polys, start;
+    __device__ __forceinline__ bool operator()(int b, int &poly, int &k, int &tbl) const {
+        k = b / polys;
+        poly = b % polys;
+        tbl = start + k;
+        return true;
+    }
+};
+
 // QlP limbs [0, l + alpha) of `polys` polynomials at level l, starting at limb k0.
 struct QlpMap {
     int limbs, k0, l, nQ;

@@ -12,6 +12,7 @@
 // single call's word for word.
 #include "bconv.cuh"
 #include "bconv_tc.cuh"
+#include "ks_fused.cuh"
 #include "launch.cuh"
 #include "ops.hpp"
 
@@ -381,6 +382,37 @@ __global__ void __launch_bounds__(256) ks_inner_product_batch(BItemsRef r, const
     }
 }
 
+// The own-limb term of item c's mod-up: HMult's d2 = a1 * b1, or the key switch's c2.
+struct BatchOwn {
+    const uint64_t *a, *b;
+    long long lps;  // offset of polynomial 1 (HMult)
+    int keyswitch, log_n;
+    __device__ __forceinline__ uint64_t operator()(int jj, const Mod &m, uint32_t idx) const {
+        const size_t o = ((size_t)jj << log_n) + idx;
+        if (keyswitch) return b[o];
+        return mul_mod(a[lps + o], b[lps + o], m);
+    }
+};
+
+// Mod-up row pass fused with the inner product for every item (ks_fused.cuh): block (c, tile,
+// tk) is item c's output limb for key limb tk over one row tile, idle where item c's level has
+// dropped q_tk.  The item index is the fastest grid dimension, so the blocks of all items that
+// read the same key tile (tk, tile) run together and the key comes from HBM once per batch.
+template <int LM>
+__global__ void __launch_bounds__(kFusedTile / kFusedE, 4)
+        ks_modup_ip_batch(BItemsRef r, NttTables T, const uint64_t *const *evk, int nQ, int qp) {
+    pdl_wait();
+    pdl_release();
+    __shared__ uint64_t sm[fused_smem_words<LM>()];
+    const int c = (int)blockIdx.x, tk = (int)blockIdx.z, l = r.it.l[c], alpha = r.alpha, log_n = r.log_n;
+    if (tk < nQ && tk >= l) return;  // uniform per block, before any barrier
+    const int jj = tk < nQ ? tk : l + (tk - nQ);
+    uint64_t *ws = r.it.ws[c];
+    const BatchOwn own{r.it.a[c], r.it.b[c], (long long)l << log_n, r.it.keyswitch, log_n};
+    modup_ip_tile<LM>(sm, T, ws + r.sl.tm, own, evk, ws + r.sl.cx, l, nQ, alpha, (l + alpha - 1) / alpha, qp, jj,
+                      blockIdx.y);
+}
+
 // Rescale-folded mod-down conversion for (item, poly) = block row (see rescale_fused_bconv).
 template <int A>
 __global__ void __launch_bounds__(256) rescale_bconv_batch(BItemsRef r, Prefix pre, const uint64_t *pmat,
@@ -515,6 +547,35 @@ static Prefix make_prefix(int count, F per_item) {
     return p;
 }
 
+// Steps 3 (mod-up forward NTT) and 4 (inner product) of every item: fused (column pass, then the
+// fused row pass + inner product) or as separate kernels; the same words.
+static void batch_modup_ntt_inner_product(const Context &c, const BItemsRef &r, const std::vector<int> &lv,
+                                          const uint64_t *const *evk, cudaStream_t s) {
+    const int count = r.it.count, alpha = c.nP, nQ = c.nQ;
+    BModupMap mm{make_prefix(count, [&](int i) { return c.beta(lv[i]) * (lv[i] + alpha); }), {}, nQ, alpha};
+    for (int i = 0; i < count; i++) mm.l[i] = lv[i];
+    BScratch<1> tm{r};
+    if (c.ks_fused) {
+        col_pass<true, false>(c, mm.pre.p[count], mm, tm, tm, s);
+        const dim3 grid((unsigned)count, (unsigned)(c.n / kFusedTile), (unsigned)(nQ + alpha));
+        const NttTables T = c.ntt();
+        count_launch();
+        switch (c.l2()) {
+            case 6: launch_pdl(c.pdl, ks_modup_ip_batch<6>, grid, dim3(kFusedTile / kFusedE), 0, s, r, T, evk, nQ, nQ + alpha); break;
+            case 7: launch_pdl(c.pdl, ks_modup_ip_batch<7>, grid, dim3(kFusedTile / kFusedE), 0, s, r, T, evk, nQ, nQ + alpha); break;
+            case 8: launch_pdl(c.pdl, ks_modup_ip_batch<8>, grid, dim3(kFusedTile / kFusedE), 0, s, r, T, evk, nQ, nQ + alpha); break;
+            case 9: launch_pdl(c.pdl, ks_modup_ip_batch<9>, grid, dim3(kFusedTile / kFusedE), 0, s, r, T, evk, nQ, nQ + alpha); break;
+            default: throw std::logic_error("unsupported NTT split");
+        }
+        return;
+    }
+    ntt_fwd2(c, mm.pre.p[count], mm, tm, tm, tm, tm, s);
+    const unsigned gx = (unsigned)std::max<uint64_t>(1, c.n / 512);
+    count_launch();
+    launch_pdl(c.pdl, ks_inner_product_batch, dim3(gx, (unsigned)(nQ + alpha)), dim3(256), 0, s, r, evk,
+               c.d_mods.as<Mod>(), nQ, nQ + alpha);
+}
+
 void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t item_words,
                                   const std::vector<BatchItem> &items, const uint64_t *const *rlk, cudaStream_t s) {
     const Mod *mods = c.d_mods.as<Mod>();
@@ -582,16 +643,8 @@ void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t it
                 });
             }
         }
-        // 3. mod-up forward NTT of every digit's complement limbs
-        {
-            BModupMap mm{make_prefix(count, [&](int i) { return beta_of(i) * (lvl(i) + alpha); }), {}, nQ, alpha};
-            for (int i = 0; i < count; i++) mm.l[i] = lvl(i);
-            BScratch<1> tm{r};
-            ntt_fwd2(c, mm.pre.p[count], mm, tm, tm, tm, tm, s);
-        }
-        // 4. inner product, one block row per key limb
-        count_launch();
-        launch_pdl(c.pdl, ks_inner_product_batch, dim3(dim3(gx, (unsigned)(nQ + alpha))), dim3(256), 0, s, r, rlk, mods, nQ, nQ + alpha);
+        // 3-4. mod-up forward NTT of every digit's complement limbs and the inner product
+        batch_modup_ntt_inner_product(c, r, std::vector<int>(r.it.l, r.it.l + count), rlk, s);
         // 5. inverse NTT of the P limbs (x PHatInv), cx limb l-1 and tensor limb l-1
         {
             BLastLimbMap lm{make_prefix(count, [&](int) { return 2 * (alpha + 2); }), {}, nQ, alpha};
@@ -704,15 +757,8 @@ void ckks_keyswitch_batch(const Context &c, uint64_t *ws_base, size_t item_words
             tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, pre.p[count], mods, c.p_inv.as<uint64_t>(),
                                    c.d_status.as<unsigned>(), s, c.pdl);
         }
-        {
-            BModupMap mm{make_prefix(count, [&](int i) { return beta_of(i) * (lvl(i) + alpha); }), {}, nQ, alpha};
-            for (int i = 0; i < count; i++) mm.l[i] = lvl(i);
-            BScratch<1> tm{r};
-            ntt_fwd2(c, mm.pre.p[count], mm, tm, tm, tm, tm, s);
-        }
-        // 4. inner product, one block row per key limb
-        count_launch();
-        launch_pdl(c.pdl, ks_inner_product_batch, dim3(dim3(gx, (unsigned)(nQ + alpha))), dim3(256), 0, s, r, evk, mods, nQ, nQ + alpha);
+        // 4. (with the mod-up's forward NTT) inner product
+        batch_modup_ntt_inner_product(c, r, std::vector<int>(r.it.l, r.it.l + count), evk, s);
         // 5. inverse NTT of the P limbs of both cx polynomials, times PHatInv
         {
             BPMap pm{make_prefix(count, [&](int) { return 2 * alpha; }), alpha, nQ};

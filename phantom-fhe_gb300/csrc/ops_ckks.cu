@@ -66,14 +66,14 @@ void ntt_forward(const Context &c, uint64_t *data, int polys, int limbs, int sta
     if (c.log_n == 12) return ntt_n12_launch<true>(c, data, polys, limbs, start, s);
     const long long ps = (long long)limbs << c.log_n;
     PtrStore st{data, ps, c.log_n};
-    ntt_fwd(c, polys * limbs, SeqMap{limbs, start}, PtrLoad{data, ps, c.log_n}, st, st, s);
+    ntt_fwd(c, polys * limbs, LimbMajorMap{polys, start}, PtrLoad{data, ps, c.log_n}, st, st, s);
 }
 
 void ntt_inverse(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s) {
     if (c.log_n == 12) return ntt_n12_launch<false>(c, data, polys, limbs, start, s);
     const long long ps = (long long)limbs << c.log_n;
     PtrStore st{data, ps, c.log_n};
-    ntt_inv(c, polys * limbs, SeqMap{limbs, start}, PtrLoad{data, ps, c.log_n}, st, st, s);
+    ntt_inv(c, polys * limbs, LimbMajorMap{polys, start}, PtrLoad{data, ps, c.log_n}, st, st, s);
 }
 
 // ------------------------------------------------------------------ functors

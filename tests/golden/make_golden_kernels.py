@@ -1272,6 +1272,10 @@ def extra_cases(K):
         "codec_n16_l30_w128": case_codec(K, 16, [60] + [40] * 29 + [60] * 5, 5, 30, 2.0 ** 80, 32768, 1611),
         "codec_n16_l30_wide": case_codec(K, 16, [60] + [40] * 29 + [60] * 5, 5, 30, 2.0 ** 150, 20000, 1612),
         "codec_n16_l20_a4": case_codec(K, 16, [60] + [40] * 19 + [60] * 4, 4, 20, 2.0 ** 40, 32768, 1613),
+        # a scale that is not a power of two: every FP64 product of the compose and the FFT rounds
+        "codec_n16_l20_oddscale": case_codec(K, 16, [60] + [40] * 19 + [60] * 4, 4, 20, 1.2345 * 2.0 ** 40, 32768,
+                                             1614),
+        "codec_n12_l5_oddscale": case_codec(K, 12, [60, 40, 40, 40, 40, 60, 60], 2, 5, 0.7071 * 2.0 ** 40, 2048, 1219),
     }
 
 

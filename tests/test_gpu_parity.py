@@ -416,14 +416,22 @@ def _batch_case(pg, ctx, mods, chains, seed):
     return key, k, items, host
 
 
-def test_batch_multiply_relin_rescale_uneven_levels_small(small, pg):
+@pytest.mark.parametrize("fused", [True, False])
+def test_batch_multiply_relin_rescale_uneven_levels_small(small, pg, fused):
+    """Both forms of the batched mod-up + inner product: the row pass fused with the inner
+    product (key tiles shared by the items through L2) and the two-kernel form."""
     ctx, oc, mods, nq, ws = small
     chains = [1, 5, 3, 2, 4, 1, 3]
     key, k, items, host = _batch_case(pg, ctx, mods, chains, 90)
     wsb = ctx.workspace(batch_items=len(chains))
-    ctx.multiply_relin_rescale_batch(wsb, items, k)
+    ctx.fused_keyswitch = fused
+    try:
+        ctx.multiply_relin_rescale_batch(wsb, items, k)
+    finally:
+        ctx.fused_keyswitch = True
     for (a, b, l), (_, _, out, ch) in zip(host, items):
-        _eq(out, oc.rescale(l, oc.ckks_mul_relin(l, a, b, key)), f"batch item at chain {ch}")
+        _eq(out, oc.rescale(l, oc.ckks_mul_relin(l, a, b, key)), f"batch item at chain {ch}, fused={fused}")
+    assert ctx.device_status() == 0
 
 
 def test_batch_more_than_one_launch_set(small, pg):
@@ -464,14 +472,19 @@ def _ks_batch_case(pg, ctx, mods, chains, seed):
     return key, pg.KeySwitchKey(pg.to_device(key)), items, host
 
 
-def test_keyswitch_batch_uneven_levels(small, pg):
+@pytest.mark.parametrize("fused", [True, False])
+def test_keyswitch_batch_uneven_levels(small, pg, fused):
     ctx, oc, mods, nq, ws = small
     chains = [1, 5, 3, 2, 4, 1, 6, 3]
     key, k, items, host = _ks_batch_case(pg, ctx, mods, chains, 95)
     wsb = ctx.workspace(batch_items=len(chains))
-    ctx.keyswitch_batch(wsb, items, k)
+    ctx.fused_keyswitch = fused
+    try:
+        ctx.keyswitch_batch(wsb, items, k)
+    finally:
+        ctx.fused_keyswitch = True
     for (ct, c2, l), (t, _, ch) in zip(host, items):
-        _eq(t, oc.keyswitch(l, ct, c2, key), f"batched key switch at chain {ch}")
+        _eq(t, oc.keyswitch(l, ct, c2, key), f"batched key switch at chain {ch}, fused={fused}")
     assert ctx.device_status() == 0
 
 
