@@ -234,11 +234,23 @@ def matvec_bench(pg, torch, timed, stream, rank, profile_only=False):
         for (ct, chain, lv), o in zip(cts, outs):
             ctx.bsgs_matvec(ws, scratch, ct, chain, diags_at[lv], d, G, B, gks, o, hoisted=hoisted, stream=stream)
 
+    # the same 32 products through the batched call: one launch per pipeline step for all of them
+    wsb = ctx.workspace(batch_items=MV_BATCH)
+    bscratch = torch.empty(MV_BATCH * ctx.bsgs_scratch_bytes(G) // 8, dtype=torch.int64, device="cuda")
+    bouts = [torch.empty_like(o) for o in outs]
+    bitems = [(ct, chain, diags_at[lv], o) for (ct, chain, lv), o in zip(cts, bouts)]
+
+    def batched():
+        ctx.bsgs_matvec_batch(wsb, bscratch, bitems, d, G, B, gks, stream=stream)
+
     batch(True)
     if profile_only:
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_push("matvec_case")  # lets a profiler skip the setup's launches
-        batch(True)
+        if os.environ.get("BENCH_MATVEC_BATCHED", "0") == "1":
+            batched()
+        else:
+            batch(True)
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
         return {}
@@ -252,6 +264,13 @@ def matvec_bench(pg, torch, timed, stream, rank, profile_only=False):
         y = enc.decode(ctx, sk.decrypt(o, chain + 1), scale * scale / mods[lv - 1], chain + 1)
         errs.append(float(np.max(np.abs(y - np.tile(M @ x, S // d)))))
     err_h = max(errs)
+    batched()
+    torch.cuda.synchronize()
+    same = all(torch.equal(a, b) for a, b in zip(outs, bouts))
+    l0 = pg.lib.fhe_kernel_launches()
+    t_b = timed(lambda i: batched(), k) / k
+    launches_b = (pg.lib.fhe_kernel_launches() - l0) / k
+    del bscratch, wsb
     batch(False)
     t_x = timed(lambda i: batch(False), k) / k
     errs = []
@@ -259,6 +278,9 @@ def matvec_bench(pg, torch, timed, stream, rank, profile_only=False):
         y = enc.decode(ctx, sk.decrypt(o, chain + 1), scale * scale / mods[lv - 1], chain + 1)
         errs.append(float(np.max(np.abs(y - np.tile(M @ x, S // d)))))
     return {"matvec128_batch32_uneven_hoisted_per_s": MV_BATCH / t_h,
+            "matvec128_batch32_uneven_batched_per_s": MV_BATCH / t_b,
+            "matvec128_batched_launches_per_batch": launches_b,
+            "matvec128_batched_equals_single_calls": same,
             "matvec128_batch32_uneven_reference_loop_per_s": MV_BATCH / t_x,
             "matvec128_hoisted_max_slot_error": err_h,
             "matvec128_reference_loop_max_slot_error": max(errs),

@@ -321,6 +321,24 @@ int fhe_ckks_bsgs_matvec(const fhe_context *ctx, fhe_workspace *ws, uint64_t *sc
                          size_t chain_index, const uint64_t *diags, size_t D, size_t G, size_t B,
                          const uint64_t *const *const *galois_keys, uint64_t *out, int hoisted, void *stream);
 
+/* A batch of matrix-vector products of the hoisted form above (baby steps sharing one mod-up,
+ * giant steps by Horner's rule with rotations by G), one per ciphertext, at their own chain
+ * indices (uneven levels allowed), sharing the Galois keys.  The reference serves such a batch
+ * as a host loop of bsgs_complete_from_cpu (python/src/binding.cu:507-595); here every pipeline
+ * step is one launch over up to 64 products, so each key is read once per launch set.  Each
+ * output equals fhe_ckks_bsgs_matvec(..., hoisted = 1) word for word.  ws must come from
+ * fhe_workspace_create_batch with at least min(count, 64) slots; scratch holds min(count, 64) x
+ * fhe_bsgs_scratch_bytes(ctx, G) bytes. */
+typedef struct fhe_matvec_item {
+    const uint64_t *ct;     /* 2 polys at chain_index, NTT form */
+    const uint64_t *diags;  /* D plaintexts [D][limbs at chain_index][N], NTT form */
+    uint64_t *out;          /* 2 polys at chain_index + 1 */
+    size_t chain_index;
+} fhe_matvec_item;
+int fhe_ckks_bsgs_matvec_batch(const fhe_context *ctx, fhe_workspace *ws, uint64_t *scratch,
+                               const fhe_matvec_item *items, size_t count, size_t D, size_t G, size_t B,
+                               const uint64_t *const *const *galois_keys, void *stream);
+
 /* PhantomSecretKey::encrypt_symmetric, CKKS (src/secretkey.cu:463-500 with
  * encrypt_zero_symmetric, 232-295) with the randomness supplied by the caller instead of the
  * reference's device PRNG: out = (pt - (a*s + NTT(e)), a).  s and a in NTT form over the

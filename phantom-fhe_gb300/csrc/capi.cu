@@ -655,6 +655,36 @@ int fhe_ckks_bsgs_matvec(const fhe_context *ctx, fhe_workspace *ws, uint64_t *sc
     });
 }
 
+int fhe_ckks_bsgs_matvec_batch(const fhe_context *ctx, fhe_workspace *ws, uint64_t *scratch,
+                               const fhe_matvec_item *items, size_t count, size_t D, size_t G, size_t B,
+                               const uint64_t *const *const *galois_keys, void *stream) {
+    return guarded([&] {
+        pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
+        pfg::Workspace w = ws_of(ctx, ws);
+        if (c.scheme != pfg::kSchemeCKKS) throw std::invalid_argument("matrix-vector product: CKKS only");
+        need_keyswitching(c);
+        need_ptr(scratch, "scratch");
+        need_ptr(items, "items");
+        need_ptr(galois_keys, "galois_keys");
+        if (D == 0 || G == 0 || B == 0 || G * B < D) throw std::invalid_argument("need D > 0 and G * B >= D");
+        if (G > 256) throw std::invalid_argument("too many baby steps");
+        if (count == 0) return;
+        if (ws->items < std::min<size_t>(count, pfg::kBatchLaunch))
+            throw std::invalid_argument("workspace has too few ciphertext slots for this batch");
+        std::vector<pfg::MatvecItem> v;
+        for (size_t i = 0; i < count; i++) {
+            need_ptr(items[i].ct, "items[i].ct");
+            need_ptr(items[i].diags, "items[i].diags");
+            need_ptr(items[i].out, "items[i].out");
+            const int l = level_of(c, items[i].chain_index);
+            if (l < 2) throw std::invalid_argument("end of modulus switching chain reached");
+            v.push_back(pfg::MatvecItem{items[i].ct, items[i].diags, items[i].out, l});
+        }
+        pfg::ckks_bsgs_matvec_batch(c, w.base, ws->words / ws->items, scratch, pfg::bsgs_scratch_words(c, (int)G), v,
+                                    (int)D, (int)G, (int)B, galois_keys, st(stream));
+    });
+}
+
 int fhe_ckks_encrypt_symmetric(const fhe_context *ctx, const uint64_t *pt, const uint64_t *s_ntt, const uint64_t *a,
                                const int64_t *e, uint64_t *out, size_t chain_index, void *stream) {
     return guarded([&] {

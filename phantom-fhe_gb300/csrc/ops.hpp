@@ -36,6 +36,13 @@ struct KsItem {  // one key switch of a batch: ct (2 polys, in place) += KeySwit
     int l;
 };
 
+struct MatvecItem {  // one matrix-vector product of a batch: ct (2 polys) and diags [D][l][N] at level l
+    const uint64_t *ct;
+    const uint64_t *diags;
+    uint64_t *out;  // 2 polys at level l - 1
+    int l;
+};
+
 void ntt_forward(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s);
 void ntt_inverse(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s);
 
@@ -52,6 +59,9 @@ void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t it
                                   const std::vector<BatchItem> &items, const uint64_t *const *rlk, cudaStream_t s);
 void ckks_keyswitch_batch(const Context &c, uint64_t *ws_base, size_t item_words, const std::vector<KsItem> &items,
                           const uint64_t *const *evk, cudaStream_t s);
+void ckks_bsgs_matvec_batch(Context &c, uint64_t *ws_base, size_t item_words, uint64_t *scratch_base,
+                            size_t scratch_words, const std::vector<MatvecItem> &items, int D, int G, int B,
+                            const uint64_t *const *const *galois_keys, cudaStream_t s);
 void ckks_rescale(const Context &c, const Workspace &w, const uint64_t *in, uint64_t *out, int size, int l,
                   cudaStream_t s);
 void ckks_apply_galois(const Context &c, const Workspace &w, uint64_t *ct, int l, const uint32_t *perm,

@@ -12,6 +12,7 @@
 // single call's word for word.
 #include "bconv.cuh"
 #include "bconv_tc.cuh"
+#include "host_tables.hpp"
 #include "ks_fused.cuh"
 #include "launch.cuh"
 #include "ops.hpp"
@@ -24,6 +25,9 @@ constexpr int kSub = 64;  // "poly" argument of batched functors = item * kSub +
 struct BatchItems {
     int count;
     int keyswitch;  // 0: HMult (c2 = a1 * b1, rescale at the end); 1: key switch of (a = ct, b = c2)
+    // key switch combine: 0 out[c] += KeySwitch (in place); 1 out[c] = (g0, 0) + KeySwitch with g0
+    // the item's permuted first polynomial in its scratch region g (a Galois automorphism)
+    int galois;
     int l[kMaxBatch];
     const uint64_t *a[kMaxBatch], *b[kMaxBatch];
     uint64_t *out[kMaxBatch];
@@ -42,8 +46,10 @@ struct Prefix {
 };
 
 // Offsets of the per-item scratch regions (same layout as the single-call workspace).
+// `mid` is where a key switch's mod-down keeps its intermediate polynomials: the mod-up region
+// tm, which is free by then, or h when tm must survive (hoisted rotations share one mod-up).
 struct ScratchLayout {
-    long long y, tm, cx, g, z;
+    long long y, tm, cx, g, z, h, mid;
 };
 
 static ScratchLayout scratch_layout(const Context &c) {
@@ -54,6 +60,8 @@ static ScratchLayout scratch_layout(const Context &c) {
     s.cx = s.tm + beta * qlp * n;
     s.g = s.cx + 2 * qlp * n;
     s.z = s.g + 2 * nQ * n;
+    s.h = s.z + 4 * n;  // [2][nQ][N]
+    s.mid = s.tm;
     return s;
 }
 
@@ -177,11 +185,11 @@ struct BScratch {
         } else if (REGION == 1) {  // tm [beta][qlp][N]
             off = r.sl.tm;
             ss = r.qlp_n(c);
-        } else if (REGION == 2) {  // tm reused as [2][alpha+2][N]
-            off = r.sl.tm;
+        } else if (REGION == 2) {  // the mod-down's region (tm or h) as [2][alpha+2][N]
+            off = r.sl.mid;
             ss = (long long)(r.alpha + 2) << r.log_n;
-        } else {  // tm reused as [2][l - drop][N]
-            off = r.sl.tm;
+        } else {  // the mod-down's region (tm or h) as [2][l - drop][N]
+            off = r.sl.mid;
             ss = (long long)(r.it.l[c] - r.drop) << r.log_n;
         }
         return r.it.ws[c] + off + sub * ss + ((long long)k << r.log_n) + idx;
@@ -241,15 +249,17 @@ __global__ void __launch_bounds__(256) batch_keyswitch_combine(BItemsRef r, Pref
     const int lc = r.it.l[c], log_n = r.log_n;
     const size_t half = (size_t)1 << (log_n - 1), work = (size_t)lc * half;
     const uint64_t *ws = r.it.ws[c];
-    const uint64_t *v = ws + r.sl.tm + t * ((long long)lc << log_n);
+    const uint64_t *v = ws + r.sl.mid + t * ((long long)lc << log_n);
     const uint64_t *cx = ws + r.sl.cx + t * r.qlp_n(c);
     uint64_t *ct = r.it.out[c] + t * ((long long)lc << log_n);
+    // the base: the output itself (in place), or (g0, 0) for an automorphism
+    const uint64_t *base = r.it.galois ? (t == 0 ? ws + r.sl.g : nullptr) : ct;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < work; e += (size_t)gridDim.x * blockDim.x) {
         const int j = (int)(e >> (log_n - 1));
         const size_t o = ((size_t)j << log_n) + 2 * (e & (half - 1));
         const Mod m = mods[j];
         const uint64_t pj = pinv[2 * j], pjs = pinv[2 * j + 1];
-        const ulonglong2 vv = ld2(v + o), cc = ld2(cx + o), b = ld2(ct + o);
+        const ulonglong2 vv = ld2(v + o), cc = ld2(cx + o), b = base ? ld2(base + o) : make_ulonglong2(0, 0);
         st2(ct + o, add_mod(b.x, mul_shoup(sub_mod(cc.x, vv.x, m.q), pj, pjs, m.q), m.q),
             add_mod(b.y, mul_shoup(sub_mod(cc.y, vv.y, m.q), pj, pjs, m.q), m.q));
     }
@@ -691,18 +701,96 @@ void ckks_mul_relin_rescale_batch(const Context &c, uint64_t *ws_base, size_t it
     }
 }
 
+// ------------------------------------------------------------------ key-switch pipeline pieces
+
+// Steps 1-2 of a key switch for every item: y = iNTT(c2) * partQlHatInv, then the tensor-core
+// mod-up conversion into tm (the column pass and the rest follow separately).
+static void batch_modup_convert(const Context &c, const BItemsRef &r, cudaStream_t s) {
+    const Mod *mods = c.d_mods.as<Mod>();
+    const int count = r.it.count;
+    auto lvl = [&](int i) { return r.it.l[i]; };
+    {
+        Prefix pre = make_prefix(count, lvl);
+        BScratch<0> y{r};
+        ntt_inv2(c, pre.p[count], BSeqMap{pre}, BD2Load{r, mods}, y, y, BScaleYStore{r, mods}, s);
+    }
+    Prefix pre = make_prefix(count, [&](int i) { return c.beta(lvl(i)); });
+    BatchModupSrc src{};
+    src.pre = pre;
+    for (int i = 0; i < count; i++) {
+        const LevelTables &lt = *c.levels[lvl(i)];
+        src.ws[i] = r.it.ws[i];
+        src.bmat[i] = lt.tc_modup.as<uint16_t>();
+        src.meta[i] = lt.tc_modup_meta.as<TcOutMeta>();
+        src.nn[i] = lt.tc_modup_nn.as<int>();
+        src.l[i] = lvl(i);
+    }
+    src.y_off = r.sl.y;
+    src.tm_off = r.sl.tm;
+    src.alpha = c.nP;
+    src.log_n = c.log_n;
+    src.kpad = c.tc_kpad;
+    tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, pre.p[count], mods, c.p_inv.as<uint64_t>(),
+                           c.d_status.as<unsigned>(), s, c.pdl);
+}
+
+// Steps 5-7 for every item: the P limbs of cx back to coefficients (x PHatInv), delta = P -> Ql on
+// the tensor cores into the mod-down region, its forward NTT and the combine into out (in place,
+// or from the automorphism's base (g0, 0)).
+static void batch_moddown_combine(const Context &c, const BItemsRef &r, cudaStream_t s) {
+    const Mod *mods = c.d_mods.as<Mod>();
+    const int count = r.it.count, alpha = c.nP, nQ = c.nQ;
+    auto lvl = [&](int i) { return r.it.l[i]; };
+    {
+        BPMap pm{make_prefix(count, [&](int) { return 2 * alpha; }), alpha, nQ};
+        BScratch<2> mid{r};
+        ntt_inv2(c, pm.pre.p[count], pm, BLastLoad{r, mods}, mid, mid, BLastStore{r, c.p_hat_inv.as<uint64_t>(), mods},
+                 s);
+    }
+    {
+        BatchModdownSrc src{};
+        for (int i = 0; i < count; i++) {
+            const LevelTables &lt = *c.levels[lvl(i)];
+            src.ws[i] = r.it.ws[i];
+            src.bmat[i] = lt.tc_moddown.as<uint16_t>();
+            src.meta[i] = lt.tc_moddown_meta.as<TcOutMeta>();
+            src.nn[i] = lt.tc_moddown_nn;
+            src.l[i] = lvl(i);
+        }
+        src.cx_off = r.sl.cx;
+        src.tm_off = r.sl.mid;
+        src.alpha = alpha;
+        src.log_n = c.log_n;
+        tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, 2 * count, mods, c.p_inv.as<uint64_t>(),
+                               c.d_status.as<unsigned>(), s, c.pdl);
+    }
+    BFinalMap fm{make_prefix(count, [&](int i) { return 2 * lvl(i); }), {}, 0};
+    for (int i = 0; i < count; i++) fm.l[i] = lvl(i);
+    BScratch<3> w{r};
+    ntt_fwd2(c, fm.pre.p[count], fm, w, w, w, w, s);
+    Prefix pre = make_prefix(count, [&](int) { return 2; });
+    const unsigned gx = (unsigned)std::max<uint64_t>(1, c.n / 512);
+    count_launch();
+    launch_pdl(c.pdl, batch_keyswitch_combine, dim3(gx, pre.p[count]), dim3(256), 0, s, r, pre,
+               c.p_inv.as<uint64_t>(), mods);
+}
+
+// Every level of the batch has the tensor-core mod-up and mod-down tables.
+static bool batch_tc_ready(const Context &c, const std::vector<int> &levels) {
+    bool tc = c.tc_on;
+    for (int l : levels) tc = tc && c.levels[l]->tc_ok && c.levels[l]->tc_moddown_ok;
+    return tc;
+}
+
 // Batched key switch (keyswitch_inplace, src/eval_key_switch.cu:95-182, over many ciphertexts at
 // uneven levels with one key): the HMult pipeline with c2 given instead of a1 * b1, the P limbs'
 // inverse NTT alone, the plain mod-down on the tensor cores and an in-place combine.  Without the
 // tensor-core conversions for every level present it runs the single-call key switch per item.
 void ckks_keyswitch_batch(const Context &c, uint64_t *ws_base, size_t item_words, const std::vector<KsItem> &items,
                           const uint64_t *const *evk, cudaStream_t s) {
-    const Mod *mods = c.d_mods.as<Mod>();
-    const int alpha = c.nP, nQ = c.nQ;
-    const unsigned gx = (unsigned)std::max<uint64_t>(1, c.n / 512);
-    bool tc = c.tc_on;
-    for (const KsItem &k : items) tc = tc && c.levels[k.l]->tc_ok && c.levels[k.l]->tc_moddown_ok;
-    if (!tc) {
+    std::vector<int> levels;
+    for (const KsItem &k : items) levels.push_back(k.l);
+    if (!batch_tc_ready(c, levels)) {
         for (size_t i = 0; i < items.size(); i++)
             ckks_keyswitch(c, Workspace{ws_base + (i % kMaxBatch) * item_words, item_words}, items[i].ct, items[i].c2,
                            items[i].l, evk, s);
@@ -715,7 +803,7 @@ void ckks_keyswitch_batch(const Context &c, uint64_t *ws_base, size_t item_words
         r.it.keyswitch = 1;
         r.sl = scratch_layout(c);
         r.log_n = c.log_n;
-        r.alpha = alpha;
+        r.alpha = c.nP;
         r.drop = 0;
         for (int i = 0; i < count; i++) {
             const KsItem &k = items[base + i];
@@ -729,71 +817,242 @@ void ckks_keyswitch_batch(const Context &c, uint64_t *ws_base, size_t item_words
             r.it.mat[i] = lt.modup_mat.as<uint64_t>();
             r.it.iq[i] = nullptr;
         }
-        auto lvl = [&](int i) { return r.it.l[i]; };
-        auto beta_of = [&](int i) { return c.beta(lvl(i)); };
-        // 1-3. mod-up: inverse NTT of c2 (scaled), tensor-core conversion, forward NTT
-        {
-            Prefix pre = make_prefix(count, lvl);
-            BScratch<0> y{r};
-            ntt_inv2(c, pre.p[count], BSeqMap{pre}, BD2Load{r, mods}, y, y, BScaleYStore{r, mods}, s);
-        }
-        {
-            Prefix pre = make_prefix(count, beta_of);
-            BatchModupSrc src{};
-            src.pre = pre;
-            for (int i = 0; i < count; i++) {
-                const LevelTables &lt = *c.levels[lvl(i)];
-                src.ws[i] = r.it.ws[i];
-                src.bmat[i] = lt.tc_modup.as<uint16_t>();
-                src.meta[i] = lt.tc_modup_meta.as<TcOutMeta>();
-                src.nn[i] = lt.tc_modup_nn.as<int>();
-                src.l[i] = lvl(i);
-            }
-            src.y_off = r.sl.y;
-            src.tm_off = r.sl.tm;
-            src.alpha = alpha;
-            src.log_n = c.log_n;
-            src.kpad = c.tc_kpad;
-            tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, pre.p[count], mods, c.p_inv.as<uint64_t>(),
-                                   c.d_status.as<unsigned>(), s, c.pdl);
-        }
-        // 4. (with the mod-up's forward NTT) inner product
+        batch_modup_convert(c, r, s);
         batch_modup_ntt_inner_product(c, r, std::vector<int>(r.it.l, r.it.l + count), evk, s);
-        // 5. inverse NTT of the P limbs of both cx polynomials, times PHatInv
-        {
-            BPMap pm{make_prefix(count, [&](int) { return 2 * alpha; }), alpha, nQ};
-            BScratch<2> mid{r};
-            ntt_inv2(c, pm.pre.p[count], pm, BLastLoad{r, mods}, mid, mid,
-                     BLastStore{r, c.p_hat_inv.as<uint64_t>(), mods}, s);
-        }
-        // 6. delta = P -> Ql conversion on the tensor cores
-        {
-            BatchModdownSrc src{};
-            for (int i = 0; i < count; i++) {
-                const LevelTables &lt = *c.levels[lvl(i)];
-                src.ws[i] = r.it.ws[i];
-                src.bmat[i] = lt.tc_moddown.as<uint16_t>();
-                src.meta[i] = lt.tc_moddown_meta.as<TcOutMeta>();
-                src.nn[i] = lt.tc_moddown_nn;
-                src.l[i] = lvl(i);
+        batch_moddown_combine(c, r, s);
+    }
+}
+
+// ------------------------------------------------------------------ batched matrix-vector product
+
+// g = the Galois automorphism of both polynomials of src_c (item c's ciphertext at its level):
+// g[t][j][i] = src[t][j][perm[i]], into the item's scratch region g.  Block row = (item, limb).
+struct PtrList {
+    const uint64_t *p[kMaxBatch];
+};
+
+__global__ void __launch_bounds__(256) batch_galois_permute(BItemsRef r, Prefix pre, PtrList src,
+                                                            const uint32_t *perm) {
+    pdl_wait();
+    pdl_release();
+    const int c = pre.find(blockIdx.y), k = blockIdx.y - pre.p[c];  // k < 2 l_c: polynomial k / l_c
+    const int log_n = r.log_n;
+    const size_t n = (size_t)1 << log_n;
+    const uint64_t *in = src.p[c] + ((size_t)k << log_n);
+    uint64_t *out = r.it.ws[c] + r.sl.g + ((size_t)k << log_n);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = in[__ldg(perm + i)];
+}
+
+// Hoisted inner product for key limb blockIdx.y over every item that has it: cx_c = sum_d
+// perm(T_d) * key_d with the shared mod-up T of each item (region tm) read through the
+// permutation and the own limbs from the item's permuted c1 (region g, polynomial 1); the key
+// tile comes from HBM for the first item and from cache for the others.  The single-call form is
+// ks_inner_product_hoisted (one step).
+__global__ void __launch_bounds__(256) ks_inner_product_hoisted_batch(BItemsRef r, const uint32_t *perm,
+                                                                      const uint64_t *const *key, const Mod *mods,
+                                                                      int nQ, int qp) {
+    pdl_wait();
+    pdl_release();
+    const int tk = blockIdx.y, alpha = r.alpha, log_n = r.log_n;
+    const Mod m = mods[tk];
+    const size_t n = (size_t)1 << log_n;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t src = __ldg(perm + idx);
+        for (int c = 0; c < r.it.count; c++) {
+            const int l = r.it.l[c];
+            if (tk >= l && tk < nQ) continue;  // this level has dropped q_tk
+            const int jj = tk < nQ ? tk : l + (tk - nQ), qlp = l + alpha, beta = (l + alpha - 1) / alpha;
+            const int own_d = jj < l ? jj / alpha : -1;
+            const uint64_t *ws = r.it.ws[c];
+            const uint64_t *tm = ws + r.sl.tm, *g1 = ws + r.sl.g + ((size_t)l << log_n);
+            u128 a{0, 0}, b{0, 0};
+            int terms = 0;
+            for (int d = 0; d < beta; d++) {
+                const uint64_t x = d == own_d ? g1[((size_t)jj << log_n) + idx]
+                                              : tm[(((size_t)d * qlp + jj) << log_n) + src];
+                const uint64_t *kd = key[d];
+                if (terms == 7) {
+                    a = u128{reduce128(a, m), 0};
+                    b = u128{reduce128(b, m), 0};
+                    terms = 1;
+                }
+                mac(a, x, __ldg(kd + ((size_t)tk << log_n) + idx));
+                mac(b, x, __ldg(kd + ((size_t)(qp + tk) << log_n) + idx));
+                terms++;
             }
-            src.cx_off = r.sl.cx;
-            src.tm_off = r.sl.tm;
-            src.alpha = alpha;
-            src.log_n = c.log_n;
-            tc_bconv_launch<false>(c.tc_kpad, c.num_sms, c.log_n, src, 2 * count, mods, c.p_inv.as<uint64_t>(),
-                                   c.d_status.as<unsigned>(), s, c.pdl);
+            uint64_t *cx = r.it.ws[c] + r.sl.cx + ((size_t)jj << log_n) + idx;
+            cx[0] = reduce128(a, m);
+            cx[(size_t)qlp << log_n] = reduce128(b, m);
         }
-        // 7. forward NTT of delta, then ct += (cx - NTT(delta)) P^-1
-        {
-            BFinalMap fm{make_prefix(count, [&](int i) { return 2 * lvl(i); }), {}, 0};
-            for (int i = 0; i < count; i++) fm.l[i] = lvl(i);
-            BScratch<3> w{r};
-            ntt_fwd2(c, fm.pre.p[count], fm, w, w, w, w, s);
-            Prefix pre = make_prefix(count, [&](int) { return 2; });
-            count_launch();
-            launch_pdl(c.pdl, batch_keyswitch_combine, dim3(dim3(gx, pre.p[count])), dim3(256), 0, s, r, pre, c.p_inv.as<uint64_t>(), mods);
+    }
+}
+
+constexpr int kMvTerms = 32;  // plaintext products per launch of the inner sums
+
+// Per-item pointers of a batched matrix-vector product.
+struct MvItems {
+    const uint64_t *ct[kMaxBatch];     // baby 0 (the input), 2 polys at level l
+    uint64_t *babies[kMaxBatch];       // babies 1..G-1, then `result`: [G][2][l][N]
+    const uint64_t *diags[kMaxBatch];  // [D][l][N]
+    int l[kMaxBatch];
+};
+
+// Inner sums of a giant step for every item: result (+)= sum_b baby_(b0 + b) * diag_(k0 + b),
+// b < nt, 128-bit accumulation (the same words as the single call's mul_plain_sum: exact modular
+// arithmetic).  Block row = (item, limb).
+__global__ void __launch_bounds__(256) mul_plain_sum_batch(MvItems mv, Prefix pre, int G, int b0, int k0, int nt,
+                                                           bool accumulate, const Mod *mods, int log_n) {
+    pdl_wait();
+    pdl_release();
+    const int c = pre.find(blockIdx.y), j = blockIdx.y - pre.p[c], l = mv.l[c];
+    const size_t n = (size_t)1 << log_n, lps = (size_t)l << log_n, cts = 2 * lps;
+    const Mod m = mods[j];
+    uint64_t *res = mv.babies[c] + (size_t)(G - 1) * cts + ((size_t)j << log_n);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        u128 a0{0, 0}, a1{0, 0};
+        int terms = 0;
+        for (int b = 0; b < nt; b++) {
+            const int bb = b0 + b;
+            const uint64_t *ct = bb == 0 ? mv.ct[c] : mv.babies[c] + (size_t)(bb - 1) * cts;
+            const uint64_t p = mv.diags[c][(size_t)(k0 + b) * lps + ((size_t)j << log_n) + i];
+            if (terms == 7) {
+                a0 = u128{reduce128(a0, m), 0};
+                a1 = u128{reduce128(a1, m), 0};
+                terms = 1;
+            }
+            mac(a0, ct[((size_t)j << log_n) + i], p);
+            mac(a1, ct[lps + ((size_t)j << log_n) + i], p);
+            terms++;
         }
+        uint64_t r0 = reduce128(a0, m), r1 = reduce128(a1, m);
+        if (accumulate) {
+            r0 = add_mod(r0, res[i], m.q);
+            r1 = add_mod(r1, res[lps + i], m.q);
+        }
+        res[i] = r0;
+        res[lps + i] = r1;
+    }
+}
+
+// Baby-step/giant-step products of many ciphertexts at uneven levels in the hoisted form of
+// ckks_bsgs_matvec (ops_linear.cu), one launch per pipeline step over up to 64 of them: the
+// baby rotations share each item's mod-up of c1 and read every key once per launch; the giant
+// steps rotate every item's running sum by G together (Horner's rule); each output equals the
+// single call's word for word.  Scratch per item: bsgs_scratch_words(c, G) at scratch_base + i *
+// scratch_words.  Without the tensor-core conversions for every level it runs the single call
+// per item.
+void ckks_bsgs_matvec_batch(Context &c, uint64_t *ws_base, size_t item_words, uint64_t *scratch_base,
+                            size_t scratch_words, const std::vector<MatvecItem> &items, int D, int G, int B,
+                            const uint64_t *const *const *galois_keys, cudaStream_t s) {
+    std::vector<int> levels;
+    for (const MatvecItem &it : items) levels.push_back(it.l);
+    const int alpha = c.nP, nQ = c.nQ;
+    if (!batch_tc_ready(c, levels) || alpha + 2 > nQ) {
+        for (size_t i = 0; i < items.size(); i++)
+            ckks_bsgs_matvec(c, Workspace{ws_base + (i % kMaxBatch) * item_words, item_words},
+                             scratch_base + (i % kMaxBatch) * scratch_words, items[i].ct, items[i].l, items[i].diags,
+                             D, G, B, galois_keys, items[i].out, true, s);
+        return;
+    }
+    auto step_key = [&](int step) {
+        const uint32_t elt = host::elt_from_step(step, c.n);
+        for (size_t i = 0; i < c.galois_elts.size(); i++)
+            if (c.galois_elts[i] == elt && galois_keys[i]) return StepKey{c.perm_table(elt), galois_keys[i]};
+        throw std::invalid_argument("Galois key not present for a baby or giant step");
+    };
+    std::vector<StepKey> baby;
+    for (int b = 1; b < G; b++) baby.push_back(step_key(b));
+    const StepKey giant = B > 1 ? step_key(G) : StepKey{nullptr, nullptr};
+    const Mod *mods = c.d_mods.as<Mod>();
+    const unsigned gx = (unsigned)std::max<uint64_t>(1, c.n / 512);
+    for (size_t base = 0; base < items.size(); base += kMaxBatch) {
+        const int count = (int)std::min<size_t>(kMaxBatch, items.size() - base);
+        BItemsRef r{};
+        r.it.count = count;
+        r.it.keyswitch = 1;
+        r.it.galois = 1;
+        r.sl = scratch_layout(c);
+        r.log_n = c.log_n;
+        r.alpha = alpha;
+        r.drop = 0;
+        MvItems mv{};
+        std::vector<const uint64_t *> cts(count), res_ptr(count);
+        for (int i = 0; i < count; i++) {
+            const MatvecItem &m = items[base + i];
+            const LevelTables &lt = *c.levels[m.l];
+            const size_t cw = 2 * ((size_t)m.l << c.log_n);
+            r.it.l[i] = m.l;
+            r.it.ws[i] = ws_base + (size_t)i * item_words;
+            r.it.phi[i] = lt.part_hat_inv.as<uint64_t>();
+            r.it.mat[i] = lt.modup_mat.as<uint64_t>();
+            mv.ct[i] = m.ct;
+            mv.babies[i] = scratch_base + (size_t)i * scratch_words;
+            mv.diags[i] = m.diags;
+            mv.l[i] = m.l;
+            cts[i] = m.ct;
+            res_ptr[i] = mv.babies[i] + (size_t)(G - 1) * cw;
+        }
+        auto ptr_list = [&](const std::vector<const uint64_t *> &v) {
+            PtrList pl{};
+            for (int i = 0; i < count; i++) pl.p[i] = v[i];
+            return pl;
+        };
+        Prefix limbs2 = make_prefix(count, [&](int i) { return 2 * mv.l[i]; });
+        // 1. baby steps: one mod-up of each item's c1, kept in tm; per step the permuted input in g,
+        //    the hoisted inner product, the mod-down into the region h (tm survives) and the combine
+        //    into baby b
+        if (G > 1) {
+            for (int i = 0; i < count; i++) {
+                r.it.a[i] = mv.ct[i];
+                r.it.b[i] = mv.ct[i] + ((size_t)mv.l[i] << c.log_n);
+            }
+            batch_modup_convert(c, r, s);
+            BModupMap mm{make_prefix(count, [&](int i) { return c.beta(mv.l[i]) * (mv.l[i] + alpha); }), {}, nQ,
+                         alpha};
+            for (int i = 0; i < count; i++) mm.l[i] = mv.l[i];
+            BScratch<1> tm{r};
+            ntt_fwd2(c, mm.pre.p[count], mm, tm, tm, tm, tm, s);
+            r.sl.mid = r.sl.h;
+            for (int b = 1; b < G; b++) {
+                for (int i = 0; i < count; i++) r.it.out[i] = mv.babies[i] + (size_t)(b - 1) * 2 * ((size_t)mv.l[i] << c.log_n);
+                count_launch();
+                launch_pdl(c.pdl, batch_galois_permute, dim3(gx, limbs2.p[count]), dim3(256), 0, s, r, limbs2,
+                           ptr_list(cts), baby[b - 1].perm);
+                count_launch();
+                launch_pdl(c.pdl, ks_inner_product_hoisted_batch, dim3(gx, (unsigned)(nQ + alpha)), dim3(256), 0, s, r,
+                           baby[b - 1].perm, baby[b - 1].key, mods, nQ, nQ + alpha);
+                batch_moddown_combine(c, r, s);
+            }
+            r.sl.mid = r.sl.tm;
+        }
+        // 2. giant steps by Horner's rule: result = inner_(B-1); result = rot_G(result) + inner_g
+        bool first = true;
+        for (int g = B - 1; g >= 0; g--) {
+            const int k0 = g * G, nt = std::min(G, D - k0);
+            if (!first) {  // rotate every item's result by G: permute, then key switch (g1) onto (g0, 0)
+                for (int i = 0; i < count; i++) {
+                    r.it.out[i] = const_cast<uint64_t *>(res_ptr[i]);
+                    r.it.b[i] = r.it.ws[i] + r.sl.g + ((size_t)mv.l[i] << c.log_n);
+                }
+                count_launch();
+                launch_pdl(c.pdl, batch_galois_permute, dim3(gx, limbs2.p[count]), dim3(256), 0, s, r, limbs2,
+                           ptr_list(res_ptr), giant.perm);
+                batch_modup_convert(c, r, s);
+                batch_modup_ntt_inner_product(c, r, std::vector<int>(mv.l, mv.l + count), giant.key, s);
+                batch_moddown_combine(c, r, s);
+            }
+            for (int t0 = 0; t0 < nt; t0 += kMvTerms) {
+                Prefix pre = make_prefix(count, [&](int i) { return mv.l[i]; });
+                count_launch();
+                launch_pdl(c.pdl, mul_plain_sum_batch, dim3(gx, pre.p[count]), dim3(256), 0, s, mv, pre, G, t0,
+                           k0 + t0, std::min(kMvTerms, nt - t0), !first || t0 > 0, mods, c.log_n);
+            }
+            if (nt > 0) first = false;
+        }
+        // 3. rescale every result
+        for (int i = 0; i < count; i++)
+            ckks_rescale(c, Workspace{r.it.ws[i], item_words}, res_ptr[i], items[base + i].out, 2, mv.l[i], s);
     }
 }
 

@@ -47,6 +47,10 @@ class _KsItem(ctypes.Structure):
     _fields_ = [("ct", _vp), ("c2", _vp), ("chain_index", _sz)]
 
 
+class _MatvecItem(ctypes.Structure):
+    _fields_ = [("ct", _vp), ("diags", _vp), ("out", _vp), ("chain_index", _sz)]
+
+
 class Tuning(ctypes.Structure):
     """fhe_tuning: the context's kernel shapes (every setting gives the same words)."""
     _fields_ = [("ntt_split", ctypes.c_int), ("ntt_tile", ctypes.c_int), ("ntt_small_tile", ctypes.c_int),
@@ -124,6 +128,8 @@ def _load():
     L.fhe_bsgs_scratch_bytes.argtypes = [_vp, _sz]
     L.fhe_ckks_bsgs_matvec.argtypes = [_vp, _vp, _vp, _vp, _sz, _vp, _sz, _sz, _sz, ctypes.POINTER(_vp), _vp,
                                        ctypes.c_int, _vp]
+    L.fhe_ckks_bsgs_matvec_batch.argtypes = [_vp, _vp, _vp, ctypes.POINTER(_MatvecItem), _sz, _sz, _sz, _sz,
+                                             ctypes.POINTER(_vp), _vp]
     L.fhe_ckks_encrypt_symmetric.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]
     L.fhe_ckks_decrypt.argtypes = [_vp, _vp, _vp, _vp, _sz, _vp]
     L.fhe_ckks_encode.argtypes = [_vp, _vp, _vp, _sz, ctypes.c_double, _sz, _vp, _vp]
@@ -422,6 +428,15 @@ class Context:
         _check(lib.fhe_ckks_bsgs_matvec(self._h, ws._h, _ptr(scratch), _ptr(ct), chain_index, _ptr(diags), D, G, B,
                                         self._gk_array(galois_keys), _ptr(out), int(bool(hoisted)),
                                         _stream(stream)))
+
+    def bsgs_matvec_batch(self, ws, scratch, items, D, G, B, galois_keys, stream=None):
+        """items: list of (ct, chain_index, diags, out): the hoisted bsgs_matvec of every item in
+        one launch per pipeline step (uneven levels); ws from workspace(batch_items=...), scratch
+        of min(len(items), 64) x bsgs_scratch_bytes(G) bytes."""
+        arr = (_MatvecItem * len(items))(*[_MatvecItem(ct.data_ptr(), dg.data_ptr(), out.data_ptr(), ci)
+                                           for ct, ci, dg, out in items])
+        _check(lib.fhe_ckks_bsgs_matvec_batch(self._h, ws._h, _ptr(scratch), arr, len(items), D, G, B,
+                                              self._gk_array(galois_keys), _stream(stream)))
 
     def encrypt_symmetric(self, pt, s_ntt, a, e, out, chain_index, stream=None):
         _check(lib.fhe_ckks_encrypt_symmetric(self._h, _ptr(pt), _ptr(s_ntt), _ptr(a), _ptr(e), _ptr(out),

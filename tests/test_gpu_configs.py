@@ -133,3 +133,28 @@ def test_matvec128_at_its_parameters_word_for_word(mv, pg, hoisted, l):
     _eq(out, _oracle_matvec(oc, pg, mods, keys, diags, ct, l, hoisted),
         f"matrix-vector product ({'hoisted' if hoisted else 'reference loop'}, l = {l})")
     assert ctx.device_status() == 0
+
+
+def test_matvec128_batch_at_its_parameters_equals_single_calls(mv, pg):
+    """The batched hoisted 128 x 128 product at its own parameters, three vectors at uneven
+    levels: every output equals the single call's words (which the test above pins to the
+    oracle)."""
+    ctx, oc, mods, keys, gks, diags, ws, rng = mv
+    items, singles = [], []
+    one = torch.empty(ctx.bsgs_scratch_bytes(MV_G) // 8, dtype=torch.int64, device="cuda")
+    for l in (20, 7, 12):
+        chain = 20 - l + 1
+        t = pg.to_device(O.random_residues(rng, mods[:l], ctx.n, 2))
+        dg = pg.to_device(np.ascontiguousarray(diags[:, :l]))
+        out = torch.empty((2, l - 1, ctx.n), dtype=torch.int64, device="cuda")
+        single = torch.empty_like(out)
+        ctx.bsgs_matvec(ws, one, t, chain, dg, MV_D, MV_G, MV_B, gks, single, hoisted=True)
+        items.append((t, chain, dg, out))
+        singles.append(single)
+    del one
+    wsb = ctx.workspace(batch_items=len(items))
+    scratch = torch.empty(len(items) * ctx.bsgs_scratch_bytes(MV_G) // 8, dtype=torch.int64, device="cuda")
+    ctx.bsgs_matvec_batch(wsb, scratch, items, MV_D, MV_G, MV_B, gks)
+    for (t, chain, dg, out), single in zip(items, singles):
+        assert torch.equal(out, single), f"chain {chain}"
+    assert ctx.device_status() == 0
