@@ -406,10 +406,15 @@ def run_ours(args):
     t_ks_cc = timed(lambda i: ctx.keyswitch(ws, ct, c2, CHAIN, key, stream), k2)
     ctx.tensor_cores = tc_default
     # ... and with the mod-up's row pass and the inner product as two kernels (t_mod_up written)
+    # and as the fused kernel, whichever the autotuner chose
+    tuned_fused = ctx.fused_keyswitch
     ctx.fused_keyswitch = False
     t_hm_unfused = timed(step, k2)
     t_ks_unfused = timed(lambda i: ctx.keyswitch(ws, ct, c2, CHAIN, key, stream), k2)
     ctx.fused_keyswitch = True
+    t_hm_fused = timed(step, k2)
+    t_ks_fused = timed(lambda i: ctx.keyswitch(ws, ct, c2, CHAIN, key, stream), k2)
+    ctx.fused_keyswitch = tuned_fused
     tc_status = ctx.device_status()
     # NTT throughput: 64 polynomials x 35 limbs (1.17 GB > 4x L2), forward transform
     polys, limbs = 64, len(mods)
@@ -455,7 +460,6 @@ def run_ours(args):
     wsb = ctx.workspace(batch_items=64)
     kb = 5
     ks_items = [(x[0], x[1][1], x[3]) for x in items]  # ct = the first operand, c2 = one poly of the second
-    tuned_fused = ctx.fused_keyswitch
     t_batch, t_ksb = {}, {}
     # both forms of the batched mod-up + inner product: the row pass fused with the inner product
     # (every item's blocks for one key tile run together) and the two-kernel form
@@ -466,7 +470,9 @@ def run_ours(args):
         # the same 64 levels as a batch of key switches (ct += KeySwitch(c2))
         ctx.keyswitch_batch(wsb, ks_items, key, stream)
         t_ksb[fused] = timed(lambda i: ctx.keyswitch_batch(wsb, ks_items, key, stream), kb) / kb
-    ctx.fused_keyswitch = tuned_fused
+    # the single calls keep the autotuner's choice; batches run fused unless told otherwise
+    ctx.fused_keyswitch = True
+    ctx.tuning = {k: v for k, v in tuning.items() if k not in ("best_us", "evaluated")}
     # ... and as loops of single calls
     t_loop = timed(lambda i: [ctx.multiply_relin_rescale(ws, x[0], x[1], x[2], x[3], key, stream) for x in items],
                    kb) / kb
@@ -609,6 +615,8 @@ def run_ours(args):
                       "keyswitch_cuda_core_bconv_per_s": k2 * world / t_ks_cc,
                       "hmult_relin_rescale_unfused_modup_ops_per_s": k2 * world / t_hm_unfused,
                       "keyswitch_unfused_modup_per_s": k2 * world / t_ks_unfused,
+                      "hmult_relin_rescale_fused_modup_ops_per_s": k2 * world / t_hm_fused,
+                      "keyswitch_fused_modup_per_s": k2 * world / t_ks_fused,
                       "ntt_forward_ms_64x35": 1000 * t_ntt,
                       "hmult_relin_rescale_algorithmic_bytes": 313524224,
                       "hmult_hbm_frac": 313524224 * value / world / 1e9 / peak,

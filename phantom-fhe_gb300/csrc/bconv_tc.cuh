@@ -122,7 +122,6 @@ __global__ void __launch_bounds__(tc::kPipeThreads, 1)
     __shared__ __align__(alignof(TcGroup)) unsigned char s_grp_raw[NSLOT * sizeof(TcGroup)];
     TcGroup *const s_grp = reinterpret_cast<TcGroup *>(s_grp_raw);
     __shared__ int s_bslot[NSLOT];
-    __shared__ uint64_t s_z[tc::kRows];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tiles = 1 << (log_n - 7);
     const long long units = (long long)ngroups * tiles;
@@ -224,20 +223,19 @@ __global__ void __launch_bounds__(tc::kPipeThreads, 1)
         const int a0 = grp * gg.nn / 4, a1 = (grp + 1) * gg.nn / 4;
         const int b0 = gg.nn + grp * nw / 4, b1 = gg.nn + (grp + 1) * nw / 4;
         if constexpr (RESCALE) {
-            if (grp == 0) {
-                const int pl = gg.npos - 1;
-                const uint64_t ql = s_p[sl][pl];
-                uint32_t x[8];
-                tc::ld8(trow + pl * 8, x);
-                tc::wait_ld();
-                uint64_t e = ql < (1ull << 40) ? tc::reduce_planes_lazy<5>(x, ql, s_inv[sl][pl])
-                                               : tc::reduce_planes_lazy<8>(x, ql, s_inv[sl][pl]);
-                e = csub(e, ql);
-                const uint64_t zcp = mul_shoup(gg.zc[n], pinv[2 * (gg.l - 1)], pinv[2 * (gg.l - 1) + 1], ql);
-                s_z[row] = sub_mod(add_mod(gg.zd[n], zcp, ql), e, ql);
-            }
-            asm volatile("bar.sync %0, 128;" ::"r"(1 + lq) : "memory");  // the four warps of this lane quarter
-            const uint64_t z = s_z[row];
+            // every warp group computes its rows' z itself (the same words four times over) rather
+            // than waiting at a barrier for one group to share it
+            const int pl = gg.npos - 1;
+            const uint64_t ql = s_p[sl][pl];
+            const uint64_t zcp = mul_shoup(gg.zc[n], pinv[2 * (gg.l - 1)], pinv[2 * (gg.l - 1) + 1], ql);
+            const uint64_t zd = gg.zd[n];
+            uint32_t x[8];
+            tc::ld8(trow + pl * 8, x);
+            tc::wait_ld();
+            uint64_t e = ql < (1ull << 40) ? tc::reduce_planes_lazy<5>(x, ql, s_inv[sl][pl])
+                                           : tc::reduce_planes_lazy<8>(x, ql, s_inv[sl][pl]);
+            e = csub(e, ql);
+            const uint64_t z = sub_mod(add_mod(zd, zcp, ql), e, ql);
             auto addz = [z](int) { return z; };
             tc_emit<5>(trow, dst, a0, a1, s_p[sl], s_off[sl], s_inv[sl], addz);
             tc_emit<8>(trow, dst, b0, b1, s_p[sl], s_off[sl], s_inv[sl], addz);

@@ -206,7 +206,7 @@ int fhe_context_fused_keyswitch(const fhe_context *ctx) {
 int fhe_context_set_fused_keyswitch(fhe_context *ctx, int enable) {
     return guarded([&] {
         pfg::Context &c = *const_cast<pfg::Context *>(&ctx_of(ctx));
-        c.ks_fused = enable != 0;
+        c.ks_fused = c.ks_fused_batch = enable != 0;
     }, false);
 }
 

@@ -151,8 +151,10 @@ struct Context {
     // kernel chains launched with programmatic dependent launch (pdl.cuh); any setting gives the
     // same words
     bool pdl = true;
-    // mod-up row pass fused with the inner product (ks_fused.cuh); any setting gives the same words
-    bool ks_fused = true;
+    // mod-up row pass fused with the inner product (ks_fused.cuh) for single calls and for batches
+    // (the autotuner sets only the first; fhe_context_set_fused_keyswitch sets both); any setting
+    // gives the same words
+    bool ks_fused = true, ks_fused_batch = true;
     // device the context's tables live on, and the device address of the fixed scratch array of
     // fhe_rescale_to_next_noalloc on it (looked up at creation, with that device current, so the
     // address belongs to the CUDA context the tables were made in)

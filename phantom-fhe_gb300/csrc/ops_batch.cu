@@ -565,7 +565,7 @@ static void batch_modup_ntt_inner_product(const Context &c, const BItemsRef &r, 
     BModupMap mm{make_prefix(count, [&](int i) { return c.beta(lv[i]) * (lv[i] + alpha); }), {}, nQ, alpha};
     for (int i = 0; i < count; i++) mm.l[i] = lv[i];
     BScratch<1> tm{r};
-    if (c.ks_fused) {
+    if (c.ks_fused_batch) {
         col_pass<true, false>(c, mm.pre.p[count], mm, tm, tm, s);
         const dim3 grid((unsigned)count, (unsigned)(c.n / kFusedTile), (unsigned)(nQ + alpha));
         const NttTables T = c.ntt();

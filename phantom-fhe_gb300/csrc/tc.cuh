@@ -124,9 +124,17 @@ __device__ __forceinline__ uint4 bytes_bf16(uint64_t v) {
 // the remainder is small.  [0, 2p) is a valid input of the lazy forward NTT.
 template <int NPL>
 __device__ __forceinline__ uint64_t reduce_planes_lazy(const uint32_t *r, uint64_t p, float invp) {
-    float vf = __uint_as_float(r[0]);
+    // f32 estimate of V as a tree of pairs (C_2k + 2^8 C_2k+1, then 2^16-weighted pairs of those,
+    // ...): the same number of roundings per term as a running sum, half the dependent chain
+    float t[NPL];
 #pragma unroll
-    for (int b = 1; b < NPL; b++) vf = fmaf(__uint_as_float(r[b]), __uint_as_float((uint32_t)(127 + 8 * b) << 23), vf);
+    for (int b = 0; b < NPL; b++) t[b] = __uint_as_float(r[b]);
+#pragma unroll
+    for (int w = 1; w < NPL; w *= 2)
+#pragma unroll
+        for (int b = 0; b + w < NPL; b += 2 * w)
+            t[b] = fmaf(t[b + w], __uint_as_float((uint32_t)(127 + 8 * w) << 23), t[b]);
+    const float vf = t[0];
     const float qf = fmaf(vf, invp, -0.625f);
     const int32_t qs = (int32_t)(__float_as_uint(qf + 12582912.0f) - 0x4B400000u);  // round to nearest
     const uint32_t q = (uint32_t)max(qs, 0);
