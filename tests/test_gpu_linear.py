@@ -170,29 +170,34 @@ def test_bsgs_hoisted_horner_word_for_word(lin, pg, chain, G, B):
     _eq(out, oc.rescale(l, result), "BSGS (hoisted, Horner)")
 
 
-@pytest.mark.parametrize("G,B", [(G, B), (2, 5)])
-def test_bsgs_batch_equals_single_calls(lin, pg, G, B):
+@pytest.mark.parametrize("G,B,tc", [(G, B, True), (2, 5, True), (G, B, False)])
+def test_bsgs_batch_equals_single_calls(lin, pg, G, B, tc):
     """The batched hoisted matrix-vector product over ciphertexts at uneven levels (one launch
-    per pipeline step for all of them) gives every single call's words."""
+    per pipeline step for all of them) gives every single call's words; without the tensor-core
+    conversions the batch runs the single calls."""
     ctx, oc, mods, keys, gks, ws = lin
     rng = np.random.default_rng(40 + G)
     chains = [1, 3, 2, 5, 1, 4]
     items, singles = [], []
     one = torch.empty(ctx.bsgs_scratch_bytes(G) // 8, dtype=torch.int64, device="cuda")
-    for ch in chains:
-        l = ctx.level(ch)
-        t = pg.to_device(O.random_residues(rng, mods[:l], ctx.n, 2))
-        dg = pg.to_device(_diags(rng, mods, l, ctx.n))
-        out = torch.empty((2, l - 1, ctx.n), dtype=torch.int64, device="cuda")
-        single = torch.empty_like(out)
-        ctx.bsgs_matvec(ws, one, t, ch, dg, D, G, B, gks, single, hoisted=True)
-        items.append((t, ch, dg, out))
-        singles.append(single)
-    wsb = ctx.workspace(batch_items=len(items))
-    scratch = torch.empty(len(items) * ctx.bsgs_scratch_bytes(G) // 8, dtype=torch.int64, device="cuda")
-    ctx.bsgs_matvec_batch(wsb, scratch, items, D, G, B, gks)
+    ctx.tensor_cores = tc
+    try:
+        for ch in chains:
+            l = ctx.level(ch)
+            t = pg.to_device(O.random_residues(rng, mods[:l], ctx.n, 2))
+            dg = pg.to_device(_diags(rng, mods, l, ctx.n))
+            out = torch.empty((2, l - 1, ctx.n), dtype=torch.int64, device="cuda")
+            single = torch.empty_like(out)
+            ctx.bsgs_matvec(ws, one, t, ch, dg, D, G, B, gks, single, hoisted=True)
+            items.append((t, ch, dg, out))
+            singles.append(single)
+        wsb = ctx.workspace(batch_items=len(items))
+        scratch = torch.empty(len(items) * ctx.bsgs_scratch_bytes(G) // 8, dtype=torch.int64, device="cuda")
+        ctx.bsgs_matvec_batch(wsb, scratch, items, D, G, B, gks)
+    finally:
+        ctx.tensor_cores = True
     for (t, ch, dg, out), single in zip(items, singles):
-        assert torch.equal(out, single), f"chain {ch}"
+        assert torch.equal(out, single), f"chain {ch}, tensor_cores={tc}"
     assert ctx.device_status() == 0
 
 
