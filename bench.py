@@ -487,6 +487,11 @@ def run_ours(args):
     t_loop = timed(lambda i: [ctx.multiply_relin_rescale(ws, x[0], x[1], x[2], x[3], key, stream) for x in items],
                    kb) / kb
     t_ksl = timed(lambda i: [ctx.keyswitch(ws, x[0], x[1], x[2], key, stream) for x in ks_items], kb) / kb
+    # algorithmic bytes of the batch: per ciphertext 8N (4l + 2(l - 1)) (both inputs read, the
+    # output written), the key once over the largest level's digits and QlP limbs
+    lmax = max(levels)
+    batch_bytes = sum(8 * N * (4 * lv + 2 * (lv - 1)) for lv in levels) + \
+        8 * N * 2 * ((lmax + SPECIAL - 1) // SPECIAL) * (lmax + SPECIAL)
     del items, ks_items, wsb
 
     # BFV multiply + relinearise (HPS) at N = 2^15, 16x50-bit + 2x60-bit, t = 65537:
@@ -577,6 +582,29 @@ def run_ours(args):
     t_e2e = max_over_ranks(t_e2e, world, "cuda")
     ck = clocks.stop()
 
+    # the host link's own rates for these buffers (the ceiling of the end-to-end figure): both
+    # input ciphertexts host -> device on their two streams, the result device -> host
+    def link_rate(fn, nbytes, reps=10):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return nbytes * reps / (time.perf_counter() - t0) / 1e9
+
+    def h2d_pair():
+        with torch.cuda.stream(h2d_s):
+            da[0].copy_(pin_a[0], non_blocking=True)
+        with torch.cuda.stream(h2d_s2):
+            db[0].copy_(pin_b[0], non_blocking=True)
+
+    def d2h_one():
+        with torch.cuda.stream(d2h_s):
+            pin_o[0].copy_(do[0], non_blocking=True)
+
+    h2d_gbs = link_rate(h2d_pair, 2 * 2 * l * N * 8)
+    d2h_gbs = link_rate(d2h_one, 2 * (l - 1) * N * 8)
+
     peak, peak_kind = measured_peaks()
     prof = profile_traffic()
     traffic = prof.get("ntt_forward_64x35_n16")
@@ -599,7 +627,10 @@ def run_ours(args):
                                                source="autotuned on this operation")),
             "clocks": ck,
             "e2e": {"value": replica_throughput(args.steps, world, t_e2e), "unit": "ops/s",
-                    "h2d_bytes_per_step": 2 * 2 * l * N * 8, "d2h_bytes_per_step": 2 * (l - 1) * N * 8},
+                    "h2d_bytes_per_step": 2 * 2 * l * N * 8, "d2h_bytes_per_step": 2 * (l - 1) * N * 8,
+                    "h2d_gbs": h2d_gbs, "d2h_gbs": d2h_gbs,
+                    "copy_bound_ops_per_s": 1.0 / max(2 * 2 * l * N * 8 / (h2d_gbs * 1e9),
+                                                       2 * (l - 1) * N * 8 / (d2h_gbs * 1e9))},
             "gpu_launches": int(launches),
             "roofline": {"kernel": f"ntt forward (column + row pass), 64 polys x 35 limbs, N=2^16, split "
                                    f"{ntt_shape[0]}+{16 - ntt_shape[0]}, {ntt_shape[1]}-coefficient tiles",
@@ -616,6 +647,8 @@ def run_ours(args):
                       "batch64_uneven_levels_fused_ops_per_s": 64 * world / t_batch[True],
                       "batch64_uneven_levels_unfused_ops_per_s": 64 * world / t_batch[False],
                       "batch64_as_single_calls_ops_per_s": 64 * world / t_loop,
+                      "batch64_algorithmic_bytes": batch_bytes,
+                      "batch64_hbm_frac": batch_bytes / min(t_batch.values()) / 1e9 / measured_peaks()[0],
                       "keyswitch_batch64_uneven_levels_per_s": 64 * world / min(t_ksb.values()),
                       "keyswitch_batch64_uneven_levels_fused_per_s": 64 * world / t_ksb[True],
                       "keyswitch_batch64_uneven_levels_unfused_per_s": 64 * world / t_ksb[False],
