@@ -8,7 +8,7 @@
 // benchmarks run at the context's top level, batch 1: CKKS HMult + relinearise + rescale, BFV
 // HPS multiply + relinearise.  Inputs and the key are uniform residues (the timing does not depend
 // on the words).  Search: coordinate descent from the current settings, two sweeps over the knobs
-// in order, each candidate timed as the best of three bursts of five operations after two warm-up
+// in order, each candidate timed as the best of five bursts of five operations after two warm-up
 // operations, a candidate kept only when it is at least 0.5 % faster.
 //
 // Cache: one JSON object per line, {"key": "<GPU>|<scheme>|N=..|Q=..|P=..|batch=1", knobs...,
@@ -188,7 +188,7 @@ Tuning autotune_op(Context &c, const Workspace &w, const char *cache_path) {
     auto time_us = [&]() {
         for (int i = 0; i < 2; i++) op();
         float best = 0.f;
-        for (int trial = 0; trial < 3; trial++) {
+        for (int trial = 0; trial < 5; trial++) {
             ck(cudaEventRecord(sc.e0, sc.s), "cudaEventRecord");
             for (int i = 0; i < 5; i++) op();
             ck(cudaEventRecord(sc.e1, sc.s), "cudaEventRecord");

@@ -201,6 +201,31 @@ def test_bsgs_batch_equals_single_calls(lin, pg, G, B, tc):
     assert ctx.device_status() == 0
 
 
+def test_bsgs_batch_more_than_one_launch_set(lin, pg):
+    """70 products (more than one launch set of 64, the second one reusing the first's scratch)
+    give the single calls' words."""
+    ctx, oc, mods, keys, gks, ws = lin
+    rng = np.random.default_rng(47)
+    one = torch.empty(ctx.bsgs_scratch_bytes(G) // 8, dtype=torch.int64, device="cuda")
+    items, singles = [], []
+    for i in range(70):
+        ch = 1 + (i * 3) % 5
+        l = ctx.level(ch)
+        t = pg.to_device(O.random_residues(rng, mods[:l], ctx.n, 2))
+        dg = pg.to_device(_diags(rng, mods, l, ctx.n))
+        out = torch.empty((2, l - 1, ctx.n), dtype=torch.int64, device="cuda")
+        single = torch.empty_like(out)
+        ctx.bsgs_matvec(ws, one, t, ch, dg, D, G, B, gks, single, hoisted=True)
+        items.append((t, ch, dg, out))
+        singles.append(single)
+    wsb = ctx.workspace(batch_items=64)
+    scratch = torch.empty(64 * ctx.bsgs_scratch_bytes(G) // 8, dtype=torch.int64, device="cuda")
+    ctx.bsgs_matvec_batch(wsb, scratch, items, D, G, B, gks)
+    for i, ((t, ch, dg, out), single) in enumerate(zip(items, singles)):
+        assert torch.equal(out, single), f"item {i}, chain {ch}"
+    assert ctx.device_status() == 0
+
+
 def test_bsgs_rejects_bad_shapes(lin, pg):
     ctx, oc, mods, keys, gks, ws = lin
     l = ctx.level(1)
