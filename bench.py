@@ -236,7 +236,7 @@ def matvec_bench(pg, torch, timed, stream, rank, profile_only=False):
 
     # the same 32 products through the batched call: one launch per pipeline step for all of them
     wsb = ctx.workspace(batch_items=MV_BATCH)
-    bscratch = torch.empty(MV_BATCH * ctx.bsgs_scratch_bytes(G) // 8, dtype=torch.int64, device="cuda")
+    bscratch = torch.empty(MV_BATCH * ctx.bsgs_batch_scratch_bytes(G, B) // 8, dtype=torch.int64, device="cuda")
     bouts = [torch.empty_like(o) for o in outs]
     bitems = [(ct, chain, diags_at[lv], o) for (ct, chain, lv), o in zip(cts, bouts)]
 

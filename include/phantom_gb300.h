@@ -328,7 +328,8 @@ int fhe_ckks_bsgs_matvec(const fhe_context *ctx, fhe_workspace *ws, uint64_t *sc
  * step is one launch over up to 64 products, so each key is read once per launch set.  Each
  * output equals fhe_ckks_bsgs_matvec(..., hoisted = 1) word for word.  ws must come from
  * fhe_workspace_create_batch with at least min(count, 64) slots; scratch holds min(count, 64) x
- * fhe_bsgs_scratch_bytes(ctx, G) bytes. */
+ * fhe_bsgs_batch_scratch_bytes(ctx, G, B) bytes (each product's babies and inner sums). */
+size_t fhe_bsgs_batch_scratch_bytes(const fhe_context *ctx, size_t G, size_t B);
 typedef struct fhe_matvec_item {
     const uint64_t *ct;     /* 2 polys at chain_index, NTT form */
     const uint64_t *diags;  /* D plaintexts [D][limbs at chain_index][N], NTT form */

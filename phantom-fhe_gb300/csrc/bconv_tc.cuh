@@ -72,24 +72,34 @@ __device__ __forceinline__ void tc_pipeline(int cnt, uint64_t *bar, uint32_t *ok
     }
 }
 
-// Output positions [o, o1) of one row: accumulator columns [8 pos, 8 pos + 8) -> dst[off[pos]],
+// Per-output record of a tile group: modulus, limb offset in the output (words), 1/p.  One
+// 16-byte shared-memory load per output.
+struct TcOut {
+    uint64_t p;
+    uint32_t off;  // jj << log_n (below 2^23)
+    float inv;
+};
+
+// Output positions [o, o1) of one row: accumulator columns [8 pos, 8 pos + 8) -> dst[off],
 // plus extra(pos) (the rescale's z).
 template <int NPL, class Extra>
-__device__ __forceinline__ void tc_emit(uint32_t trow, uint64_t *dst, int o, int o1, const uint64_t *p,
-                                        const uint64_t *off, const float *inv, Extra extra) {
+__device__ __forceinline__ void tc_emit(uint32_t trow, uint64_t *dst, int o, int o1, const TcOut *meta,
+                                        Extra extra) {
     for (; o + 1 < o1; o += 2) {
         uint32_t x0[8], x1[8];
         tc::ld8(trow + o * 8, x0);
         tc::ld8(trow + o * 8 + 8, x1);
+        const TcOut m0 = meta[o], m1 = meta[o + 1];
         tc::wait_ld();
-        dst[off[o]] = tc::reduce_planes_lazy<NPL>(x0, p[o], inv[o]) + extra(o);
-        dst[off[o + 1]] = tc::reduce_planes_lazy<NPL>(x1, p[o + 1], inv[o + 1]) + extra(o + 1);
+        dst[m0.off] = tc::reduce_planes_lazy<NPL>(x0, m0.p, m0.inv) + extra(o);
+        dst[m1.off] = tc::reduce_planes_lazy<NPL>(x1, m1.p, m1.inv) + extra(o + 1);
     }
     if (o < o1) {
         uint32_t x0[8];
         tc::ld8(trow + o * 8, x0);
+        const TcOut m0 = meta[o];
         tc::wait_ld();
-        dst[off[o]] = tc::reduce_planes_lazy<NPL>(x0, p[o], inv[o]) + extra(o);
+        dst[m0.off] = tc::reduce_planes_lazy<NPL>(x0, m0.p, m0.inv) + extra(o);
     }
 }
 
@@ -115,8 +125,7 @@ __global__ void __launch_bounds__(tc::kPipeThreads, 1)
     uint8_t *sB = smem + 2 * ABYTES;  // 2 x 256 x KP bf16
     __shared__ uint32_t tmem_slot, ok_flag;
     __shared__ __align__(8) uint64_t bar[2];
-    __shared__ uint64_t s_p[NSLOT][tc::kMaxOut], s_off[NSLOT][tc::kMaxOut];
-    __shared__ float s_inv[NSLOT][tc::kMaxOut];
+    __shared__ __align__(16) TcOut s_out[NSLOT][tc::kMaxOut];
     // raw storage: TcGroup's default member initialisers would ask for a dynamic initialisation
     // that shared memory does not have; every slot is written (thread 0, in fill) before it is read
     __shared__ __align__(alignof(TcGroup)) unsigned char s_grp_raw[NSLOT * sizeof(TcGroup)];
@@ -175,9 +184,7 @@ __global__ void __launch_bounds__(tc::kPipeThreads, 1)
             else sg2 = gi;
             if (tid < g.npos) {
                 const TcOutMeta m = g.meta[tid];
-                s_p[sl][tid] = mods[m.tbl].q;
-                s_off[sl][tid] = (size_t)m.jj << log_n;
-                s_inv[sl][tid] = m.invp;
+                s_out[sl][tid] = TcOut{mods[m.tbl].q, m.jj << log_n, m.invp};
             }
             if (tid == 0) {
                 s_grp[sl] = g;
@@ -226,22 +233,23 @@ __global__ void __launch_bounds__(tc::kPipeThreads, 1)
             // every warp group computes its rows' z itself (the same words four times over) rather
             // than waiting at a barrier for one group to share it
             const int pl = gg.npos - 1;
-            const uint64_t ql = s_p[sl][pl];
+            const TcOut ml = s_out[sl][pl];
+            const uint64_t ql = ml.p;
             const uint64_t zcp = mul_shoup(gg.zc[n], pinv[2 * (gg.l - 1)], pinv[2 * (gg.l - 1) + 1], ql);
             const uint64_t zd = gg.zd[n];
             uint32_t x[8];
             tc::ld8(trow + pl * 8, x);
             tc::wait_ld();
-            uint64_t e = ql < (1ull << 40) ? tc::reduce_planes_lazy<5>(x, ql, s_inv[sl][pl])
-                                           : tc::reduce_planes_lazy<8>(x, ql, s_inv[sl][pl]);
+            uint64_t e = ql < (1ull << 40) ? tc::reduce_planes_lazy<5>(x, ql, ml.inv)
+                                           : tc::reduce_planes_lazy<8>(x, ql, ml.inv);
             e = csub(e, ql);
             const uint64_t z = sub_mod(add_mod(zd, zcp, ql), e, ql);
             auto addz = [z](int) { return z; };
-            tc_emit<5>(trow, dst, a0, a1, s_p[sl], s_off[sl], s_inv[sl], addz);
-            tc_emit<8>(trow, dst, b0, b1, s_p[sl], s_off[sl], s_inv[sl], addz);
+            tc_emit<5>(trow, dst, a0, a1, s_out[sl], addz);
+            tc_emit<8>(trow, dst, b0, b1, s_out[sl], addz);
         } else {
-            tc_emit<5>(trow, dst, a0, a1, s_p[sl], s_off[sl], s_inv[sl], NoExtra{});
-            tc_emit<8>(trow, dst, b0, b1, s_p[sl], s_off[sl], s_inv[sl], NoExtra{});
+            tc_emit<5>(trow, dst, a0, a1, s_out[sl], NoExtra{});
+            tc_emit<8>(trow, dst, b0, b1, s_out[sl], NoExtra{});
         }
     };
     tc_pipeline(cnt, bar, &ok_flag, status, load, fill, issue, epilogue);

@@ -633,6 +633,11 @@ size_t fhe_bsgs_scratch_bytes(const fhe_context *ctx, size_t G) {
     return pfg::bsgs_scratch_words(*ctx->c, (int)G) * sizeof(uint64_t);
 }
 
+size_t fhe_bsgs_batch_scratch_bytes(const fhe_context *ctx, size_t G, size_t B) {
+    if (!ctx || !ctx->c || G == 0 || B == 0 || G > 256) return 0;
+    return pfg::bsgs_batch_scratch_words(*ctx->c, (int)G, (int)B) * sizeof(uint64_t);
+}
+
 int fhe_ckks_bsgs_matvec(const fhe_context *ctx, fhe_workspace *ws, uint64_t *scratch, const uint64_t *ct,
                          size_t chain_index, const uint64_t *diags, size_t D, size_t G, size_t B,
                          const uint64_t *const *const *galois_keys, uint64_t *out, int hoisted, void *stream) {
@@ -680,7 +685,8 @@ int fhe_ckks_bsgs_matvec_batch(const fhe_context *ctx, fhe_workspace *ws, uint64
             if (l < 2) throw std::invalid_argument("end of modulus switching chain reached");
             v.push_back(pfg::MatvecItem{items[i].ct, items[i].diags, items[i].out, l});
         }
-        pfg::ckks_bsgs_matvec_batch(c, w.base, ws->words / ws->items, scratch, pfg::bsgs_scratch_words(c, (int)G), v,
+        pfg::ckks_bsgs_matvec_batch(c, w.base, ws->words / ws->items, scratch,
+                                    pfg::bsgs_batch_scratch_words(c, (int)G, (int)B), v,
                                     (int)D, (int)G, (int)B, galois_keys, st(stream));
     });
 }

@@ -78,6 +78,7 @@ void ckks_add(const Context &c, const uint64_t *a, const uint64_t *b, uint64_t *
 void ckks_rotate(Context &c, const Workspace &w, uint64_t *ct, int l, int step,
                  const uint64_t *const *const *galois_keys, cudaStream_t s);
 size_t bsgs_scratch_words(const Context &c, int G);
+size_t bsgs_batch_scratch_words(const Context &c, int G, int B);
 void ckks_bsgs_matvec(Context &c, const Workspace &w, uint64_t *scratch, const uint64_t *ct, int l,
                       const uint64_t *diags, int D, int G, int B, const uint64_t *const *const *galois_keys,
                       uint64_t *out, bool hoisted, cudaStream_t s);

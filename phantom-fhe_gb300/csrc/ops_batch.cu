@@ -29,6 +29,8 @@ struct BatchItems {
     // the item's permuted first polynomial in its scratch region g (a Galois automorphism)
     int galois;
     int l[kMaxBatch];
+    // key switch combine: when add[c] is set, the item's two polynomials there are added too
+    const uint64_t *add[kMaxBatch];
     const uint64_t *a[kMaxBatch], *b[kMaxBatch];
     uint64_t *out[kMaxBatch];
     uint64_t *ws[kMaxBatch];
@@ -254,14 +256,21 @@ __global__ void __launch_bounds__(256) batch_keyswitch_combine(BItemsRef r, Pref
     uint64_t *ct = r.it.out[c] + t * ((long long)lc << log_n);
     // the base: the output itself (in place), or (g0, 0) for an automorphism
     const uint64_t *base = r.it.galois ? (t == 0 ? ws + r.sl.g : nullptr) : ct;
+    const uint64_t *addend = r.it.add[c] ? r.it.add[c] + t * ((long long)lc << log_n) : nullptr;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < work; e += (size_t)gridDim.x * blockDim.x) {
         const int j = (int)(e >> (log_n - 1));
         const size_t o = ((size_t)j << log_n) + 2 * (e & (half - 1));
         const Mod m = mods[j];
         const uint64_t pj = pinv[2 * j], pjs = pinv[2 * j + 1];
         const ulonglong2 vv = ld2(v + o), cc = ld2(cx + o), b = base ? ld2(base + o) : make_ulonglong2(0, 0);
-        st2(ct + o, add_mod(b.x, mul_shoup(sub_mod(cc.x, vv.x, m.q), pj, pjs, m.q), m.q),
-            add_mod(b.y, mul_shoup(sub_mod(cc.y, vv.y, m.q), pj, pjs, m.q), m.q));
+        uint64_t r0 = add_mod(b.x, mul_shoup(sub_mod(cc.x, vv.x, m.q), pj, pjs, m.q), m.q);
+        uint64_t r1 = add_mod(b.y, mul_shoup(sub_mod(cc.y, vv.y, m.q), pj, pjs, m.q), m.q);
+        if (addend) {
+            const ulonglong2 a = ld2(addend + o);
+            r0 = add_mod(r0, a.x, m.q);
+            r1 = add_mod(r1, a.y, m.q);
+        }
+        st2(ct + o, r0, r1);
     }
 }
 
@@ -888,50 +897,48 @@ __global__ void __launch_bounds__(256) ks_inner_product_hoisted_batch(BItemsRef 
     }
 }
 
-constexpr int kMvTerms = 32;  // plaintext products per launch of the inner sums
-
 // Per-item pointers of a batched matrix-vector product.
 struct MvItems {
     const uint64_t *ct[kMaxBatch];     // baby 0 (the input), 2 polys at level l
-    uint64_t *babies[kMaxBatch];       // babies 1..G-1, then `result`: [G][2][l][N]
+    uint64_t *slots[kMaxBatch];        // babies 1..G-1, then one inner sum per giant step: [G-1+B][2][l][N]
     const uint64_t *diags[kMaxBatch];  // [D][l][N]
     int l[kMaxBatch];
 };
 
-// Inner sums of a giant step for every item: result (+)= sum_b baby_(b0 + b) * diag_(k0 + b),
-// b < nt, 128-bit accumulation (the same words as the single call's mul_plain_sum: exact modular
-// arithmetic).  Block row = (item, limb).
-__global__ void __launch_bounds__(256) mul_plain_sum_batch(MvItems mv, Prefix pre, int G, int b0, int k0, int nt,
-                                                           bool accumulate, const Mod *mods, int log_n) {
+// Every giant step's inner sum of every item in one launch: slot G - 1 + g of item c receives
+// inner_g = sum_b baby_b * diag_(g G + b) (128-bit accumulation; the same words as the single
+// call's mul_plain_sum: exact modular arithmetic).  Block row = (item, limb).  Each thread walks
+// the giant steps over its coefficients and reads its coefficient of every baby again for each
+// one; after the first giant step those words (G x 2 x 8 B a thread) come from L1, so the babies
+// are read from HBM once per batch, not once per giant step.
+__global__ void __launch_bounds__(256) mul_plain_sums_batch(MvItems mv, Prefix pre, int G, int steps, int D,
+                                                            const Mod *mods, int log_n) {
     pdl_wait();
     pdl_release();
     const int c = pre.find(blockIdx.y), j = blockIdx.y - pre.p[c], l = mv.l[c];
-    const size_t n = (size_t)1 << log_n, lps = (size_t)l << log_n, cts = 2 * lps;
+    const size_t n = (size_t)1 << log_n, lps = (size_t)l << log_n, cts = 2 * lps, jo = (size_t)j << log_n;
     const Mod m = mods[j];
-    uint64_t *res = mv.babies[c] + (size_t)(G - 1) * cts + ((size_t)j << log_n);
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        u128 a0{0, 0}, a1{0, 0};
-        int terms = 0;
-        for (int b = 0; b < nt; b++) {
-            const int bb = b0 + b;
-            const uint64_t *ct = bb == 0 ? mv.ct[c] : mv.babies[c] + (size_t)(bb - 1) * cts;
-            const uint64_t p = mv.diags[c][(size_t)(k0 + b) * lps + ((size_t)j << log_n) + i];
-            if (terms == 7) {
-                a0 = u128{reduce128(a0, m), 0};
-                a1 = u128{reduce128(a1, m), 0};
-                terms = 1;
+        for (int g = 0; g < steps; g++) {
+            const int nt = min(G, D - g * G);
+            u128 a0{0, 0}, a1{0, 0};
+            int terms = 0;
+            for (int b = 0; b < nt; b++) {
+                const uint64_t *ct = b == 0 ? mv.ct[c] : mv.slots[c] + (size_t)(b - 1) * cts;
+                const uint64_t p = __ldcs(mv.diags[c] + (size_t)(g * G + b) * lps + jo + i);
+                if (terms == 7) {
+                    a0 = u128{reduce128(a0, m), 0};
+                    a1 = u128{reduce128(a1, m), 0};
+                    terms = 1;
+                }
+                mac(a0, __ldg(ct + jo + i), p);
+                mac(a1, __ldg(ct + lps + jo + i), p);
+                terms++;
             }
-            mac(a0, ct[((size_t)j << log_n) + i], p);
-            mac(a1, ct[lps + ((size_t)j << log_n) + i], p);
-            terms++;
+            uint64_t *out = mv.slots[c] + (size_t)(G - 1 + g) * cts + jo + i;
+            out[0] = reduce128(a0, m);
+            out[lps] = reduce128(a1, m);
         }
-        uint64_t r0 = reduce128(a0, m), r1 = reduce128(a1, m);
-        if (accumulate) {
-            r0 = add_mod(r0, res[i], m.q);
-            r1 = add_mod(r1, res[lps + i], m.q);
-        }
-        res[i] = r0;
-        res[lps + i] = r1;
     }
 }
 
@@ -939,9 +946,9 @@ __global__ void __launch_bounds__(256) mul_plain_sum_batch(MvItems mv, Prefix pr
 // ckks_bsgs_matvec (ops_linear.cu), one launch per pipeline step over up to 64 of them: the
 // baby rotations share each item's mod-up of c1 and read every key once per launch; the giant
 // steps rotate every item's running sum by G together (Horner's rule); each output equals the
-// single call's word for word.  Scratch per item: bsgs_scratch_words(c, G) at scratch_base + i *
-// scratch_words.  Without the tensor-core conversions for every level it runs the single call
-// per item.
+// single call's word for word.  Scratch per item: bsgs_batch_scratch_words(c, G, B) at
+// scratch_base + i * scratch_words (the babies, then every giant step's inner sum).  Without the
+// tensor-core conversions for every level it runs the single call per item.
 void ckks_bsgs_matvec_batch(Context &c, uint64_t *ws_base, size_t item_words, uint64_t *scratch_base,
                             size_t scratch_words, const std::vector<MatvecItem> &items, int D, int G, int B,
                             const uint64_t *const *const *galois_keys, cudaStream_t s) {
@@ -987,11 +994,11 @@ void ckks_bsgs_matvec_batch(Context &c, uint64_t *ws_base, size_t item_words, ui
             r.it.phi[i] = lt.part_hat_inv.as<uint64_t>();
             r.it.mat[i] = lt.modup_mat.as<uint64_t>();
             mv.ct[i] = m.ct;
-            mv.babies[i] = scratch_base + (size_t)i * scratch_words;
+            mv.slots[i] = scratch_base + (size_t)i * scratch_words;
             mv.diags[i] = m.diags;
             mv.l[i] = m.l;
             cts[i] = m.ct;
-            res_ptr[i] = mv.babies[i] + (size_t)(G - 1) * cw;
+            (void)cw;
         }
         auto ptr_list = [&](const std::vector<const uint64_t *> &v) {
             PtrList pl{};
@@ -1015,7 +1022,7 @@ void ckks_bsgs_matvec_batch(Context &c, uint64_t *ws_base, size_t item_words, ui
             ntt_fwd2(c, mm.pre.p[count], mm, tm, tm, tm, tm, s);
             r.sl.mid = r.sl.h;
             for (int b = 1; b < G; b++) {
-                for (int i = 0; i < count; i++) r.it.out[i] = mv.babies[i] + (size_t)(b - 1) * 2 * ((size_t)mv.l[i] << c.log_n);
+                for (int i = 0; i < count; i++) r.it.out[i] = mv.slots[i] + (size_t)(b - 1) * 2 * ((size_t)mv.l[i] << c.log_n);
                 count_launch();
                 launch_pdl(c.pdl, batch_galois_permute, dim3(gx, limbs2.p[count]), dim3(256), 0, s, r, limbs2,
                            ptr_list(cts), baby[b - 1].perm);
@@ -1026,30 +1033,33 @@ void ckks_bsgs_matvec_batch(Context &c, uint64_t *ws_base, size_t item_words, ui
             }
             r.sl.mid = r.sl.tm;
         }
-        // 2. giant steps by Horner's rule: result = inner_(B-1); result = rot_G(result) + inner_g
-        bool first = true;
-        for (int g = B - 1; g >= 0; g--) {
-            const int k0 = g * G, nt = std::min(G, D - k0);
-            if (!first) {  // rotate every item's result by G: permute, then key switch (g1) onto (g0, 0)
-                for (int i = 0; i < count; i++) {
-                    r.it.out[i] = const_cast<uint64_t *>(res_ptr[i]);
-                    r.it.b[i] = r.it.ws[i] + r.sl.g + ((size_t)mv.l[i] << c.log_n);
-                }
-                count_launch();
-                launch_pdl(c.pdl, batch_galois_permute, dim3(gx, limbs2.p[count]), dim3(256), 0, s, r, limbs2,
-                           ptr_list(res_ptr), giant.perm);
-                batch_modup_convert(c, r, s);
-                batch_modup_ntt_inner_product(c, r, std::vector<int>(mv.l, mv.l + count), giant.key, s);
-                batch_moddown_combine(c, r, s);
-            }
-            for (int t0 = 0; t0 < nt; t0 += kMvTerms) {
-                Prefix pre = make_prefix(count, [&](int i) { return mv.l[i]; });
-                count_launch();
-                launch_pdl(c.pdl, mul_plain_sum_batch, dim3(gx, pre.p[count]), dim3(256), 0, s, mv, pre, G, t0,
-                           k0 + t0, std::min(kMvTerms, nt - t0), !first || t0 > 0, mods, c.log_n);
-            }
-            if (nt > 0) first = false;
+        // 2. every giant step's inner sum in one launch (slots G - 1 ..), then Horner's rule:
+        //    result = inner_gl (gl the last giant step with diagonals), result = rot_G(result) +
+        //    inner_g for g = gl - 1 .. 0, the addition folded into the rotation's combine
+        const int gl = (D - 1) / G;
+        {
+            Prefix pre = make_prefix(count, [&](int i) { return mv.l[i]; });
+            count_launch();
+            launch_pdl(c.pdl, mul_plain_sums_batch, dim3(gx, pre.p[count]), dim3(256), 0, s, mv, pre, G, gl + 1, D,
+                       mods, c.log_n);
         }
+        auto slot = [&](int i, int k) { return mv.slots[i] + (size_t)k * 2 * ((size_t)mv.l[i] << c.log_n); };
+        for (int i = 0; i < count; i++) res_ptr[i] = slot(i, G - 1 + gl);
+        for (int g = gl - 1; g >= 0; g--) {
+            // rotate every item's result by G (permute, then key switch g1 onto (g0, 0)) plus inner_g
+            for (int i = 0; i < count; i++) {
+                r.it.out[i] = const_cast<uint64_t *>(res_ptr[i]);
+                r.it.b[i] = r.it.ws[i] + r.sl.g + ((size_t)mv.l[i] << c.log_n);
+                r.it.add[i] = slot(i, G - 1 + g);
+            }
+            count_launch();
+            launch_pdl(c.pdl, batch_galois_permute, dim3(gx, limbs2.p[count]), dim3(256), 0, s, r, limbs2,
+                       ptr_list(res_ptr), giant.perm);
+            batch_modup_convert(c, r, s);
+            batch_modup_ntt_inner_product(c, r, std::vector<int>(mv.l, mv.l + count), giant.key, s);
+            batch_moddown_combine(c, r, s);
+        }
+        for (int i = 0; i < count; i++) r.it.add[i] = nullptr;
         // 3. rescale every result
         for (int i = 0; i < count; i++)
             ckks_rescale(c, Workspace{r.it.ws[i], item_words}, res_ptr[i], items[base + i].out, 2, mv.l[i], s);

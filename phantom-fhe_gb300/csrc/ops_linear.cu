@@ -8,6 +8,7 @@
 //   bsgs_complete_from_cpu (baby rotations, inner sums of
 //   multiply_plain, giant rotations by g*G, rescale)        python/src/binding.cu:507-595
 //   encrypt_symmetric / decrypt / generate_one_kswitch_key  src/secretkey.cu:130-341
+#include <algorithm>
 #include <cstdlib>
 #include <stdexcept>
 
@@ -123,6 +124,12 @@ void ckks_rotate(Context &c, const Workspace &w, uint64_t *ct, int l, int step,
 
 // Scratch of the matrix-vector driver: (G + 1) ciphertexts at the key level's data size.
 size_t bsgs_scratch_words(const Context &c, int G) { return (size_t)(G + 1) * 2 * c.nQ * c.n; }
+
+// Scratch per item of the batched form: the babies and one inner sum per giant step (and at least
+// the single call's, which runs when the batch falls back to it).
+size_t bsgs_batch_scratch_words(const Context &c, int G, int B) {
+    return (size_t)std::max(G - 1 + B, G + 1) * 2 * c.nQ * c.n;
+}
 
 void ckks_bsgs_matvec(Context &c, const Workspace &w, uint64_t *scratch, const uint64_t *ct, int l,
                       const uint64_t *diags, int D, int G, int B, const uint64_t *const *const *galois_keys,

@@ -126,6 +126,8 @@ def _load():
     L.fhe_ckks_add.argtypes = [_vp, _vp, _vp, _vp, _sz, _sz, _vp]
     L.fhe_bsgs_scratch_bytes.restype = _sz
     L.fhe_bsgs_scratch_bytes.argtypes = [_vp, _sz]
+    L.fhe_bsgs_batch_scratch_bytes.restype = _sz
+    L.fhe_bsgs_batch_scratch_bytes.argtypes = [_vp, _sz, _sz]
     L.fhe_ckks_bsgs_matvec.argtypes = [_vp, _vp, _vp, _vp, _sz, _vp, _sz, _sz, _sz, ctypes.POINTER(_vp), _vp,
                                        ctypes.c_int, _vp]
     L.fhe_ckks_bsgs_matvec_batch.argtypes = [_vp, _vp, _vp, ctypes.POINTER(_MatvecItem), _sz, _sz, _sz, _sz,
@@ -422,6 +424,10 @@ class Context:
     def bsgs_scratch_bytes(self, G):
         return int(lib.fhe_bsgs_scratch_bytes(self._h, G))
 
+    def bsgs_batch_scratch_bytes(self, G, B):
+        """Scratch per product of bsgs_matvec_batch (babies and inner sums)."""
+        return int(lib.fhe_bsgs_batch_scratch_bytes(self._h, G, B))
+
     def bsgs_matvec(self, ws, scratch, ct, chain_index, diags, D, G, B, galois_keys, out, hoisted=True,
                     stream=None):
         """out <- Rescale(sum_g rot_{gG}(sum_b rot_b(ct) * diags[gG + b]))."""
@@ -432,7 +438,7 @@ class Context:
     def bsgs_matvec_batch(self, ws, scratch, items, D, G, B, galois_keys, stream=None):
         """items: list of (ct, chain_index, diags, out): the hoisted bsgs_matvec of every item in
         one launch per pipeline step (uneven levels); ws from workspace(batch_items=...), scratch
-        of min(len(items), 64) x bsgs_scratch_bytes(G) bytes."""
+        of min(len(items), 64) x bsgs_batch_scratch_bytes(G, B) bytes."""
         arr = (_MatvecItem * len(items))(*[_MatvecItem(ct.data_ptr(), dg.data_ptr(), out.data_ptr(), ci)
                                            for ct, ci, dg, out in items])
         _check(lib.fhe_ckks_bsgs_matvec_batch(self._h, ws._h, _ptr(scratch), arr, len(items), D, G, B,

@@ -153,7 +153,7 @@ def test_matvec128_batch_at_its_parameters_equals_single_calls(mv, pg):
         singles.append(single)
     del one
     wsb = ctx.workspace(batch_items=len(items))
-    scratch = torch.empty(len(items) * ctx.bsgs_scratch_bytes(MV_G) // 8, dtype=torch.int64, device="cuda")
+    scratch = torch.empty(len(items) * ctx.bsgs_batch_scratch_bytes(MV_G, MV_B) // 8, dtype=torch.int64, device="cuda")
     ctx.bsgs_matvec_batch(wsb, scratch, items, MV_D, MV_G, MV_B, gks)
     for (t, chain, dg, out), single in zip(items, singles):
         assert torch.equal(out, single), f"chain {chain}"

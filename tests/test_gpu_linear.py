@@ -192,7 +192,7 @@ def test_bsgs_batch_equals_single_calls(lin, pg, G, B, tc):
             items.append((t, ch, dg, out))
             singles.append(single)
         wsb = ctx.workspace(batch_items=len(items))
-        scratch = torch.empty(len(items) * ctx.bsgs_scratch_bytes(G) // 8, dtype=torch.int64, device="cuda")
+        scratch = torch.empty(len(items) * ctx.bsgs_batch_scratch_bytes(G, B) // 8, dtype=torch.int64, device="cuda")
         ctx.bsgs_matvec_batch(wsb, scratch, items, D, G, B, gks)
     finally:
         ctx.tensor_cores = True
@@ -219,7 +219,7 @@ def test_bsgs_batch_more_than_one_launch_set(lin, pg):
         items.append((t, ch, dg, out))
         singles.append(single)
     wsb = ctx.workspace(batch_items=64)
-    scratch = torch.empty(64 * ctx.bsgs_scratch_bytes(G) // 8, dtype=torch.int64, device="cuda")
+    scratch = torch.empty(64 * ctx.bsgs_batch_scratch_bytes(G, B) // 8, dtype=torch.int64, device="cuda")
     ctx.bsgs_matvec_batch(wsb, scratch, items, D, G, B, gks)
     for i, ((t, ch, dg, out), single) in enumerate(zip(items, singles)):
         assert torch.equal(out, single), f"item {i}, chain {ch}"
