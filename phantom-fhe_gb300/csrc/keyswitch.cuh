@@ -7,6 +7,7 @@
 // below q * 2^64 for q < 2^61).
 #pragma once
 #include "modarith.cuh"
+#include "pdl.cuh"
 
 namespace pfg {
 

@@ -7,22 +7,66 @@
 // Here one CTA owns one output limb jj and one tile of rows and walks every digit d: it finishes
 // T_d[jj]'s transform over its tile (the row pass's stages, from the column pass's lazy output), or
 // reads the digit's own limb (the input itself, already in NTT form), and multiplies the tile into
-// 128-bit accumulators held in registers with the key words at the same positions.  T never goes
-// back to HBM and is never re-read; cx is written once.  The words equal the two-kernel form's
-// (exact modular arithmetic, the sum reduced every 7 terms as there).
+// 128-bit accumulators with the key words at the same positions.  T never goes back to HBM and is
+// never re-read; cx is written once.  The words equal the two-kernel form's (exact modular
+// arithmetic, the sum reduced every 7 terms as there).
 //
 // Layout per thread: the row pass's last register phase leaves each thread E = 8 coefficients in
 // runs of 2^K consecutive positions (the phase's smallest stride is 1), so the key words and the
 // cx stores are 16-byte accesses at those positions, and no shared-memory sweep follows the
 // transform.
+//
+// The accumulators (E coefficients x 2 polynomials x 128 bits a thread, 32 KB a CTA) live in
+// tensor memory, not in registers: thread t owns lane t of the CTA's 64 columns, one 16-column
+// chunk per pair of its coefficients.  Each digit loads a chunk (tcgen05.ld), adds the pair's four
+// products and stores it back (tcgen05.st), so 16 accumulator words are live at a time instead of
+// 64, and the transform runs at the occupancy of the plain row pass.
 #pragma once
 #include "keyswitch.cuh"
 #include "ntt.cuh"
+#include "tc.cuh"
 
 namespace pfg {
 
 constexpr int kFusedE = 8;       // coefficients per thread
 constexpr int kFusedTile = 1024; // coefficients per CTA (128 threads)
+constexpr int kFusedCols = 64;   // tensor-memory columns per CTA: E x 2 polynomials x 4 words
+constexpr int kFusedCtas = 8;    // CTAs per SM: 8 x 64 columns fill the SM's 512
+
+namespace tacc {
+// One warp's 32 lanes x 16 consecutive 32-bit columns, one lane per thread.
+__device__ __forceinline__ void ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+}
+// Waits for this thread's tensor-memory loads; the registers pass through, so no use of them
+// moves above the wait.  These statements carry no memory clobber: the volatile statements keep
+// their order among themselves, and global loads (the key words) may still move across them.
+__device__ __forceinline__ void wait_ld(uint32_t (&r)[16]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]));
+}
+__device__ __forceinline__ void st16(uint32_t taddr, const uint32_t (&r)[16]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+                 ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+                   "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]));
+}
+// Waits for this thread's tensor-memory stores (before it loads the same columns again).
+__device__ __forceinline__ void wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;"); }
+
+__device__ __forceinline__ u128 get(const uint32_t (&r)[16], int k) {
+    return u128{(uint64_t)r[4 * k] | ((uint64_t)r[4 * k + 1] << 32), (uint64_t)r[4 * k + 2] | ((uint64_t)r[4 * k + 3] << 32)};
+}
+__device__ __forceinline__ void put(uint32_t (&r)[16], int k, const u128 &a) {
+    r[4 * k] = (uint32_t)a.lo;
+    r[4 * k + 1] = (uint32_t)(a.lo >> 32);
+    r[4 * k + 2] = (uint32_t)a.hi;
+    r[4 * k + 3] = (uint32_t)(a.hi >> 32);
+}
+}  // namespace tacc
 
 // Shared-memory words of one CTA: its tile as V = TILE / M padded vectors of M = 2^LM words.
 template <int LM>
@@ -32,11 +76,11 @@ __host__ __device__ constexpr int fused_smem_words() {
 
 // One CTA's work: output limb jj (prime table index tbl) of the rows in tile `tile`, over every
 // digit d < beta.  tm and cx are the ciphertext's mod-up and accumulator buffers, sm the CTA's
-// shared tile.
+// shared tile, tacc the tensor-memory address of this thread's lane (column 0).
 template <int LM, class Own>
-__device__ __forceinline__ void modup_ip_tile(uint64_t *sm, const NttTables &T, const uint64_t *tm, const Own &own,
-                                              const uint64_t *const *evk, uint64_t *cx, int l, int nQ, int alpha,
-                                              int beta, int qp, int jj, uint32_t tile) {
+__device__ __forceinline__ void modup_ip_tile(uint64_t *sm, uint32_t tacc, const NttTables &T, const uint64_t *tm,
+                                              const Own &own, const uint64_t *const *evk, uint64_t *cx, int l, int nQ,
+                                              int alpha, int beta, int qp, int jj, uint32_t tile) {
     constexpr int E = kFusedE, TILE = kFusedTile;
     constexpr int M = 1 << LM, TPV = M / E, V = TILE / M, VP = M + M / 16 + 1;
     using F = PhaseAt<LM, true, 0, E>;
@@ -54,9 +98,6 @@ __device__ __forceinline__ void modup_ip_tile(uint64_t *sm, const NttTables &T, 
     uint64_t *vec = sm + vv * VP;
     const int own_d = jj < l ? jj / alpha : -1;
     const TwPair *tw = T.tw + ((size_t)tbl << log_n);
-    u128 a0[E], a1[E];
-#pragma unroll
-    for (int i = 0; i < E; i++) a0[i] = a1[i] = u128{0, 0};
     int terms = 0;
     for (int d = 0; d < beta; d++) {
         uint64_t x[E];
@@ -81,14 +122,10 @@ __device__ __forceinline__ void modup_ip_tile(uint64_t *sm, const NttTables &T, 
 #pragma unroll
             for (int i = 0; i < E; i++) x[i] = fwd_canonical(x[i], md);
         }
-        if (terms == 7) {  // keep every sum below q * 2^64 (reduce128's precondition)
-#pragma unroll
-            for (int i = 0; i < E; i++) {
-                a0[i] = u128{reduce128(a0[i], md), 0};
-                a1[i] = u128{reduce128(a1[i], md), 0};
-            }
-            terms = 1;
-        }
+        // keep every sum below q * 2^64 (reduce128's precondition)
+        const bool fold = terms == 7;
+        if (fold) terms = 1;
+        if (d > 0) tacc::wait_st();  // the previous digit's sums are in tensor memory
         const uint64_t *k0 = evk[d] + ((size_t)tbl << log_n), *k1 = evk[d] + ((size_t)(qp + tbl) << log_n);
 #pragma unroll
         for (int gg = 0; gg < LG; gg++)
@@ -99,13 +136,29 @@ __device__ __forceinline__ void modup_ip_tile(uint64_t *sm, const NttTables &T, 
                 // the key is read once per call: streaming loads
                 const ulonglong2 w0 = __ldcs(reinterpret_cast<const ulonglong2 *>(k0 + idx));
                 const ulonglong2 w1 = __ldcs(reinterpret_cast<const ulonglong2 *>(k1 + idx));
-                mac(a0[i], x[i], w0.x);
-                mac(a0[i + 1], x[i + 1], w0.y);
-                mac(a1[i], x[i], w1.x);
-                mac(a1[i + 1], x[i + 1], w1.y);
+                // chunk i / 2: a0[i], a0[i + 1], a1[i], a1[i + 1]
+                uint32_t r[16];
+                u128 acc[4] = {u128{0, 0}, u128{0, 0}, u128{0, 0}, u128{0, 0}};
+                if (d > 0) {
+                    tacc::ld16(tacc + 8 * i, r);
+                    tacc::wait_ld(r);
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        acc[k] = tacc::get(r, k);
+                        if (fold) acc[k] = u128{reduce128(acc[k], md), 0};
+                    }
+                }
+                mac(acc[0], x[i], w0.x);
+                mac(acc[1], x[i + 1], w0.y);
+                mac(acc[2], x[i], w1.x);
+                mac(acc[3], x[i + 1], w1.y);
+#pragma unroll
+                for (int k = 0; k < 4; k++) tacc::put(r, k, acc[k]);
+                tacc::st16(tacc + 8 * i, r);
             }
         terms++;
     }
+    tacc::wait_st();
     const size_t total = (size_t)qlp << log_n;
     uint64_t *c0 = cx + ((size_t)jj << log_n);
 #pragma unroll
@@ -114,22 +167,55 @@ __device__ __forceinline__ void modup_ip_tile(uint64_t *sm, const NttTables &T, 
         for (int j = 0; j < LS; j += 2) {
             const uint32_t idx = vbase + grp_elem<LM, L::K, L::SA, E>(u, gg, j);
             const int i = gg * LS + j;
+            uint32_t r[16];
+            tacc::ld16(tacc + 8 * i, r);
+            tacc::wait_ld(r);
             *reinterpret_cast<ulonglong2 *>(c0 + idx) =
-                    make_ulonglong2(reduce128(a0[i], md), reduce128(a0[i + 1], md));
+                    make_ulonglong2(reduce128(tacc::get(r, 0), md), reduce128(tacc::get(r, 1), md));
             *reinterpret_cast<ulonglong2 *>(c0 + total + idx) =
-                    make_ulonglong2(reduce128(a1[i], md), reduce128(a1[i + 1], md));
+                    make_ulonglong2(reduce128(tacc::get(r, 2), md), reduce128(tacc::get(r, 3), md));
         }
 }
 
+// The CTA's tensor-memory columns: allocated by warp 0 after the grid dependency wait (so no CTA
+// holds columns while it waits on another grid), freed once every thread's accesses are done.
+// Eight CTAs of 64 columns fill an SM; a ninth would wait in the allocation until one finishes.
+struct FusedTmem {
+    uint32_t base;
+    __device__ __forceinline__ static uint32_t alloc(uint32_t *slot) {
+        if (threadIdx.x < 32) tc::tmem_alloc(slot, kFusedCols);
+        tc::fence_before();
+        __syncthreads();
+        tc::fence_after();
+        return *slot;
+    }
+    __device__ __forceinline__ static void free(uint32_t base) {
+        tc::fence_before();
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            tc::fence_after();
+            tc::tmem_free(base, kFusedCols);
+        }
+    }
+    // this thread's lane: warp w reads and writes lanes 32 w .. 32 w + 31
+    __device__ __forceinline__ static uint32_t lane(uint32_t base) {
+        return base + ((uint32_t)(threadIdx.x & ~31u) << 16);
+    }
+};
+
 // One ciphertext: grid (N / TILE row tiles, l + alpha output limbs).
 template <int LM, class Own>
-__global__ void __launch_bounds__(kFusedTile / kFusedE, 4)
+__global__ void __launch_bounds__(kFusedTile / kFusedE, kFusedCtas)
         ks_modup_ip(NttTables T, const uint64_t *tm, Own own, const uint64_t *const *evk, uint64_t *cx, int l,
                     int nQ, int alpha, int beta, int qp) {
     pdl_wait();
     pdl_release();
     __shared__ uint64_t sm[fused_smem_words<LM>()];
-    modup_ip_tile<LM>(sm, T, tm, own, evk, cx, l, nQ, alpha, beta, qp, (int)blockIdx.y, blockIdx.x);
+    __shared__ uint32_t tslot;
+    const uint32_t tbase = FusedTmem::alloc(&tslot);
+    modup_ip_tile<LM>(sm, FusedTmem::lane(tbase), T, tm, own, evk, cx, l, nQ, alpha, beta, qp, (int)blockIdx.y,
+                      blockIdx.x);
+    FusedTmem::free(tbase);
 }
 
 }  // namespace pfg

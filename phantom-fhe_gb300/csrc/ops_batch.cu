@@ -418,18 +418,21 @@ struct BatchOwn {
 // dropped q_tk.  The item index is the fastest grid dimension, so the blocks of all items that
 // read the same key tile (tk, tile) run together and the key comes from HBM once per batch.
 template <int LM>
-__global__ void __launch_bounds__(kFusedTile / kFusedE, 4)
+__global__ void __launch_bounds__(kFusedTile / kFusedE, kFusedCtas)
         ks_modup_ip_batch(BItemsRef r, NttTables T, const uint64_t *const *evk, int nQ, int qp) {
     pdl_wait();
     pdl_release();
     __shared__ uint64_t sm[fused_smem_words<LM>()];
+    __shared__ uint32_t tslot;
     const int c = (int)blockIdx.x, tk = (int)blockIdx.z, l = r.it.l[c], alpha = r.alpha, log_n = r.log_n;
-    if (tk < nQ && tk >= l) return;  // uniform per block, before any barrier
+    if (tk < nQ && tk >= l) return;  // uniform per block, before any barrier or allocation
     const int jj = tk < nQ ? tk : l + (tk - nQ);
     uint64_t *ws = r.it.ws[c];
     const BatchOwn own{r.it.a[c], r.it.b[c], (long long)l << log_n, r.it.keyswitch, log_n};
-    modup_ip_tile<LM>(sm, T, ws + r.sl.tm, own, evk, ws + r.sl.cx, l, nQ, alpha, (l + alpha - 1) / alpha, qp, jj,
-                      blockIdx.y);
+    const uint32_t tbase = FusedTmem::alloc(&tslot);
+    modup_ip_tile<LM>(sm, FusedTmem::lane(tbase), T, ws + r.sl.tm, own, evk, ws + r.sl.cx, l, nQ, alpha,
+                      (l + alpha - 1) / alpha, qp, jj, blockIdx.y);
+    FusedTmem::free(tbase);
 }
 
 // Rescale-folded mod-down conversion for (item, poly) = block row (see rescale_fused_bconv).
