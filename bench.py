@@ -195,7 +195,9 @@ def matvec_bench(pg, torch, timed, stream, rank, profile_only=False):
     levels drawn uniformly from 3..20, real keys from seeded randomness, matrix entries uniform
     in [-1, 1].  Hoisted form: baby steps 1..10 share one mod-up, giant steps by Horner's rule
     with rotations by 11 only (11 Galois keys); the reference's loop (giant rotations by g*11,
-    21 keys) runs beside it.  Slot error of the decrypted results against an FP64 matmul."""
+    21 keys) runs beside it.  The per-vector calls read diagonals encoded at each vector's level;
+    the batched call reads one array encoded at the top level (its first l limbs are the same
+    words).  Slot error of the decrypted results against an FP64 matmul."""
     from phantom_gb300.ckks import CkksEncoder, SecretKey
     n, d, G, B = N, MV_DIM, MV_G, MV_B
     mods = pg.create_coeff_modulus(n, MV_BITS)
@@ -219,7 +221,6 @@ def matvec_bench(pg, torch, timed, stream, rank, profile_only=False):
     diags_at = {}
     for lv in sorted(set(levels)):
         diags_at[lv] = diag_full[:, :lv].contiguous()
-    del diag_full
     xs, cts, outs = [], [], []
     for lv in levels:
         x = rng.uniform(-1, 1, size=d) + 1j * rng.uniform(-1, 1, size=d)
@@ -234,11 +235,12 @@ def matvec_bench(pg, torch, timed, stream, rank, profile_only=False):
         for (ct, chain, lv), o in zip(cts, outs):
             ctx.bsgs_matvec(ws, scratch, ct, chain, diags_at[lv], d, G, B, gks, o, hoisted=hoisted, stream=stream)
 
-    # the same 32 products through the batched call: one launch per pipeline step for all of them
+    # the same 32 products through the batched call: one launch per pipeline step for all of them,
+    # every item reading the one matrix's diagonals encoded at the top level (the first l limbs)
     wsb = ctx.workspace(batch_items=MV_BATCH)
     bscratch = torch.empty(MV_BATCH * ctx.bsgs_batch_scratch_bytes(G, B) // 8, dtype=torch.int64, device="cuda")
     bouts = [torch.empty_like(o) for o in outs]
-    bitems = [(ct, chain, diags_at[lv], o) for (ct, chain, lv), o in zip(cts, bouts)]
+    bitems = [(ct, chain, diag_full, o) for (ct, chain, lv), o in zip(cts, bouts)]
 
     def batched():
         ctx.bsgs_matvec_batch(wsb, bscratch, bitems, d, G, B, gks, stream=stream)

@@ -332,9 +332,13 @@ int fhe_ckks_bsgs_matvec(const fhe_context *ctx, fhe_workspace *ws, uint64_t *sc
 size_t fhe_bsgs_batch_scratch_bytes(const fhe_context *ctx, size_t G, size_t B);
 typedef struct fhe_matvec_item {
     const uint64_t *ct;     /* 2 polys at chain_index, NTT form */
-    const uint64_t *diags;  /* D plaintexts [D][limbs at chain_index][N], NTT form */
+    const uint64_t *diags;  /* D plaintexts [D][diag_limbs][N], NTT form; limbs [0, l) are read */
     uint64_t *out;          /* 2 polys at chain_index + 1 */
     size_t chain_index;
+    size_t diag_limbs;      /* limbs per diagonal (its stride), from l (the limbs at chain_index) to
+                             * the data primes; 0 means l.  Items of one matrix may share one array
+                             * encoded at the top level: the batch then reads each diagonal tile once
+                             * for all of them. */
 } fhe_matvec_item;
 int fhe_ckks_bsgs_matvec_batch(const fhe_context *ctx, fhe_workspace *ws, uint64_t *scratch,
                                const fhe_matvec_item *items, size_t count, size_t D, size_t G, size_t B,

@@ -683,7 +683,10 @@ int fhe_ckks_bsgs_matvec_batch(const fhe_context *ctx, fhe_workspace *ws, uint64
             need_ptr(items[i].out, "items[i].out");
             const int l = level_of(c, items[i].chain_index);
             if (l < 2) throw std::invalid_argument("end of modulus switching chain reached");
-            v.push_back(pfg::MatvecItem{items[i].ct, items[i].diags, items[i].out, l});
+            const size_t dl = items[i].diag_limbs ? items[i].diag_limbs : (size_t)l;
+            if (dl < (size_t)l || dl > (size_t)c.nQ)
+                throw std::invalid_argument("items[i].diag_limbs must lie between the item's limbs and the data primes");
+            v.push_back(pfg::MatvecItem{items[i].ct, items[i].diags, items[i].out, l, (int)dl});
         }
         pfg::ckks_bsgs_matvec_batch(c, w.base, ws->words / ws->items, scratch,
                                     pfg::bsgs_batch_scratch_words(c, (int)G, (int)B), v,

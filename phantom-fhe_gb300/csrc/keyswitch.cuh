@@ -8,6 +8,7 @@
 #pragma once
 #include "modarith.cuh"
 #include "pdl.cuh"
+#include "pdl.cuh"
 
 namespace pfg {
 

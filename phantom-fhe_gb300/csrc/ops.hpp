@@ -36,11 +36,11 @@ struct KsItem {  // one key switch of a batch: ct (2 polys, in place) += KeySwit
     int l;
 };
 
-struct MatvecItem {  // one matrix-vector product of a batch: ct (2 polys) and diags [D][l][N] at level l
+struct MatvecItem {  // one matrix-vector product of a batch: ct (2 polys) at level l, diags [D][dl][N]
     const uint64_t *ct;
-    const uint64_t *diags;
-    uint64_t *out;  // 2 polys at level l - 1
-    int l;
+    const uint64_t *diags;  // limbs [0, l) of each diagonal are read; dl >= l is the limb stride
+    uint64_t *out;          // 2 polys at level l - 1
+    int l, dl;
 };
 
 void ntt_forward(const Context &c, uint64_t *data, int polys, int limbs, int start, cudaStream_t s);
@@ -81,7 +81,7 @@ size_t bsgs_scratch_words(const Context &c, int G);
 size_t bsgs_batch_scratch_words(const Context &c, int G, int B);
 void ckks_bsgs_matvec(Context &c, const Workspace &w, uint64_t *scratch, const uint64_t *ct, int l,
                       const uint64_t *diags, int D, int G, int B, const uint64_t *const *const *galois_keys,
-                      uint64_t *out, bool hoisted, cudaStream_t s);
+                      uint64_t *out, bool hoisted, cudaStream_t s, int diag_limbs = 0);
 void ckks_encrypt_sk(const Context &c, const uint64_t *m, const uint64_t *s_ntt, const uint64_t *a, const int64_t *e,
                      uint64_t *out, int l, cudaStream_t st);
 void ckks_decrypt(const Context &c, const uint64_t *ct, const uint64_t *s_ntt, uint64_t *m, int l, cudaStream_t st);

@@ -856,92 +856,116 @@ __global__ void __launch_bounds__(256) batch_galois_permute(BItemsRef r, Prefix 
         out[i] = in[__ldg(perm + i)];
 }
 
-// Hoisted inner product for key limb blockIdx.y over every item that has it: cx_c = sum_d
-// perm(T_d) * key_d with the shared mod-up T of each item (region tm) read through the
-// permutation and the own limbs from the item's permuted c1 (region g, polynomial 1); the key
-// tile comes from HBM for the first item and from cache for the others.  The single-call form is
-// ks_inner_product_hoisted (one step).
+// Hoisted inner product, block (item c, row tile, key limb tk): cx_c = sum_d perm(T_d) * key_d
+// over two coefficients per thread, with item c's shared mod-up T (region tm) read through the
+// permutation and the own limbs from its permuted c1 (region g, polynomial 1).  The item index is
+// the fastest grid dimension, so the blocks of all items that read one key tile run together and
+// the tile comes from HBM once per launch; the parallelism is in the grid, each thread's digit
+// chain is short.  The permutation keeps every warp's 32 words within 8 sectors (a Galois
+// automorphism of the bit-reversed NTT order moves words only inside aligned 256-byte blocks).
+// The single-call form is ks_inner_product_hoisted (one step).
 __global__ void __launch_bounds__(256) ks_inner_product_hoisted_batch(BItemsRef r, const uint32_t *perm,
                                                                       const uint64_t *const *key, const Mod *mods,
                                                                       int nQ, int qp) {
     pdl_wait();
     pdl_release();
-    const int tk = blockIdx.y, alpha = r.alpha, log_n = r.log_n;
+    const int c = (int)blockIdx.x, tk = (int)blockIdx.z, l = r.it.l[c], alpha = r.alpha, log_n = r.log_n;
+    if (tk >= l && tk < nQ) return;  // this level has dropped q_tk
+    const int jj = tk < nQ ? tk : l + (tk - nQ), qlp = l + alpha, beta = (l + alpha - 1) / alpha;
+    const int own_d = jj < l ? jj / alpha : -1;
     const Mod m = mods[tk];
-    const size_t n = (size_t)1 << log_n;
-    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
-        const uint32_t src = __ldg(perm + idx);
-        for (int c = 0; c < r.it.count; c++) {
-            const int l = r.it.l[c];
-            if (tk >= l && tk < nQ) continue;  // this level has dropped q_tk
-            const int jj = tk < nQ ? tk : l + (tk - nQ), qlp = l + alpha, beta = (l + alpha - 1) / alpha;
-            const int own_d = jj < l ? jj / alpha : -1;
-            const uint64_t *ws = r.it.ws[c];
-            const uint64_t *tm = ws + r.sl.tm, *g1 = ws + r.sl.g + ((size_t)l << log_n);
-            u128 a{0, 0}, b{0, 0};
-            int terms = 0;
-            for (int d = 0; d < beta; d++) {
-                const uint64_t x = d == own_d ? g1[((size_t)jj << log_n) + idx]
-                                              : tm[(((size_t)d * qlp + jj) << log_n) + src];
-                const uint64_t *kd = key[d];
-                if (terms == 7) {
-                    a = u128{reduce128(a, m), 0};
-                    b = u128{reduce128(b, m), 0};
-                    terms = 1;
-                }
-                mac(a, x, __ldg(kd + ((size_t)tk << log_n) + idx));
-                mac(b, x, __ldg(kd + ((size_t)(qp + tk) << log_n) + idx));
-                terms++;
-            }
-            uint64_t *cx = r.it.ws[c] + r.sl.cx + ((size_t)jj << log_n) + idx;
-            cx[0] = reduce128(a, m);
-            cx[(size_t)qlp << log_n] = reduce128(b, m);
+    const uint32_t idx = 2 * (blockIdx.y * blockDim.x + threadIdx.x);
+    const uint64_t *ws = r.it.ws[c];
+    const uint64_t *tm = ws + r.sl.tm, *g1 = ws + r.sl.g + ((size_t)l << log_n);
+    const uint2 src = *reinterpret_cast<const uint2 *>(perm + idx);
+    u128 a0{0, 0}, a1{0, 0}, b0{0, 0}, b1{0, 0};
+    int terms = 0;
+    for (int d = 0; d < beta; d++) {
+        uint64_t x0, x1;
+        if (d == own_d) {
+            const ulonglong2 v = ld2(g1 + ((size_t)jj << log_n) + idx);
+            x0 = v.x;
+            x1 = v.y;
+        } else {
+            const uint64_t *t = tm + (((size_t)d * qlp + jj) << log_n);
+            x0 = t[src.x];
+            x1 = t[src.y];
         }
+        // each key tile serves every item's block: cached loads
+        const uint64_t *kd = key[d];
+        const ulonglong2 k0 = __ldg(reinterpret_cast<const ulonglong2 *>(kd + ((size_t)tk << log_n) + idx));
+        const ulonglong2 k1 = __ldg(reinterpret_cast<const ulonglong2 *>(kd + ((size_t)(qp + tk) << log_n) + idx));
+        if (terms == 7) {
+            a0 = u128{reduce128(a0, m), 0};
+            a1 = u128{reduce128(a1, m), 0};
+            b0 = u128{reduce128(b0, m), 0};
+            b1 = u128{reduce128(b1, m), 0};
+            terms = 1;
+        }
+        mac(a0, x0, k0.x);
+        mac(a1, x1, k0.y);
+        mac(b0, x0, k1.x);
+        mac(b1, x1, k1.y);
+        terms++;
     }
+    uint64_t *cx = r.it.ws[c] + r.sl.cx + ((size_t)jj << log_n) + idx;
+    st2(cx, reduce128(a0, m), reduce128(a1, m));
+    st2(cx + ((size_t)qlp << log_n), reduce128(b0, m), reduce128(b1, m));
 }
 
 // Per-item pointers of a batched matrix-vector product.
 struct MvItems {
     const uint64_t *ct[kMaxBatch];     // baby 0 (the input), 2 polys at level l
     uint64_t *slots[kMaxBatch];        // babies 1..G-1, then one inner sum per giant step: [G-1+B][2][l][N]
-    const uint64_t *diags[kMaxBatch];  // [D][l][N]
-    int l[kMaxBatch];
+    const uint64_t *diags[kMaxBatch];  // [D][dl][N], limbs [0, l) read
+    int l[kMaxBatch], dl[kMaxBatch];
 };
 
 // Every giant step's inner sum of every item in one launch: slot G - 1 + g of item c receives
 // inner_g = sum_b baby_b * diag_(g G + b) (128-bit accumulation; the same words as the single
-// call's mul_plain_sum: exact modular arithmetic).  Block row = (item, limb).  Each thread walks
-// the giant steps over its coefficients and reads its coefficient of every baby again for each
-// one; after the first giant step those words (G x 2 x 8 B a thread) come from L1, so the babies
-// are read from HBM once per batch, not once per giant step.
-__global__ void __launch_bounds__(256) mul_plain_sums_batch(MvItems mv, Prefix pre, int G, int steps, int D,
-                                                            const Mod *mods, int log_n) {
+// call's mul_plain_sum: exact modular arithmetic).  Block (item c, tile of 512 coefficients, limb
+// j), two coefficients per thread with 16-byte loads.  The item index is the fastest grid
+// dimension: when items share one diagonal array (one matrix, dl its limb stride) the blocks that
+// read a diagonal tile run together and the tile comes from HBM about once per launch, not once
+// per item.  Each thread walks the giant steps and reads its words of every baby again for each
+// one, from L1 or L2 after the first.
+__global__ void __launch_bounds__(256) mul_plain_sums_batch(MvItems mv, int G, int steps, int D, const Mod *mods,
+                                                            int log_n) {
     pdl_wait();
     pdl_release();
-    const int c = pre.find(blockIdx.y), j = blockIdx.y - pre.p[c], l = mv.l[c];
-    const size_t n = (size_t)1 << log_n, lps = (size_t)l << log_n, cts = 2 * lps, jo = (size_t)j << log_n;
+    const int c = (int)blockIdx.x, j = (int)blockIdx.z, l = mv.l[c];
+    if (j >= l) return;  // uniform per block
+    const size_t lps = (size_t)l << log_n, cts = 2 * lps, jo = (size_t)j << log_n;
+    const size_t dstride = (size_t)mv.dl[c] << log_n;
+    const uint32_t i = 2 * (blockIdx.y * blockDim.x + threadIdx.x);
     const Mod m = mods[j];
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        for (int g = 0; g < steps; g++) {
-            const int nt = min(G, D - g * G);
-            u128 a0{0, 0}, a1{0, 0};
-            int terms = 0;
-            for (int b = 0; b < nt; b++) {
-                const uint64_t *ct = b == 0 ? mv.ct[c] : mv.slots[c] + (size_t)(b - 1) * cts;
-                const uint64_t p = __ldcs(mv.diags[c] + (size_t)(g * G + b) * lps + jo + i);
-                if (terms == 7) {
-                    a0 = u128{reduce128(a0, m), 0};
-                    a1 = u128{reduce128(a1, m), 0};
-                    terms = 1;
-                }
-                mac(a0, __ldg(ct + jo + i), p);
-                mac(a1, __ldg(ct + lps + jo + i), p);
-                terms++;
+    const uint64_t *dg = mv.diags[c] + jo + i;
+    for (int g = 0; g < steps; g++) {
+        const int nt = min(G, D - g * G);
+        u128 a0{0, 0}, a1{0, 0}, b0{0, 0}, b1{0, 0};  // polynomial 0, 1 at coefficients i, i + 1
+        int terms = 0;
+#pragma unroll 2
+        for (int b = 0; b < nt; b++) {
+            const uint64_t *ct = (b == 0 ? mv.ct[c] : mv.slots[c] + (size_t)(b - 1) * cts) + jo + i;
+            const ulonglong2 p = __ldg(reinterpret_cast<const ulonglong2 *>(dg + (size_t)(g * G + b) * dstride));
+            const ulonglong2 x = __ldg(reinterpret_cast<const ulonglong2 *>(ct));
+            const ulonglong2 y = __ldg(reinterpret_cast<const ulonglong2 *>(ct + lps));
+            if (terms == 7) {
+                a0 = u128{reduce128(a0, m), 0};
+                a1 = u128{reduce128(a1, m), 0};
+                b0 = u128{reduce128(b0, m), 0};
+                b1 = u128{reduce128(b1, m), 0};
+                terms = 1;
             }
-            uint64_t *out = mv.slots[c] + (size_t)(G - 1 + g) * cts + jo + i;
-            out[0] = reduce128(a0, m);
-            out[lps] = reduce128(a1, m);
+            mac(a0, x.x, p.x);
+            mac(a1, x.y, p.y);
+            mac(b0, y.x, p.x);
+            mac(b1, y.y, p.y);
+            terms++;
         }
+        uint64_t *out = mv.slots[c] + (size_t)(G - 1 + g) * cts + jo + i;
+        st2(out, reduce128(a0, m), reduce128(a1, m));
+        st2(out + lps, reduce128(b0, m), reduce128(b1, m));
     }
 }
 
@@ -962,7 +986,7 @@ void ckks_bsgs_matvec_batch(Context &c, uint64_t *ws_base, size_t item_words, ui
         for (size_t i = 0; i < items.size(); i++)
             ckks_bsgs_matvec(c, Workspace{ws_base + (i % kMaxBatch) * item_words, item_words},
                              scratch_base + (i % kMaxBatch) * scratch_words, items[i].ct, items[i].l, items[i].diags,
-                             D, G, B, galois_keys, items[i].out, true, s);
+                             D, G, B, galois_keys, items[i].out, true, s, items[i].dl);
         return;
     }
     auto step_key = [&](int step) {
@@ -1000,6 +1024,7 @@ void ckks_bsgs_matvec_batch(Context &c, uint64_t *ws_base, size_t item_words, ui
             mv.slots[i] = scratch_base + (size_t)i * scratch_words;
             mv.diags[i] = m.diags;
             mv.l[i] = m.l;
+            mv.dl[i] = m.dl;
             cts[i] = m.ct;
             (void)cw;
         }
@@ -1030,7 +1055,8 @@ void ckks_bsgs_matvec_batch(Context &c, uint64_t *ws_base, size_t item_words, ui
                 launch_pdl(c.pdl, batch_galois_permute, dim3(gx, limbs2.p[count]), dim3(256), 0, s, r, limbs2,
                            ptr_list(cts), baby[b - 1].perm);
                 count_launch();
-                launch_pdl(c.pdl, ks_inner_product_hoisted_batch, dim3(gx, (unsigned)(nQ + alpha)), dim3(256), 0, s, r,
+                launch_pdl(c.pdl, ks_inner_product_hoisted_batch,
+                           dim3((unsigned)count, (unsigned)(c.n / 512), (unsigned)(nQ + alpha)), dim3(256), 0, s, r,
                            baby[b - 1].perm, baby[b - 1].key, mods, nQ, nQ + alpha);
                 batch_moddown_combine(c, r, s);
             }
@@ -1041,10 +1067,11 @@ void ckks_bsgs_matvec_batch(Context &c, uint64_t *ws_base, size_t item_words, ui
         //    inner_g for g = gl - 1 .. 0, the addition folded into the rotation's combine
         const int gl = (D - 1) / G;
         {
-            Prefix pre = make_prefix(count, [&](int i) { return mv.l[i]; });
+            int lmax = 0;
+            for (int i = 0; i < count; i++) lmax = std::max(lmax, mv.l[i]);
             count_launch();
-            launch_pdl(c.pdl, mul_plain_sums_batch, dim3(gx, pre.p[count]), dim3(256), 0, s, mv, pre, G, gl + 1, D,
-                       mods, c.log_n);
+            launch_pdl(c.pdl, mul_plain_sums_batch, dim3((unsigned)count, (unsigned)(c.n / 512), (unsigned)lmax),
+                       dim3(256), 0, s, mv, G, gl + 1, D, mods, c.log_n);
         }
         auto slot = [&](int i, int k) { return mv.slots[i] + (size_t)k * 2 * ((size_t)mv.l[i] << c.log_n); };
         for (int i = 0; i < count; i++) res_ptr[i] = slot(i, G - 1 + gl);

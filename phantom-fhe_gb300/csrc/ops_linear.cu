@@ -133,8 +133,10 @@ size_t bsgs_batch_scratch_words(const Context &c, int G, int B) {
 
 void ckks_bsgs_matvec(Context &c, const Workspace &w, uint64_t *scratch, const uint64_t *ct, int l,
                       const uint64_t *diags, int D, int G, int B, const uint64_t *const *const *galois_keys,
-                      uint64_t *out, bool hoisted, cudaStream_t s) {
+                      uint64_t *out, bool hoisted, cudaStream_t s, int diag_limbs) {
     const size_t lps = (size_t)l << c.log_n, cts = 2 * lps;
+    // one diagonal every diag_limbs limbs (its first l are read); 0: the diagonals are [D][l][N]
+    const size_t dstride = (size_t)(diag_limbs > 0 ? diag_limbs : l) << c.log_n;
     // babies[0] = ct; babies[b] (b >= 1) in scratch; then `inner` and `result`
     std::vector<const uint64_t *> babies(G);
     babies[0] = ct;
@@ -153,7 +155,7 @@ void ckks_bsgs_matvec(Context &c, const Workspace &w, uint64_t *scratch, const u
             const int k = g * G + b;
             if (k >= D) break;
             cv.push_back(babies[b]);
-            pv.push_back(diags + (size_t)k * lps);
+            pv.push_back(diags + (size_t)k * dstride);
         }
     };
     std::vector<const uint64_t *> cv, pv;

@@ -48,7 +48,7 @@ class _KsItem(ctypes.Structure):
 
 
 class _MatvecItem(ctypes.Structure):
-    _fields_ = [("ct", _vp), ("diags", _vp), ("out", _vp), ("chain_index", _sz)]
+    _fields_ = [("ct", _vp), ("diags", _vp), ("out", _vp), ("chain_index", _sz), ("diag_limbs", _sz)]
 
 
 class Tuning(ctypes.Structure):
@@ -439,7 +439,10 @@ class Context:
         """items: list of (ct, chain_index, diags, out): the hoisted bsgs_matvec of every item in
         one launch per pipeline step (uneven levels); ws from workspace(batch_items=...), scratch
         of min(len(items), 64) x bsgs_batch_scratch_bytes(G, B) bytes."""
-        arr = (_MatvecItem * len(items))(*[_MatvecItem(ct.data_ptr(), dg.data_ptr(), out.data_ptr(), ci)
+        # diags [D][limbs][N]: the limb count is the array's stride (an array encoded at a higher
+        # level than the item's serves it too)
+        arr = (_MatvecItem * len(items))(*[_MatvecItem(ct.data_ptr(), dg.data_ptr(), out.data_ptr(), ci,
+                                                       dg.shape[1] if dg.dim() == 3 else 0)
                                            for ct, ci, dg, out in items])
         _check(lib.fhe_ckks_bsgs_matvec_batch(self._h, ws._h, _ptr(scratch), arr, len(items), D, G, B,
                                               self._gk_array(galois_keys), _stream(stream)))

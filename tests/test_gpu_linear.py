@@ -201,6 +201,44 @@ def test_bsgs_batch_equals_single_calls(lin, pg, G, B, tc):
     assert ctx.device_status() == 0
 
 
+@pytest.mark.parametrize("tc", [True, False])
+def test_bsgs_batch_shared_diagonals(lin, pg, tc):
+    """Items at uneven levels all reading one diagonal array encoded at the top level (its limb
+    count is the stride, the first l limbs are read) give the words of single calls on contiguous
+    per-level copies; without the tensor-core conversions the batch's single calls take the same
+    stride."""
+    ctx, oc, mods, keys, gks, ws = lin
+    rng = np.random.default_rng(48)
+    top = ctx.level(1)
+    shared = pg.to_device(_diags(rng, mods, top, ctx.n))
+    chains = [2, 1, 4, 3, 2]
+    items, singles = [], []
+    one = torch.empty(ctx.bsgs_scratch_bytes(G) // 8, dtype=torch.int64, device="cuda")
+    ctx.tensor_cores = tc
+    try:
+        for ch in chains:
+            l = ctx.level(ch)
+            t = pg.to_device(O.random_residues(rng, mods[:l], ctx.n, 2))
+            out = torch.empty((2, l - 1, ctx.n), dtype=torch.int64, device="cuda")
+            single = torch.empty_like(out)
+            ctx.bsgs_matvec(ws, one, t, ch, shared[:, :l].contiguous(), D, G, B, gks, single, hoisted=True)
+            items.append((t, ch, shared, out))
+            singles.append(single)
+        wsb = ctx.workspace(batch_items=len(items))
+        scratch = torch.empty(len(items) * ctx.bsgs_batch_scratch_bytes(G, B) // 8, dtype=torch.int64, device="cuda")
+        ctx.bsgs_matvec_batch(wsb, scratch, items, D, G, B, gks)
+    finally:
+        ctx.tensor_cores = True
+    for (t, ch, dg, out), single in zip(items, singles):
+        assert torch.equal(out, single), f"chain {ch}, tensor_cores={tc}"
+    # a diagonal array with fewer limbs than the item's level is refused
+    l = ctx.level(1)
+    short = shared[:, : l - 1].contiguous()
+    with pytest.raises(RuntimeError):
+        ctx.bsgs_matvec_batch(wsb, scratch, [(items[1][0], 1, short, items[1][3])], D, G, B, gks)
+    assert ctx.device_status() == 0
+
+
 def test_bsgs_batch_more_than_one_launch_set(lin, pg):
     """70 products (more than one launch set of 64, the second one reusing the first's scratch)
     give the single calls' words."""

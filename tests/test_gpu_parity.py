@@ -434,6 +434,42 @@ def test_batch_multiply_relin_rescale_uneven_levels_small(small, pg, fused):
     assert ctx.device_status() == 0
 
 
+@pytest.mark.parametrize("fused", [True, False])
+def test_many_digits_fold_the_digit_sums(pg, fused):
+    """One special prime over ten data primes: beta = l digits (8 to 10), so the 128-bit digit
+    sums of the inner product are reduced after every 7 terms (in the fused kernel a tensor-memory
+    load, reduce and store of the running sums).  Single key switch, HMult + relin + rescale and
+    the batched call, each word for word against the oracle."""
+    ctx, oc, mods, nq = _ckks(pg, 4096, [60] + [40] * 9 + [60], 1)
+    ws = ctx.workspace()
+    rng = np.random.default_rng(1010)
+    key = _key(rng, mods, ctx.dnum, ctx.n)
+    k = pg.KeySwitchKey(pg.to_device(key))
+    ctx.fused_keyswitch = fused
+    try:
+        for chain in (1, 2, 3):  # l = 10, 9, 8
+            l = ctx.level(chain)
+            ct = O.random_residues(rng, mods[:l], ctx.n, 2)
+            c2 = O.random_residues(rng, mods[:l], ctx.n, 1)[0]
+            t = pg.to_device(ct)
+            ctx.keyswitch(ws, t, pg.to_device(c2), chain, k)
+            _eq(t, oc.keyswitch(l, ct, c2, key), f"key switch, {l} digits, fused={fused}")
+            a = O.random_residues(rng, mods[:l], ctx.n, 2)
+            b = O.random_residues(rng, mods[:l], ctx.n, 2)
+            out = torch.empty((2, l - 1, ctx.n), dtype=torch.int64, device="cuda")
+            ctx.multiply_relin_rescale(ws, pg.to_device(a), pg.to_device(b), out, chain, k)
+            _eq(out, oc.rescale(l, oc.ckks_mul_relin(l, a, b, key)), f"HMult+relin+rescale, {l} digits, fused={fused}")
+        chains = [1, 3, 2, 1]
+        key_b, kb, items, host = _batch_case(pg, ctx, mods, chains, 1011)
+        wsb = ctx.workspace(batch_items=len(chains))
+        ctx.multiply_relin_rescale_batch(wsb, items, kb)
+        for (a, b, l), (_, _, out, ch) in zip(host, items):
+            _eq(out, oc.rescale(l, oc.ckks_mul_relin(l, a, b, key_b)), f"batch item, {l} digits, fused={fused}")
+    finally:
+        ctx.fused_keyswitch = True
+    assert ctx.device_status() == 0
+
+
 def test_batch_more_than_one_launch_set(small, pg):
     ctx, oc, mods, nq, ws = small
     chains = [1 + (i * 7) % 5 for i in range(70)]  # 70 > 64: two launch sets
