@@ -12,7 +12,10 @@
  *    ciphertext = [size][coeff_modulus_size][N] uint64 limb-major (include/ciphertext.h:44-72),
  *    key-switching key = dnum device pointers (a device array, as returned by
  *    PhantomRelinKey::public_keys_ptr(), include/secretkey.h:124-127), each to [2][QP][N]
- *    in NTT form.
+ *    in NTT form.  Device buffers of residues (ciphertexts, plaintexts, keys, diagonals,
+ *    scratch) must start on a 16-byte boundary: the kernels move them in 16-byte vectors.
+ *    Every cudaMalloc / caching-allocator block is 256-byte aligned, and limb offsets
+ *    (multiples of N words) keep that alignment.
  *  - `chain_index` follows the reference: 0 is the key level (QP), 1 the full data level Q,
  *    each further index drops one prime (src/context.cu:141-158).
  *  - Calls enqueue work on `stream` (a cudaStream_t; NULL = the legacy default stream) and
