@@ -239,6 +239,35 @@ def test_bsgs_batch_shared_diagonals(lin, pg, tc):
     assert ctx.device_status() == 0
 
 
+def test_bsgs_batch_many_babies_ragged(pg):
+    """G = 14 babies (13 hoisted baby rotations, every giant step's inner sum over 14 diagonals)
+    and a ragged last giant step (D = 20): every output equals the single call's words."""
+    n = 4096
+    mods = pg.create_coeff_modulus(n, [60, 40, 40, 40, 40, 40, 60, 60])
+    g_, b_, d_ = 14, 2, 20
+    ctx = pg.Context(n, mods, 2, galois_elts=[pg.elt_from_step(s, n) for s in range(1, g_ + 1)])
+    ws = ctx.workspace()
+    rng = np.random.default_rng(49)
+    gks = [pg.KeySwitchKey(pg.to_device(_key(rng, mods, ctx.dnum, n))) for _ in ctx.galois_elts]
+    one = torch.empty(ctx.bsgs_scratch_bytes(g_) // 8, dtype=torch.int64, device="cuda")
+    items, singles = [], []
+    for ch in (1, 3, 2):
+        l = ctx.level(ch)
+        t = pg.to_device(O.random_residues(rng, mods[:l], n, 2))
+        dg = pg.to_device(O.random_residues(rng, mods[:l], n, d_))
+        out = torch.empty((2, l - 1, n), dtype=torch.int64, device="cuda")
+        single = torch.empty_like(out)
+        ctx.bsgs_matvec(ws, one, t, ch, dg, d_, g_, b_, gks, single, hoisted=True)
+        items.append((t, ch, dg, out))
+        singles.append(single)
+    wsb = ctx.workspace(batch_items=len(items))
+    scratch = torch.empty(len(items) * ctx.bsgs_batch_scratch_bytes(g_, b_) // 8, dtype=torch.int64, device="cuda")
+    ctx.bsgs_matvec_batch(wsb, scratch, items, d_, g_, b_, gks)
+    for (t, ch, dg, out), single in zip(items, singles):
+        assert torch.equal(out, single), f"chain {ch}"
+    assert ctx.device_status() == 0
+
+
 def test_bsgs_batch_more_than_one_launch_set(lin, pg):
     """70 products (more than one launch set of 64, the second one reusing the first's scratch)
     give the single calls' words."""
