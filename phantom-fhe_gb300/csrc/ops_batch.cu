@@ -880,6 +880,7 @@ __global__ void __launch_bounds__(256) ks_inner_product_hoisted_batch(BItemsRef 
     const uint2 src = *reinterpret_cast<const uint2 *>(perm + idx);
     u128 a0{0, 0}, a1{0, 0}, b0{0, 0}, b1{0, 0};
     int terms = 0;
+#pragma unroll 2
     for (int d = 0; d < beta; d++) {
         uint64_t x0, x1;
         if (d == own_d) {
