@@ -1016,7 +1016,6 @@ void ckks_bsgs_matvec_batch(Context &c, uint64_t *ws_base, size_t item_words, ui
         for (int i = 0; i < count; i++) {
             const MatvecItem &m = items[base + i];
             const LevelTables &lt = *c.levels[m.l];
-            const size_t cw = 2 * ((size_t)m.l << c.log_n);
             r.it.l[i] = m.l;
             r.it.ws[i] = ws_base + (size_t)i * item_words;
             r.it.phi[i] = lt.part_hat_inv.as<uint64_t>();
@@ -1027,7 +1026,6 @@ void ckks_bsgs_matvec_batch(Context &c, uint64_t *ws_base, size_t item_words, ui
             mv.l[i] = m.l;
             mv.dl[i] = m.dl;
             cts[i] = m.ct;
-            (void)cw;
         }
         auto ptr_list = [&](const std::vector<const uint64_t *> &v) {
             PtrList pl{};
