@@ -63,3 +63,14 @@ def test_bad_arguments_return_status(lib):
     rc = lib.fhe_create_coeff_modulus(65536, (ctypes.c_int * 1)(70), 1, out)
     assert rc == -1 and b"invalid" in lib.fhe_last_error()
     assert lib.fhe_context_create(None, None) == -1
+
+
+def test_matvec_item_layout_and_batch_scratch_query(lib):
+    """The Python mirror of fhe_matvec_item has the C layout (three pointers, then chain_index and
+    diag_limbs as size_t), and the batch scratch query returns 0 for what it cannot size."""
+    import phantom_gb300 as pg
+    assert ctypes.sizeof(pg._MatvecItem) == 3 * ctypes.sizeof(ctypes.c_void_p) + 2 * ctypes.sizeof(ctypes.c_size_t)
+    assert [f for f, _ in pg._MatvecItem._fields_] == ["ct", "diags", "out", "chain_index", "diag_limbs"]
+    lib.fhe_bsgs_batch_scratch_bytes.restype = ctypes.c_size_t
+    lib.fhe_bsgs_batch_scratch_bytes.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t]
+    assert lib.fhe_bsgs_batch_scratch_bytes(None, 11, 12) == 0
