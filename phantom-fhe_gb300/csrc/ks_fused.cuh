@@ -11,16 +11,16 @@
 // never re-read; cx is written once.  The words equal the two-kernel form's (exact modular
 // arithmetic, the sum reduced every 7 terms as there).
 //
-// Layout per thread: the row pass's last register phase leaves each thread E = 8 coefficients in
-// runs of 2^K consecutive positions (the phase's smallest stride is 1), so the key words and the
-// cx stores are 16-byte accesses at those positions, and no shared-memory sweep follows the
+// Layout per thread: the row pass's last register phase leaves each thread E coefficients (4 or 8)
+// in runs of 2^K consecutive positions (the phase's smallest stride is 1), so the key words and
+// the cx stores are 16-byte accesses at those positions, and no shared-memory sweep follows the
 // transform.
 //
-// The accumulators (E coefficients x 2 polynomials x 128 bits a thread, 32 KB a CTA) live in
-// tensor memory, not in registers: thread t owns lane t of the CTA's 64 columns, one 16-column
-// chunk per pair of its coefficients.  Each digit loads a chunk (tcgen05.ld), adds the pair's four
-// products and stores it back (tcgen05.st), so 16 accumulator words are live at a time instead of
-// 64, and the transform runs at the occupancy of the plain row pass.
+// The accumulators (E coefficients x 2 polynomials x 128 bits a thread) live in tensor memory,
+// not in registers: thread t owns lane t of the CTA's 8 E columns, one 16-column chunk per pair of
+// its coefficients.  Each digit loads a chunk (tcgen05.ld), adds the pair's four products and
+// stores it back (tcgen05.st), so 16 accumulator words are live at a time instead of 8 E, and the
+// transform runs at the occupancy of the plain row pass.
 #pragma once
 #include "keyswitch.cuh"
 #include "ntt.cuh"
@@ -28,10 +28,21 @@
 
 namespace pfg {
 
-constexpr int kFusedE = 8;       // coefficients per thread
-constexpr int kFusedTile = 1024; // coefficients per CTA (128 threads)
-constexpr int kFusedCols = 64;   // tensor-memory columns per CTA: E x 2 polynomials x 4 words
-constexpr int kFusedCtas = 8;    // CTAs per SM: 8 x 64 columns fill the SM's 512
+// CTA shape for FE coefficients per thread (128 threads): 4 for single ciphertexts, 8 for batches
+// (measured: 4 per thread at 10 CTAs per SM took 125 us against 128 us at 8 per thread for one
+// ciphertext; the batch, whose grid runs every item's blocks of one key tile together, was 1-2 %
+// faster at 8 per thread).
+template <int FE>
+struct FusedShape {
+    static_assert(FE == 4 || FE == 8, "4 or 8 coefficients per thread");
+    static constexpr int kThreads = 128;
+    static constexpr int kTile = kThreads * FE;  // coefficients per CTA
+    static constexpr int kCols = FE * 2 * 4;     // tensor-memory columns: FE x 2 polynomials x 4 words
+    // CTAs per SM: 8 x 64 columns fill the SM's 512 at 8 per thread; at 4 per thread the register
+    // file bounds it (10 CTAs at 48 registers, 320 columns)
+    static constexpr int kCtas = FE == 8 ? 8 : 10;
+};
+constexpr int kFusedSingleE = 4, kFusedBatchE = 8;
 
 namespace tacc {
 // One warp's 32 lanes x 16 consecutive 32-bit columns, one lane per thread.
@@ -69,25 +80,25 @@ __device__ __forceinline__ void put(uint32_t (&r)[16], int k, const u128 &a) {
 }  // namespace tacc
 
 // Shared-memory words of one CTA: its tile as V = TILE / M padded vectors of M = 2^LM words.
-template <int LM>
+template <int LM, int FE>
 __host__ __device__ constexpr int fused_smem_words() {
-    return (kFusedTile >> LM) * ((1 << LM) + (1 << LM) / 16 + 1);
+    return (FusedShape<FE>::kTile >> LM) * ((1 << LM) + (1 << LM) / 16 + 1);
 }
 
 // One CTA's work: output limb jj (prime table index tbl) of the rows in tile `tile`, over every
 // digit d < beta.  tm and cx are the ciphertext's mod-up and accumulator buffers, sm the CTA's
 // shared tile, tacc the tensor-memory address of this thread's lane (column 0).
-template <int LM, class Own>
+template <int LM, int FE, class Own>
 __device__ __forceinline__ void modup_ip_tile(uint64_t *sm, uint32_t tacc, const NttTables &T, const uint64_t *tm,
                                               const Own &own, const uint64_t *const *evk, uint64_t *cx, int l, int nQ,
                                               int alpha, int beta, int qp, int jj, uint32_t tile) {
-    constexpr int E = kFusedE, TILE = kFusedTile;
+    constexpr int E = FE, TILE = FusedShape<FE>::kTile;
     constexpr int M = 1 << LM, TPV = M / E, V = TILE / M, VP = M + M / 16 + 1;
     using F = PhaseAt<LM, true, 0, E>;
     using L = PhaseAt<LM, true, F::NPH - 1, E>;
     constexpr int LG = E >> L::K, LS = 1 << L::K;  // last phase: groups per thread, group size
     static_assert(LS % 2 == 0, "the last phase pairs consecutive positions");
-    static_assert(V * VP == fused_smem_words<LM>(), "shared tile size");
+    static_assert(V * VP == fused_smem_words<LM, FE>(), "shared tile size");
     const int log_n = T.log_n;
     const int qlp = l + alpha;
     const int tbl = jj < l ? jj : nQ + (jj - l);
@@ -177,13 +188,13 @@ __device__ __forceinline__ void modup_ip_tile(uint64_t *sm, uint32_t tacc, const
         }
 }
 
-// The CTA's tensor-memory columns: allocated by warp 0 after the grid dependency wait (so no CTA
-// holds columns while it waits on another grid), freed once every thread's accesses are done.
+// The CTA's COLS tensor-memory columns: allocated by warp 0 after the grid dependency wait (so no
+// CTA holds columns while it waits on another grid), freed once every thread's accesses are done.
 // Eight CTAs of 64 columns fill an SM; a ninth would wait in the allocation until one finishes.
+template <int COLS>
 struct FusedTmem {
-    uint32_t base;
     __device__ __forceinline__ static uint32_t alloc(uint32_t *slot) {
-        if (threadIdx.x < 32) tc::tmem_alloc(slot, kFusedCols);
+        if (threadIdx.x < 32) tc::tmem_alloc(slot, COLS);
         tc::fence_before();
         __syncthreads();
         tc::fence_after();
@@ -194,7 +205,7 @@ struct FusedTmem {
         __syncthreads();
         if (threadIdx.x < 32) {
             tc::fence_after();
-            tc::tmem_free(base, kFusedCols);
+            tc::tmem_free(base, COLS);
         }
     }
     // this thread's lane: warp w reads and writes lanes 32 w .. 32 w + 31
@@ -203,19 +214,21 @@ struct FusedTmem {
     }
 };
 
-// One ciphertext: grid (N / TILE row tiles, l + alpha output limbs).
+// One ciphertext: grid (N / TILE row tiles, l + alpha output limbs), kFusedSingleE per thread.
 template <int LM, class Own>
-__global__ void __launch_bounds__(kFusedTile / kFusedE, kFusedCtas)
+__global__ void __launch_bounds__(FusedShape<kFusedSingleE>::kThreads, FusedShape<kFusedSingleE>::kCtas)
         ks_modup_ip(NttTables T, const uint64_t *tm, Own own, const uint64_t *const *evk, uint64_t *cx, int l,
                     int nQ, int alpha, int beta, int qp) {
+    using S = FusedShape<kFusedSingleE>;
+    using TM = FusedTmem<S::kCols>;
     pdl_wait();
     pdl_release();
-    __shared__ uint64_t sm[fused_smem_words<LM>()];
+    __shared__ uint64_t sm[fused_smem_words<LM, kFusedSingleE>()];
     __shared__ uint32_t tslot;
-    const uint32_t tbase = FusedTmem::alloc(&tslot);
-    modup_ip_tile<LM>(sm, FusedTmem::lane(tbase), T, tm, own, evk, cx, l, nQ, alpha, beta, qp, (int)blockIdx.y,
-                      blockIdx.x);
-    FusedTmem::free(tbase);
+    const uint32_t tbase = TM::alloc(&tslot);
+    modup_ip_tile<LM, kFusedSingleE>(sm, TM::lane(tbase), T, tm, own, evk, cx, l, nQ, alpha, beta, qp,
+                                     (int)blockIdx.y, blockIdx.x);
+    TM::free(tbase);
 }
 
 }  // namespace pfg

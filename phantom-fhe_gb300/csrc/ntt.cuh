@@ -43,10 +43,10 @@ constexpr int kTileElems = 4096;  // V * M coefficients per CTA
 // and 1024 at E = 8, 128 threads).
 template <int E, int TILE = kTileElems>
 struct NttShape {
-    static_assert(E == 8 || E == 16, "8 or 16 coefficients per thread");
+    static_assert(E == 4 || E == 8 || E == 16, "4, 8 or 16 coefficients per thread");
     static_assert(TILE == kTileElems || TILE == kTileElems / 2 || TILE == kTileElems / 4,
                   "4096, 2048 or 1024 coefficients per tile");
-    static constexpr int LGE = E == 16 ? 4 : 3;
+    static constexpr int LGE = E == 16 ? 4 : E == 8 ? 3 : 2;
     static constexpr int kThreads = TILE / E;
     // 80 registers a thread at 16 per thread, 64 at 8
     static constexpr int kMinBlocks = (E == 16 ? 3 : 2) * (kTileElems / TILE);

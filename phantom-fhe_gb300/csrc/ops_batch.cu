@@ -418,21 +418,22 @@ struct BatchOwn {
 // dropped q_tk.  The item index is the fastest grid dimension, so the blocks of all items that
 // read the same key tile (tk, tile) run together and the key comes from HBM once per batch.
 template <int LM>
-__global__ void __launch_bounds__(kFusedTile / kFusedE, kFusedCtas)
+__global__ void __launch_bounds__(FusedShape<kFusedBatchE>::kThreads, FusedShape<kFusedBatchE>::kCtas)
         ks_modup_ip_batch(BItemsRef r, NttTables T, const uint64_t *const *evk, int nQ, int qp) {
+    using TM = FusedTmem<FusedShape<kFusedBatchE>::kCols>;
     pdl_wait();
     pdl_release();
-    __shared__ uint64_t sm[fused_smem_words<LM>()];
+    __shared__ uint64_t sm[fused_smem_words<LM, kFusedBatchE>()];
     __shared__ uint32_t tslot;
     const int c = (int)blockIdx.x, tk = (int)blockIdx.z, l = r.it.l[c], alpha = r.alpha, log_n = r.log_n;
     if (tk < nQ && tk >= l) return;  // uniform per block, before any barrier or allocation
     const int jj = tk < nQ ? tk : l + (tk - nQ);
     uint64_t *ws = r.it.ws[c];
     const BatchOwn own{r.it.a[c], r.it.b[c], (long long)l << log_n, r.it.keyswitch, log_n};
-    const uint32_t tbase = FusedTmem::alloc(&tslot);
-    modup_ip_tile<LM>(sm, FusedTmem::lane(tbase), T, ws + r.sl.tm, own, evk, ws + r.sl.cx, l, nQ, alpha,
-                      (l + alpha - 1) / alpha, qp, jj, blockIdx.y);
-    FusedTmem::free(tbase);
+    const uint32_t tbase = TM::alloc(&tslot);
+    modup_ip_tile<LM, kFusedBatchE>(sm, TM::lane(tbase), T, ws + r.sl.tm, own, evk, ws + r.sl.cx, l, nQ, alpha,
+                                    (l + alpha - 1) / alpha, qp, jj, blockIdx.y);
+    TM::free(tbase);
 }
 
 // Rescale-folded mod-down conversion for (item, poly) = block row (see rescale_fused_bconv).
@@ -579,14 +580,15 @@ static void batch_modup_ntt_inner_product(const Context &c, const BItemsRef &r, 
     BScratch<1> tm{r};
     if (c.ks_fused_batch) {
         col_pass<true, false>(c, mm.pre.p[count], mm, tm, tm, s);
-        const dim3 grid((unsigned)count, (unsigned)(c.n / kFusedTile), (unsigned)(nQ + alpha));
+        using S = FusedShape<kFusedBatchE>;
+        const dim3 grid((unsigned)count, (unsigned)(c.n / S::kTile), (unsigned)(nQ + alpha));
         const NttTables T = c.ntt();
         count_launch();
         switch (c.l2()) {
-            case 6: launch_pdl(c.pdl, ks_modup_ip_batch<6>, grid, dim3(kFusedTile / kFusedE), 0, s, r, T, evk, nQ, nQ + alpha); break;
-            case 7: launch_pdl(c.pdl, ks_modup_ip_batch<7>, grid, dim3(kFusedTile / kFusedE), 0, s, r, T, evk, nQ, nQ + alpha); break;
-            case 8: launch_pdl(c.pdl, ks_modup_ip_batch<8>, grid, dim3(kFusedTile / kFusedE), 0, s, r, T, evk, nQ, nQ + alpha); break;
-            case 9: launch_pdl(c.pdl, ks_modup_ip_batch<9>, grid, dim3(kFusedTile / kFusedE), 0, s, r, T, evk, nQ, nQ + alpha); break;
+            case 6: launch_pdl(c.pdl, ks_modup_ip_batch<6>, grid, dim3(S::kThreads), 0, s, r, T, evk, nQ, nQ + alpha); break;
+            case 7: launch_pdl(c.pdl, ks_modup_ip_batch<7>, grid, dim3(S::kThreads), 0, s, r, T, evk, nQ, nQ + alpha); break;
+            case 8: launch_pdl(c.pdl, ks_modup_ip_batch<8>, grid, dim3(S::kThreads), 0, s, r, T, evk, nQ, nQ + alpha); break;
+            case 9: launch_pdl(c.pdl, ks_modup_ip_batch<9>, grid, dim3(S::kThreads), 0, s, r, T, evk, nQ, nQ + alpha); break;
             default: throw std::logic_error("unsupported NTT split");
         }
         return;

@@ -208,7 +208,8 @@ template <class Own>
 static void modup_row_inner_product(const Context &c, const KsBuffers &b, Own own, int l, const uint64_t *const *evk,
                                     cudaStream_t s) {
     const int alpha = c.nP, qlp = l + alpha;
-    const dim3 grid((unsigned)(c.n / kFusedTile), (unsigned)qlp), block(kFusedTile / kFusedE);
+    using S = FusedShape<kFusedSingleE>;
+    const dim3 grid((unsigned)(c.n / S::kTile), (unsigned)qlp), block(S::kThreads);
     const NttTables T = c.ntt();
     const uint64_t *tm = b.tm;
     count_launch();
